@@ -1,0 +1,391 @@
+#!/usr/bin/env python
+"""Particle-steps/s of CUBE's per-step gravity/update path on one GB300.
+
+Workload ``cdm512``: 512^3 CDM particles, 600 Mpc/h, coarse mesh 256^3, fine
+mesh 1024^3 (2^3 tiles of the reference), PP within +-1 fine cell with
+rsoft=0.1, int8 positions / int16 velocities, Zel'dovich initial conditions at
+z=49 from the Eisenstein-Hu no-wiggle spectrum (synthetic, seeded).
+
+One step is the reference's loop body (CUBEnu/work/main/main.f90:102-118):
+timestep (host) -> update_x -> buffer_grid -> buffer_x -> ext_pp_force ->
+particle_mesh -> buffer_v, every call through the C ABI of libcube_gb300.so.
+
+``value``: N*K / device time of K steps (CUDA events on the library's
+stream), state resident in HBM.  ``e2e``: the same metric when every step also
+uploads the state from pinned host arrays and downloads it again (what a host
+caller holding the reference's arrays pays).  ``--impl reference`` times the
+reference's CPU algorithm (the oracle restatement, OpenMP on every host core)
+on a one-tile sample per step.  ``--gpus N`` runs N independent replicas
+(the path does not shard on one-GPU machines); value sums them, time is the max.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s at 512^3 PM+PP"
+UNIT = "particle-steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="cdm512")
+    ap.add_argument("--z", type=float, default=49.0)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--e2e-steps", type=int, default=0)
+    return ap.parse_args()
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    lrank = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    return ws, rank, lrank
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce_max(x, ws, device):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allreduce_sum(x, ws, device):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.f = tempfile.NamedTemporaryFile(mode="w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.flush()
+        rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ gb300 arm
+
+
+def algorithmic_bytes(p, n):
+    """Algorithmic bytes per launch of each phase (each array element read or
+    written once; s = 3*izipx+3*izipv bytes of particle code)."""
+    nf3, nc3 = p.nf ** 3, p.nc ** 3
+    hf = (p.nf // 2 + 1) * p.nf * p.nf
+    hc = (p.nc // 2 + 1) * p.nc * p.nc
+    s = 3 * p.izipx + 3 * p.izipv
+    cell = 4 + 4  # rhoc + cell start (int32 index, int32 count)
+    return {
+        "update_dest": n * (s + 4) + n * 5,                 # read x,v,cell; write dest+frame
+        "update_rank": n * (5 + 3 * p.izipv) + nc3 * (cell + 12 + 4 + 12),
+        "update_scan": nc3 * (4 + 8),
+        "update_scatter": n * (s + 4 + 4 + 4 + 5) + n * (s + 4 + 4),
+        "update_sigma": n * (3 * p.izipv + 4) + nc3 * 12,
+        "pp_force": n * (3 * p.izipx + 2 * 3 * p.izipv + 4),
+        "fine_deposit": n * (3 * p.izipx + 4) + 4 * nf3,
+        "fine_r2c": 4 * nf3 + 8 * hf,
+        "fine_green": 8 * hf + 12 * hf + 3 * 8 * hf,
+        "fine_c2r": 3 * (8 * hf + 4 * nf3),
+        "fine_f2max": 12 * nf3,
+        "fine_kick": n * (3 * p.izipx + 2 * 3 * p.izipv + 4) + 12 * nf3,
+        "coarse_deposit": n * (3 * p.izipx + 4) + 4 * nc3,
+        "coarse_fft": (4 * nc3 + 8 * hc) + (8 * hc + 12 * hc + 24 * hc) + 3 * (8 * hc + 4 * nc3) + 12 * nc3,
+        "coarse_kick": n * (3 * p.izipx + 2 * 3 * p.izipv + 4 + 12) + 12 * nc3,
+    }
+
+
+def run_gb300(args, ws, rank, lrank):
+    import torch
+
+    from cafproject_gb300 import cube as C
+    from cafproject_gb300 import ic, params as P
+    from cafproject_gb300.cosmology import TimeState
+
+    torch.cuda.set_device(lrank)
+    dev = torch.device("cuda", lrank)
+    p = P.WORKLOADS[args.workload]()
+    t_ic = time.perf_counter()
+    st = ic.zeldovich(p, args.z, args.seed + rank, device=dev)
+    host = {k: st[k].cpu().numpy() for k in ("xp", "vp", "pid", "rhoc", "vfield")}
+    sigma, a0, vm = st["sigma_vi"], st["a"], st["vmax"]
+    del st
+    torch.cuda.empty_cache()
+    t_ic = time.perf_counter() - t_ic
+    g = C.CubeGPU(p, device=lrank)
+    g.upload(host["xp"], host["vp"], host["pid"], host["rhoc"], host["vfield"])
+    g.set_sigma(sigma, sigma)
+    ts = TimeState(a=np.float32(a0), omega_m=p.omega_m, omega_l=p.omega_l, z_checkpoints=[0.0])
+    ts.vz_max = np.float32(vm[2])
+    ts.dt_vmax = np.float32(np.float32(18.0) / np.float32(max(vm)))
+    stream = torch.cuda.ExternalStream(g.stream())
+
+    def step():
+        dt, a_mid = ts.timestep()
+        g.update_x(ts.dt_old, dt, ts.vz_max)
+        g.buffer_grid()
+        g.buffer_x()
+        pps = g.ext_pp_force(a_mid, dt) if p.pp_on else None
+        pms = g.particle_mesh(a_mid, dt)
+        g.buffer_v()
+        ts.constrain(pms, pps, p.ncell)
+        return pms
+
+    for _ in range(args.warmup):
+        step()
+    g.synchronize()
+    n0 = g.nplocal()
+    clocks = ClockSampler(lrank)
+    barrier(ws)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g.synchronize()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    g.synchronize()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    barrier(ws)
+    ms_max = allreduce_max(ms, ws, dev)
+    ntot = allreduce_sum(float(n0), ws, dev)
+    value = ntot * args.steps / (ms_max / 1000.0)
+
+    # per-phase device time (timers on, a separate pass so the headline is unperturbed)
+    g.timing(True)
+    kph = max(1, min(args.steps, 3))
+    for _ in range(kph):
+        step()
+    tphase = g.timing_read()
+    g.timing(False)
+    ab = algorithmic_bytes(p, n0)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    phases = {}
+    for name, (tms, cnt) in tphase.items():
+        if cnt == 0:
+            continue
+        per = tms / cnt
+        gbs = ab.get(name, 0) / (per / 1000.0) / 1e9 if per > 0 else 0.0
+        phases[name] = {"ms_per_launch": round(per, 4), "launches": int(cnt), "share": 0.0,
+                        "algo_bytes": int(ab.get(name, 0)), "achieved_gbs": round(gbs, 1)}
+    tot = sum(v["ms_per_launch"] * v["launches"] for v in phases.values())
+    for v in phases.values():
+        v["share"] = round(v["ms_per_launch"] * v["launches"] / tot, 4) if tot else 0.0
+    own = {k: v for k, v in phases.items() if k not in ("fine_r2c", "fine_c2r", "coarse_fft")}
+    dom = max(own, key=lambda k: own[k]["ms_per_launch"] * own[k]["launches"]) if own else None
+    roof = None
+    if dom:
+        d = phases[dom]
+        roof = {"kernel": dom, "bound": "hbm", "achieved": d["achieved_gbs"], "peak": hbm, "unit": "GB/s",
+                "frac": round(d["achieved_gbs"] / hbm, 4), "peak_source": peak_src,
+                "traffic": None, "algo_bytes_per_launch": d["algo_bytes"]}
+
+    # e2e: host arrays in, host arrays out, every step
+    ke = args.e2e_steps or max(1, min(args.steps, 3))
+    pin = {k: torch.from_numpy(v).pin_memory() for k, v in g.download().items()}
+    hin = {k: v.numpy() for k, v in pin.items()}
+    outt = {k: torch.empty_like(v).pin_memory() for k, v in pin.items()}
+    out = {k: v.numpy() for k, v in outt.items()}
+    h2d = sum(v.nbytes for v in hin.values())
+    barrier(ws)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        g.upload(hin["xp"], hin["vp"], hin["pid"], hin["rhoc"], hin["vfield"])
+        step()
+        g.download(out=out)
+    torch.cuda.synchronize()
+    te = time.perf_counter() - t0
+    te = allreduce_max(te, ws, dev)
+    e2e = {"value": ntot * ke / te, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(h2d),
+           "steps": ke}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        cpu = cpu_baseline(p, g.download(), float(g.get_sigma()[0]), ts)
+    g.close()
+    return dict(value=value, ms=ms_max / args.steps, clocks=clk, phases=phases, roofline=roof, e2e=e2e,
+                cpu=cpu, n=int(ntot), p=p, t_ic=t_ic, gpu_launches=gpu_launches(p, args.steps))
+
+
+def gpu_launches(p, steps):
+    """Launches of this library's kernels per step (cuFFT kernels not counted)."""
+    upd = 2 + 3 + 1 + 1        # dest, rank, scan x3, scatter, sigma
+    pp = 1 if p.pp_on else 0
+    fine = 1 + 1 + 1 + 1       # deposit, green, f2max, kick
+    coarse = 1 + 1 + 1 + 1
+    dec = 1                    # decode table when sigma changes
+    return steps * (upd + pp + fine + coarse + dec)
+
+
+def cpu_baseline(p, state, sigma, ts):
+    from oracle import cube_oracle as O
+    ncore = os.cpu_count() or 1
+    r = O.time_sample(p, state, sigma, float(ts.a_mid), float(ts.dt), float(ts.dt_old), float(ts.vz_max),
+                      tile=0, nthreads=0)
+    n = state["xp"].shape[0]
+    return {"value": n / r["step_estimate"], "unit": UNIT, "cores": ncore, "kind": "port",
+            "sample": "one of %d tiles of update_xp, PP and fine PM plus the image-wide buffering and coarse PM "
+                      "(%.1f s of CPU work); step = %d x tile + image-wide" % (p.nnt ** 3, r["sampled"],
+                                                                                p.nnt ** 3),
+            "detail": {k: round(v, 3) for k, v in r.items()}}
+
+
+# -------------------------------------------------------------- reference arm
+
+
+def run_reference(args, ws, rank):
+    """The reference's CPU algorithm (oracle restatement, all host cores) on
+    the same workload; each step is a one-tile sample scaled to a full step."""
+    if rank != 0:
+        return None
+    import torch
+
+    from cafproject_gb300 import ic, params as P
+    from cafproject_gb300.cosmology import TimeState
+    from oracle import cube_oracle as O
+
+    p = P.WORKLOADS[args.workload]()
+    dev = torch.device("cuda", 0) if torch.cuda.is_available() else torch.device("cpu")
+    st = ic.zeldovich(p, args.z, args.seed, device=dev)
+    state = {k: st[k].cpu().numpy() for k in ("xp", "vp", "pid", "rhoc", "vfield")}
+    sigma, a0, vm = st["sigma_vi"], st["a"], st["vmax"]
+    del st
+    ts = TimeState(a=np.float32(a0), omega_m=p.omega_m, omega_l=p.omega_l)
+    ts.vz_max = np.float32(vm[2])
+    ts.dt_vmax = np.float32(np.float32(18.0) / np.float32(max(vm)))
+    n = state["xp"].shape[0]
+    ests, samples = [], []
+    for i in range(args.warmup + args.steps):
+        dt, a_mid = ts.timestep()
+        r = O.time_sample(p, state, sigma, float(a_mid), float(dt), float(ts.dt_old), float(ts.vz_max), tile=0,
+                          nthreads=0)
+        if i >= args.warmup:
+            ests.append(r["step_estimate"])
+            samples.append(r["sampled"])
+    value = n * len(ests) / sum(ests)
+    return dict(value=value, ms=1000.0 * sum(ests) / len(ests), n=n, p=p, sample=sum(samples) / len(samples))
+
+
+def main():
+    args = parse()
+    ws, rank, lrank = dist_init()
+    if args.impl == "reference":
+        r = run_reference(args, ws, rank)
+        if rank == 0:
+            ncore = os.cpu_count() or 1
+            p = r["p"]
+            line = {"impl": "reference", "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": args.gpus,
+                    "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms"], "higher_is_better": True,
+                    "scaling": "weak", "vs_baseline": None, "dtype": "int8/int16 state, fp32/fp64 arithmetic",
+                    "data": "synthetic (seeded Zel'dovich ICs, Eisenstein-Hu no-wiggle P(k), z=%g)" % args.z,
+                    "config": {"workload": args.workload, "particles": r["n"], "nc": p.nc, "nf": p.nf,
+                               "nnt": p.nnt, "pp": bool(p.pp_on), "parallelism": "host OpenMP"},
+                    "cpu_baseline": {"value": r["value"], "unit": UNIT, "cores": ncore, "kind": "port",
+                                     "sample": "one of %d tiles per step (%.1f s sampled), scaled by the tile count"
+                                               % (p.nnt ** 3, r["sample"])},
+                    "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            print(json.dumps(line), flush=True)
+        return
+    r = run_gb300(args, ws, rank, lrank)
+    if rank == 0:
+        p = r["p"]
+        line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": r["ms"], "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "int8/int16 state, fp32 mesh, fp64 velocity codes",
+                "data": "synthetic (seeded Zel'dovich ICs, Eisenstein-Hu no-wiggle P(k), z=%g)" % args.z,
+                "config": {"workload": args.workload, "particles": r["n"], "nc": p.nc, "nf": p.nf, "nnt": p.nnt,
+                           "pp": bool(p.pp_on), "rsoft": p.rsoft, "izipx": p.izipx, "izipv": p.izipv,
+                           "parallelism": "replicas x%d" % ws if ws > 1 else "single GPU",
+                           "l2": "inputs larger than L2 (state 1.7 GB, meshes 4.3 GB each)"},
+                "clocks": r["clocks"], "e2e": r["e2e"], "roofline": r["roofline"], "gpu_launches": r["gpu_launches"],
+                "phases": r["phases"]}
+        if r["cpu"]:
+            line["cpu_baseline"] = r["cpu"]
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,336 @@
+// cube_api.cu -- the C ABI (include/cube_gpu.h): context life cycle, state
+// transfer, field inspection, and the entry points that replace the bodies of
+// the reference subroutines update_x, ext_pp_force and particle_mesh.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "cube_internal.cuh"
+
+int cube_fail(cube_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+int cube_grid(int64_t work, int block, int max_blocks_per_sm) {
+  static int nsm = 0;
+  if (nsm == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (nsm <= 0) nsm = 152;
+  }
+  int64_t need = (work + block - 1) / block;
+  int64_t cap = (int64_t)nsm * max_blocks_per_sm;
+  if (need < 1) need = 1;
+  return (int)(need < cap ? need : cap);
+}
+
+static int alloc(cube_ctx* c, void** p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+  if (e != cudaSuccess) {
+    return cube_fail(c, CUBE_ERR_NOMEM, std::string("cudaMalloc of ") + std::to_string(bytes) +
+                                            " bytes failed: " + cudaGetErrorString(e));
+  }
+  return CUBE_OK;
+}
+#define ALLOC(ptr, bytes)                                  \
+  do {                                                     \
+    int r_ = alloc(c, (void**)&(ptr), (size_t)(bytes));    \
+    if (r_) return r_;                                     \
+  } while (0)
+
+static void release(cube_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  cube_timers_free(c);
+  void* bufs[] = {c->xp[0], c->xp[1], c->vp[0], c->vp[1], c->pid[0], c->pid[1], c->pcell[0], c->pcell[1],
+                  c->rhoc[0], c->rhoc[1],
+                  c->vfield[0], c->vfield[1], c->cstart[0], c->cstart[1], c->dest, c->dframe, c->rank, c->xtra,
+                  c->scan_tmp, c->red_tmp, c->tan_tab, c->dec_old, c->dec_new, c->rho_f, c->force_f[0],
+                  c->force_f[1], c->force_f[2], c->kern_f, c->kern_f_raw, c->rho_c, c->force_c[0],
+                  c->force_c[1], c->force_c[2], c->kern_c, c->fpp, c->dstats, c->cufft_work};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  if (c->hstats) cudaFreeHost(c->hstats);
+  if (c->plan_f_r2c) cufftDestroy(c->plan_f_r2c);
+  if (c->plan_f_c2r) cufftDestroy(c->plan_f_c2r);
+  if (c->plan_c_r2c) cufftDestroy(c->plan_c_r2c);
+  if (c->plan_c_c2r) cufftDestroy(c->plan_c_c2r);
+  if (c->stream) cudaStreamDestroy(c->stream);
+}
+
+static int make_plans(cube_ctx* c) {
+  // fine: nf^3 in place, FFTW-compatible padded layout; one shared work area
+  size_t wf1 = 0, wf2 = 0, wc1 = 0, wc2 = 0;
+  int nf = c->nf, nc = c->p.nc;
+  CUBE_FFT(c, cufftCreate(&c->plan_f_r2c));
+  CUBE_FFT(c, cufftCreate(&c->plan_f_c2r));
+  CUBE_FFT(c, cufftCreate(&c->plan_c_r2c));
+  CUBE_FFT(c, cufftCreate(&c->plan_c_c2r));
+  for (cufftHandle h : {c->plan_f_r2c, c->plan_f_c2r, c->plan_c_r2c, c->plan_c_c2r})
+    CUBE_FFT(c, cufftSetAutoAllocation(h, 0));
+  CUBE_FFT(c, cufftMakePlan3d(c->plan_f_r2c, nf, nf, nf, CUFFT_R2C, &wf1));
+  CUBE_FFT(c, cufftMakePlan3d(c->plan_f_c2r, nf, nf, nf, CUFFT_C2R, &wf2));
+  CUBE_FFT(c, cufftMakePlan3d(c->plan_c_r2c, nc, nc, nc, CUFFT_R2C, &wc1));
+  CUBE_FFT(c, cufftMakePlan3d(c->plan_c_c2r, nc, nc, nc, CUFFT_C2R, &wc2));
+  size_t w = wf1;
+  for (size_t x : {wf2, wc1, wc2})
+    if (x > w) w = x;
+  c->cufft_work_bytes = w;
+  ALLOC(c->cufft_work, w);
+  for (cufftHandle h : {c->plan_f_r2c, c->plan_f_c2r, c->plan_c_r2c, c->plan_c_c2r}) {
+    CUBE_FFT(c, cufftSetWorkArea(h, c->cufft_work));
+    CUBE_FFT(c, cufftSetStream(h, c->stream));
+  }
+  return CUBE_OK;
+}
+
+extern "C" int cube_create(const cube_params* p, const float* fine_table, const float* coarse_table, int device,
+                           cube_ctx** out) {
+  if (!p || !out || !fine_table || !coarse_table) return CUBE_ERR_ARG;
+  *out = nullptr;
+  cube_ctx* c = new (std::nothrow) cube_ctx();
+  if (!c) return CUBE_ERR_NOMEM;
+  c->p = *p;
+  c->device = device;
+  auto bad = [&](const char* m) {
+    c->err = m;
+    *out = c;
+    return CUBE_ERR_ARG;
+  };
+  if (p->nc <= 0 || p->nnt <= 0 || p->nc % p->nnt) return bad("nc must be a positive multiple of nnt");
+  // LRCKCORR rescales the coarse modes with |k|<=8 by 1/Im FFT(raw kernel)
+  // (kernel_c.f90:111-113); at nc<=16 that sphere reaches the Nyquist plane,
+  // where the odd kernel's transform is zero.
+  if (p->nc <= 16) return bad("nc must exceed 16 (coarse kernel correction needs |k|<=8 below Nyquist)");
+  if (p->ncell != 4) return bad("ncell must be 4");
+  if (p->izipx < 1 || p->izipx > 2 || p->izipv < 1 || p->izipv > 2) return bad("izipx/izipv must be 1 or 2");
+  c->nt = p->nc / p->nnt;
+  if (c->nt < 2 * p->ncb) return bad("nt must be at least 2*ncb");
+  if (p->nf_cutoff >= p->ncb * p->ncell) return bad("nf_cutoff must be below the tile buffer nfb");
+  if (p->pp_range != 1 && p->pp_on) return bad("pp_range must be 1");
+  if (p->np_max <= 0) return bad("np_max must be positive");
+  if (p->ncb < 1 || p->ncb > 8) return bad("ncb must be in 1..8");
+  c->nf = p->nc * p->ncell;
+  c->ntiles = p->nnt * p->nnt * p->nnt;
+  c->ncells = (int64_t)p->nc * p->nc * p->nc;
+  c->nfine = (int64_t)c->nf * c->nf * c->nf;
+  c->nvbin = 1 << (8 * p->izipv);
+  *out = c;
+  CUBE_CUDA(c, cudaSetDevice(device));
+  CUBE_CUDA(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  int64_t np = p->np_max;
+  for (int k = 0; k < 2; k++) {
+    ALLOC(c->xp[k], 3 * np * p->izipx);
+    ALLOC(c->vp[k], 3 * np * p->izipv);
+    ALLOC(c->pid[k], 4 * np);
+    ALLOC(c->pcell[k], 4 * np);
+    ALLOC(c->rhoc[k], 4 * c->ncells);
+    ALLOC(c->vfield[k], 12 * c->ncells);
+    ALLOC(c->cstart[k], 8 * (c->ncells + 1));
+  }
+  ALLOC(c->dest, 4 * np);
+  ALLOC(c->dframe, np);
+  ALLOC(c->rank, 4 * np);
+  c->xtra_cap = 1 << 20;
+  ALLOC(c->xtra, sizeof(int4) * c->xtra_cap);
+  c->scan_tmp_bytes = 8 * (c->ncells / 256 + 1024);
+  ALLOC(c->scan_tmp, c->scan_tmp_bytes);
+  c->red_blocks = 2048;
+  ALLOC(c->red_tmp, sizeof(double) * 4 * c->red_blocks);
+  ALLOC(c->tan_tab, 4 * c->nvbin);
+  ALLOC(c->dec_old, 8 * c->nvbin);
+  ALLOC(c->dec_new, 8 * c->nvbin);
+  int64_t nfh = (int64_t)(c->nf / 2 + 1);
+  int64_t fpad = 2 * nfh * c->nf * (int64_t)c->nf;  // floats of a padded fine mesh
+  ALLOC(c->rho_f, 4 * fpad);
+  for (int d = 0; d < 3; d++) ALLOC(c->force_f[d], 4 * fpad);
+  ALLOC(c->kern_f, 4 * 3 * nfh * c->nf * (int64_t)c->nf);
+  int64_t nch = (int64_t)(p->nc / 2 + 1);
+  int64_t cpad = 2 * nch * p->nc * (int64_t)p->nc;
+  ALLOC(c->rho_c, 4 * cpad);
+  for (int d = 0; d < 3; d++) ALLOC(c->force_c[d], 4 * cpad);
+  ALLOC(c->kern_c, 4 * 3 * nch * p->nc * (int64_t)p->nc);
+  ALLOC(c->dstats, sizeof(DevStats));
+  CUBE_CUDA(c, cudaMallocHost((void**)&c->hstats, sizeof(DevStats)));
+  int r = make_plans(c);
+  if (r) return r;
+  r = cube_build_tables(c);
+  if (r) return r;
+  r = cube_kernels_init(c, fine_table, coarse_table);
+  if (r) return r;
+  CUBE_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CUBE_OK;
+}
+
+extern "C" int cube_destroy(cube_ctx* c) {
+  if (!c) return CUBE_ERR_ARG;
+  release(c);
+  delete c;
+  return CUBE_OK;
+}
+
+extern "C" const char* cube_last_error(const cube_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+extern "C" int cube_upload_state(cube_ctx* c, int64_t nplocal, const void* xp, const void* vp, const int32_t* pid,
+                                 const int32_t* rhoc, const float* vfield) {
+  if (!c || !xp || !vp || !rhoc || !vfield || nplocal < 0) return CUBE_ERR_ARG;
+  if (nplocal > c->p.np_max) return cube_fail(c, CUBE_ERR_IMAGE_OVERFLOW, "nplocal exceeds np_max");
+  CUBE_CUDA(c, cudaSetDevice(c->device));
+  return cube_state_in(c, nplocal, xp, vp, pid, rhoc, vfield);
+}
+
+extern "C" int cube_download_state(cube_ctx* c, int64_t* nplocal, void* xp, void* vp, int32_t* pid, int32_t* rhoc,
+                                   float* vfield) {
+  if (!c) return CUBE_ERR_ARG;
+  if (!c->have_state) return cube_fail(c, CUBE_ERR_STATE, "no state uploaded");
+  CUBE_CUDA(c, cudaSetDevice(c->device));
+  return cube_state_out(c, nplocal, xp, vp, pid, rhoc, vfield);
+}
+
+extern "C" int cube_set_sigma(cube_ctx* c, float s, float sn) {
+  if (!c) return CUBE_ERR_ARG;
+  c->sigma_vi = s;
+  c->sigma_vi_new = sn;
+  return CUBE_OK;
+}
+
+extern "C" int cube_get_sigma(const cube_ctx* c, float* s, float* sn) {
+  if (!c) return CUBE_ERR_ARG;
+  if (s) *s = c->sigma_vi;
+  if (sn) *sn = c->sigma_vi_new;
+  return CUBE_OK;
+}
+
+static int check_ready(cube_ctx* c) {
+  if (!c) return CUBE_ERR_ARG;
+  if (!c->have_state) return cube_fail(c, CUBE_ERR_STATE, "no state uploaded");
+  CUBE_CUDA(c, cudaSetDevice(c->device));
+  return CUBE_OK;
+}
+
+extern "C" int cube_update_x(cube_ctx* c, float dt_old, float dt, float vz_max, cube_stats* st) {
+  int r = check_ready(c);
+  if (r) return r;
+  return cube_update_x_impl(c, dt_old, dt, vz_max, st);
+}
+
+extern "C" int cube_buffer_grid(cube_ctx* c) { return check_ready(c); }
+extern "C" int cube_buffer_x(cube_ctx* c) { return check_ready(c); }
+extern "C" int cube_buffer_v(cube_ctx* c) { return check_ready(c); }
+
+extern "C" int cube_pp_force(cube_ctx* c, float a_mid, float dt, cube_stats* st) {
+  int r = check_ready(c);
+  if (r) return r;
+  return cube_pp_impl(c, a_mid, dt, st);
+}
+
+extern "C" int cube_pm_fine_density(cube_ctx* c, cube_stats* st) {
+  int r = check_ready(c);
+  if (r) return r;
+  return cube_fine_density_impl(c, st);
+}
+extern "C" int cube_pm_coarse_density(cube_ctx* c, cube_stats* st) {
+  int r = check_ready(c);
+  if (r) return r;
+  return cube_coarse_density_impl(c, st);
+}
+extern "C" int cube_pm_fine_forces(cube_ctx* c, cube_stats* st) {
+  int r = check_ready(c);
+  if (r) return r;
+  return cube_fine_forces_impl(c, st);
+}
+extern "C" int cube_pm_fine_kick(cube_ctx* c, float a_mid, float dt) {
+  int r = check_ready(c);
+  if (r) return r;
+  return cube_fine_kick_impl(c, a_mid, dt);
+}
+extern "C" int cube_pm_coarse_forces(cube_ctx* c, cube_stats* st) {
+  int r = check_ready(c);
+  if (r) return r;
+  return cube_coarse_forces_impl(c, st);
+}
+extern "C" int cube_pm_coarse_kick(cube_ctx* c, float a_mid, float dt, cube_stats* st) {
+  int r = check_ready(c);
+  if (r) return r;
+  return cube_coarse_kick_impl(c, a_mid, dt, st);
+}
+
+extern "C" int cube_particle_mesh(cube_ctx* c, float a_mid, float dt, cube_stats* st) {
+  int r = check_ready(c);
+  if (r) return r;
+  if ((r = cube_fine_forces_impl(c, st))) return r;
+  if ((r = cube_fine_kick_impl(c, a_mid, dt))) return r;
+  c->sigma_vi = c->sigma_vi_new;  // pm.f90:193
+  if ((r = cube_coarse_forces_impl(c, st))) return r;
+  return cube_coarse_kick_impl(c, a_mid, dt, st);
+}
+
+extern "C" int64_t cube_nplocal(const cube_ctx* c) { return c ? c->np : -1; }
+
+extern "C" int cube_synchronize(cube_ctx* c) {
+  if (!c) return CUBE_ERR_ARG;
+  CUBE_CUDA(c, cudaSetDevice(c->device));
+  CUBE_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CUBE_OK;
+}
+
+// ------------------------------------------------------------------ fields
+// Copy between a dense host array and a padded device mesh (row stride n+2).
+static int mesh_copy(cube_ctx* c, float* dev, int n, void* host, bool to_host) {
+  size_t row = (size_t)n * 4, dpitch = (size_t)(n + 2) * 4;
+  size_t rows = (size_t)n * n;
+  if (to_host)
+    CUBE_CUDA(c, cudaMemcpy2DAsync(host, row, dev, dpitch, row, rows, cudaMemcpyDeviceToHost, c->stream));
+  else
+    CUBE_CUDA(c, cudaMemcpy2DAsync(dev, dpitch, host, row, row, rows, cudaMemcpyHostToDevice, c->stream));
+  CUBE_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CUBE_OK;
+}
+
+static int field_io(cube_ctx* c, int field, void* host, bool to_host) {
+  if (!c || !host) return CUBE_ERR_ARG;
+  CUBE_CUDA(c, cudaSetDevice(c->device));
+  int nf = c->nf, nc = c->p.nc;
+  switch (field) {
+    case CUBE_FIELD_RHO_F:
+      return mesh_copy(c, c->rho_f, nf, host, to_host);
+    case CUBE_FIELD_FORCE_F:
+      for (int d = 0; d < 3; d++) {
+        int r = mesh_copy(c, c->force_f[d], nf, (char*)host + (size_t)d * 4 * c->nfine, to_host);
+        if (r) return r;
+      }
+      return CUBE_OK;
+    case CUBE_FIELD_RHO_C:
+      return mesh_copy(c, c->rho_c, nc, host, to_host);
+    case CUBE_FIELD_FORCE_C:
+      for (int d = 0; d < 3; d++) {
+        int r = mesh_copy(c, c->force_c[d], nc, (char*)host + (size_t)d * 4 * c->ncells, to_host);
+        if (r) return r;
+      }
+      return CUBE_OK;
+    case CUBE_FIELD_KERN_F:
+    case CUBE_FIELD_KERN_C: {
+      if (!to_host) return cube_fail(c, CUBE_ERR_ARG, "kernels are read-only");
+      bool fine = field == CUBE_FIELD_KERN_F;
+      int n = fine ? nf : nc;
+      size_t cnt = 3 * (size_t)(n / 2 + 1) * n * n;
+      CUBE_CUDA(c, cudaMemcpyAsync(host, fine ? c->kern_f : c->kern_c, cnt * 4, cudaMemcpyDeviceToHost, c->stream));
+      CUBE_CUDA(c, cudaStreamSynchronize(c->stream));
+      // undo the folded 1/n^3 normalisation
+      double s = (double)n * n * n;
+      float* h = (float*)host;
+      for (size_t i = 0; i < cnt; i++) h[i] = (float)((double)h[i] * s);
+      return CUBE_OK;
+    }
+    default:
+      return cube_fail(c, CUBE_ERR_ARG, "unknown field");
+  }
+}
+
+extern "C" int cube_get_field(cube_ctx* c, int field, void* host) { return field_io(c, field, host, true); }
+extern "C" int cube_set_field(cube_ctx* c, int field, const void* host) {
+  return field_io(c, field, const_cast<void*>(host), false);
+}

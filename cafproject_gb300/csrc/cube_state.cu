@@ -1,0 +1,190 @@
+// cube_state.cu -- state upload/download, the per-particle cell index, the
+// velocity-code tables, the deterministic exclusive scan (the spine of
+// variables.f90:96-211) and the statistics read-back.
+#include <cmath>
+#include <vector>
+
+#include "cube_internal.cuh"
+
+// ------------------------------------------------------------------ scan
+// Exclusive scan of int32 counts into int64 starts[0..n] (starts[n] = total),
+// three passes with a fixed block partition so the result never depends on
+// scheduling: block sums, one-block scan of the sums, block-local scan + offset.
+constexpr int SCAN_T = 256;
+constexpr int SCAN_I = 16;
+constexpr int SCAN_CHUNK = SCAN_T * SCAN_I;
+
+__device__ __forceinline__ long long warp_incl_scan(long long v) {
+  for (int o = 1; o < 32; o <<= 1) {
+    long long n = __shfl_up_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) >= o) v += n;
+  }
+  return v;
+}
+// block-wide exclusive scan of one value per thread; returns the block total
+__device__ long long block_excl_scan(long long v, long long* s_warp, long long& total) {
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  long long inc = warp_incl_scan(v);
+  if (lane == 31) s_warp[w] = inc;
+  __syncthreads();
+  if (w == 0) {
+    long long t = lane < nw ? s_warp[lane] : 0;
+    long long ti = warp_incl_scan(t);
+    if (lane < nw) s_warp[lane] = ti - t;
+    if (lane == nw - 1) s_warp[32] = ti;
+  }
+  __syncthreads();
+  long long r = inc - v + s_warp[w];
+  total = s_warp[32];
+  __syncthreads();
+  return r;
+}
+
+__global__ void k_scan_blocksum(const int32_t* __restrict__ cnt, int64_t n, long long* __restrict__ bsum) {
+  __shared__ long long s[33];
+  int64_t base = (int64_t)blockIdx.x * SCAN_CHUNK;
+  long long v = 0;
+  for (int i = 0; i < SCAN_I; i++) {
+    int64_t k = base + (int64_t)i * SCAN_T + threadIdx.x;
+    if (k < n) v += cnt[k];
+  }
+  long long tot;
+  block_excl_scan(v, s, tot);
+  if (threadIdx.x == 0) bsum[blockIdx.x] = tot;
+}
+
+__global__ void k_scan_sums(long long* __restrict__ bsum, int64_t nb) {
+  __shared__ long long s[33];
+  long long carry = 0;
+  for (int64_t b0 = 0; b0 < nb; b0 += blockDim.x) {
+    int64_t k = b0 + threadIdx.x;
+    long long v = k < nb ? bsum[k] : 0;
+    long long tot;
+    long long e = block_excl_scan(v, s, tot);
+    if (k < nb) bsum[k] = e + carry;
+    carry += tot;
+  }
+}
+
+__global__ void k_scan_final(const int32_t* __restrict__ cnt, int64_t n, const long long* __restrict__ bsum,
+                             int64_t* __restrict__ starts) {
+  __shared__ long long s[33];
+  __shared__ int32_t tile[SCAN_CHUNK];
+  int64_t base = (int64_t)blockIdx.x * SCAN_CHUNK;
+  for (int i = threadIdx.x; i < SCAN_CHUNK; i += SCAN_T) {
+    int64_t k = base + i;
+    tile[i] = k < n ? cnt[k] : 0;
+  }
+  __syncthreads();
+  long long v = 0;
+  for (int i = 0; i < SCAN_I; i++) v += tile[threadIdx.x * SCAN_I + i];
+  long long tot;
+  long long run = block_excl_scan(v, s, tot) + bsum[blockIdx.x];
+  for (int i = 0; i < SCAN_I; i++) {
+    int64_t k = base + (int64_t)threadIdx.x * SCAN_I + i;
+    if (k < n) starts[k] = run;
+    run += tile[threadIdx.x * SCAN_I + i];
+    if (k == n - 1) starts[n] = run;
+  }
+}
+
+int cube_scan_counts(cube_ctx* c, const int32_t* counts, int64_t* starts, int64_t n) {
+  int64_t nb = (n + SCAN_CHUNK - 1) / SCAN_CHUNK;
+  if ((size_t)nb * 8 > c->scan_tmp_bytes) return cube_fail(c, CUBE_ERR_ARG, "scan scratch too small");
+  long long* bsum = (long long*)c->scan_tmp;
+  k_scan_blocksum<<<(unsigned)nb, SCAN_T, 0, c->stream>>>(counts, n, bsum);
+  k_scan_sums<<<1, 1024, 0, c->stream>>>(bsum, nb);
+  k_scan_final<<<(unsigned)nb, SCAN_T, 0, c->stream>>>(counts, n, bsum, starts);
+  CUBE_CUDA(c, cudaGetLastError());
+  return CUBE_OK;
+}
+
+// ---------------------------------------------------------- cell index
+// pcell[p] = cell of particle p, from the spine: one thread per cell.
+__global__ void k_fill_pcell(const int64_t* __restrict__ cstart, int64_t ncells, int32_t* __restrict__ pcell) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncells; c += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t p = cstart[c]; p < cstart[c + 1]; p++) pcell[p] = (int32_t)c;
+  }
+}
+
+int cube_state_in(cube_ctx* c, int64_t np, const void* xp, const void* vp, const int32_t* pid, const int32_t* rhoc,
+                  const float* vfield) {
+  int k = c->cur;
+  const cube_params& p = c->p;
+  // check the counts before touching the device state
+  int64_t tot = 0;
+  for (int64_t i = 0; i < c->ncells; i++) {
+    if (rhoc[i] < 0) return cube_fail(c, CUBE_ERR_ARG, "negative rhoc");
+    tot += rhoc[i];
+  }
+  if (tot != np) return cube_fail(c, CUBE_ERR_COUNT_MISMATCH, "sum(rhoc) != nplocal");
+  CUBE_CUDA(c, cudaMemcpyAsync(c->xp[k], xp, (size_t)3 * np * p.izipx, cudaMemcpyHostToDevice, c->stream));
+  CUBE_CUDA(c, cudaMemcpyAsync(c->vp[k], vp, (size_t)3 * np * p.izipv, cudaMemcpyHostToDevice, c->stream));
+  if (pid)
+    CUBE_CUDA(c, cudaMemcpyAsync(c->pid[k], pid, (size_t)4 * np, cudaMemcpyHostToDevice, c->stream));
+  else
+    CUBE_CUDA(c, cudaMemsetAsync(c->pid[k], 0, (size_t)4 * np, c->stream));
+  CUBE_CUDA(c, cudaMemcpyAsync(c->rhoc[k], rhoc, (size_t)4 * c->ncells, cudaMemcpyHostToDevice, c->stream));
+  CUBE_CUDA(c, cudaMemcpyAsync(c->vfield[k], vfield, (size_t)12 * c->ncells, cudaMemcpyHostToDevice, c->stream));
+  int r = cube_scan_counts(c, c->rhoc[k], c->cstart[k], c->ncells);
+  if (r) return r;
+  k_fill_pcell<<<cube_grid(c->ncells, 256), 256, 0, c->stream>>>(c->cstart[k], c->ncells, c->pcell[k]);
+  CUBE_CUDA(c, cudaGetLastError());
+  CUBE_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->np = np;
+  c->npglobal = np;
+  c->have_state = true;
+  return CUBE_OK;
+}
+
+int cube_state_out(cube_ctx* c, int64_t* np, void* xp, void* vp, int32_t* pid, int32_t* rhoc, float* vfield) {
+  int k = c->cur;
+  const cube_params& p = c->p;
+  if (np) *np = c->np;
+  if (xp) CUBE_CUDA(c, cudaMemcpyAsync(xp, c->xp[k], (size_t)3 * c->np * p.izipx, cudaMemcpyDeviceToHost, c->stream));
+  if (vp) CUBE_CUDA(c, cudaMemcpyAsync(vp, c->vp[k], (size_t)3 * c->np * p.izipv, cudaMemcpyDeviceToHost, c->stream));
+  if (pid) CUBE_CUDA(c, cudaMemcpyAsync(pid, c->pid[k], (size_t)4 * c->np, cudaMemcpyDeviceToHost, c->stream));
+  if (rhoc) CUBE_CUDA(c, cudaMemcpyAsync(rhoc, c->rhoc[k], (size_t)4 * c->ncells, cudaMemcpyDeviceToHost, c->stream));
+  if (vfield)
+    CUBE_CUDA(c, cudaMemcpyAsync(vfield, c->vfield[k], (size_t)12 * c->ncells, cudaMemcpyDeviceToHost, c->stream));
+  CUBE_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CUBE_OK;
+}
+
+// ------------------------------------------------------ velocity tables
+// tan_tab[v + nvbin/2] = real(4) tan(pi*real(v)/real(nvbin-1)), the decode of
+// update_particle.f90:67, taken as the correctly rounded float(tan(double)).
+int cube_build_tables(cube_ctx* c) {
+  int nv = c->nvbin;
+  std::vector<float> t(nv);
+  float nvm1 = (float)(nv - 1);
+  for (int i = 0; i < nv; i++) {
+    int v = i - nv / 2;
+    volatile float a = CUBE_PI_F * (float)v;  // real(4) product, then real(4) quotient
+    volatile float arg = a / nvm1;
+    t[i] = (float)std::tan((double)arg);
+  }
+  CUBE_CUDA(c, cudaMemcpyAsync(c->tan_tab, t.data(), 4 * (size_t)nv, cudaMemcpyHostToDevice, c->stream));
+  CUBE_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CUBE_OK;
+}
+
+__global__ void k_decode_table(const float* __restrict__ tan_tab, int nv, float sigma, double* __restrict__ dec) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nv) dec[i] = __ddiv_rn((double)tan_tab[i], vcoef(sigma));
+}
+
+// dec[v+nvbin/2] = tan(...)/(sqrt(pi/2)/(sigma*vrel_boost)) in real(8)
+int cube_ensure_decode(cube_ctx* c, double* tab, float sigma, float& cached) {
+  if (cached == sigma) return CUBE_OK;
+  k_decode_table<<<(c->nvbin + 255) / 256, 256, 0, c->stream>>>(c->tan_tab, c->nvbin, sigma, tab);
+  CUBE_CUDA(c, cudaGetLastError());
+  cached = sigma;
+  return CUBE_OK;
+}
+
+int cube_stats_fetch(cube_ctx* c) {
+  CUBE_CUDA(c, cudaMemcpyAsync(c->hstats, c->dstats, sizeof(DevStats), cudaMemcpyDeviceToHost, c->stream));
+  CUBE_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CUBE_OK;
+}

@@ -1,0 +1,282 @@
+"""Host-side mirror of CUBE's per-step subroutine surface over the C ABI.
+
+``CubeGPU`` exposes the reference's call surface -- ``update_x``,
+``buffer_grid``, ``buffer_x``, ``ext_pp_force``, ``particle_mesh``,
+``buffer_v`` (CUBEnu/work/main/main.f90:102-118) -- with the same argument
+meaning, on a device-resident state.  It loads ``libcube_gb300.so`` built from
+this tree and raises if the library or a GPU is missing: there is no CPU
+fallback.  Errors come back as ``CubeError`` carrying the C status code (each
+replaces one of the reference's ``stop`` statements).
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from .params import CubeParams
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBPATH = os.path.join(HERE, "_build", "libcube_gb300.so")
+
+FIELD_RHO_F, FIELD_FORCE_F, FIELD_RHO_C, FIELD_FORCE_C, FIELD_KERN_F, FIELD_KERN_C = 1, 2, 3, 4, 5, 6
+
+STATUS = {0: "CUBE_OK", 1: "CUBE_ERR_ARG", 2: "CUBE_ERR_CUDA", 3: "CUBE_ERR_TILE_OVERFLOW",
+          4: "CUBE_ERR_IMAGE_OVERFLOW", 5: "CUBE_ERR_PP_OVERFLOW", 6: "CUBE_ERR_COUNT_MISMATCH",
+          7: "CUBE_ERR_NONFINITE", 8: "CUBE_ERR_DISPLACEMENT", 9: "CUBE_ERR_NOMEM", 10: "CUBE_ERR_STATE"}
+
+# every symbol include/cube_gpu.h declares
+EXPORTS = ["cube_create", "cube_destroy", "cube_last_error", "cube_upload_state", "cube_download_state",
+           "cube_set_sigma", "cube_get_sigma", "cube_update_x", "cube_buffer_grid", "cube_buffer_x",
+           "cube_buffer_v", "cube_pp_force", "cube_particle_mesh", "cube_pm_fine_density", "cube_pm_coarse_density",
+           "cube_pm_fine_forces", "cube_pm_fine_kick",
+           "cube_pm_coarse_forces", "cube_pm_coarse_kick", "cube_get_field", "cube_set_field", "cube_nplocal",
+           "cube_synchronize", "cube_timing", "cube_timing_read", "cube_phase_name", "cube_stream"]
+NPHASE = 15
+
+
+class CubeError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s: %s" % (STATUS.get(code, code), msg))
+        self.code = code
+
+
+class CubeStats(ctypes.Structure):
+    """ctypes image of ``cube_stats`` (include/cube_gpu.h)."""
+
+    _fields_ = [("nplocal", ctypes.c_int64), ("max_tile_np", ctypes.c_int64), ("nlost", ctypes.c_int64),
+                ("ndup", ctypes.c_int64), ("sum_c", ctypes.c_double), ("sum_r", ctypes.c_double),
+                ("sum_s", ctypes.c_double), ("sigma_vi_new", ctypes.c_float), ("nlayer", ctypes.c_int32),
+                ("max_disp", ctypes.c_int32), ("pad0", ctypes.c_int32), ("f2_max_pp", ctypes.c_float),
+                ("pad1", ctypes.c_int32), ("npairs", ctypes.c_int64), ("itest1", ctypes.c_int64),
+                ("f2_max_fine", ctypes.c_float), ("f2_max_coarse", ctypes.c_float),
+                ("vmax", ctypes.c_float * 3), ("pad2", ctypes.c_int32), ("testrhof", ctypes.c_double),
+                ("testrhoc", ctypes.c_double), ("flags", ctypes.c_int32), ("pad3", ctypes.c_int32)]
+
+    def as_dict(self):
+        d = {}
+        for name, _ in self._fields_:
+            if name.startswith("pad"):
+                continue
+            v = getattr(self, name)
+            d[name] = list(v) if name == "vmax" else v
+        return d
+
+
+_lib = None
+
+
+def load_library(path=None):
+    """Load the in-tree library; raise if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIBPATH
+    if not os.path.exists(path):
+        raise RuntimeError("libcube_gb300.so is not built (%s); run __graft_entry__.build()" % path)
+    L = ctypes.CDLL(path)
+    P, I64, F = ctypes.c_void_p, ctypes.c_int64, ctypes.c_float
+    L.cube_create.argtypes = [P, P, P, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
+    L.cube_destroy.argtypes = [P]
+    L.cube_last_error.argtypes = [P]
+    L.cube_last_error.restype = ctypes.c_char_p
+    L.cube_upload_state.argtypes = [P, I64, P, P, P, P, P]
+    L.cube_download_state.argtypes = [P, ctypes.POINTER(I64), P, P, P, P, P]
+    L.cube_set_sigma.argtypes = [P, F, F]
+    L.cube_get_sigma.argtypes = [P, ctypes.POINTER(F), ctypes.POINTER(F)]
+    L.cube_update_x.argtypes = [P, F, F, F, P]
+    for n in ("cube_buffer_grid", "cube_buffer_x", "cube_buffer_v", "cube_synchronize"):
+        getattr(L, n).argtypes = [P]
+    L.cube_pp_force.argtypes = [P, F, F, P]
+    L.cube_particle_mesh.argtypes = [P, F, F, P]
+    L.cube_pm_fine_density.argtypes = [P, P]
+    L.cube_pm_coarse_density.argtypes = [P, P]
+    L.cube_pm_fine_forces.argtypes = [P, P]
+    L.cube_pm_fine_kick.argtypes = [P, F, F]
+    L.cube_pm_coarse_forces.argtypes = [P, P]
+    L.cube_pm_coarse_kick.argtypes = [P, F, F, P]
+    L.cube_get_field.argtypes = [P, ctypes.c_int, P]
+    L.cube_set_field.argtypes = [P, ctypes.c_int, P]
+    L.cube_nplocal.argtypes = [P]
+    L.cube_nplocal.restype = I64
+    L.cube_timing.argtypes = [P, ctypes.c_int]
+    L.cube_timing_read.argtypes = [P, P, P, ctypes.c_int]
+    L.cube_phase_name.argtypes = [ctypes.c_int]
+    L.cube_phase_name.restype = ctypes.c_char_p
+    L.cube_stream.argtypes = [P]
+    L.cube_stream.restype = ctypes.c_void_p
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def force_tables():
+    d = os.path.join(HERE, "data")
+    fine = np.fromfile(os.path.join(d, "fine_force_table.f32"), "<f4")
+    coarse = np.fromfile(os.path.join(d, "coarse_force_table.f32"), "<f4")
+    return np.ascontiguousarray(fine), np.ascontiguousarray(coarse)
+
+
+class CubeGPU:
+    """One image of CUBE's state resident on one GPU."""
+
+    def __init__(self, params: CubeParams, device=0):
+        self.p = params
+        self.L = load_library()
+        fine, coarse = force_tables()
+        self._cp = params.to_c()
+        h = ctypes.c_void_p()
+        rc = self.L.cube_create(ctypes.byref(self._cp), _ptr(fine), _ptr(coarse), device, ctypes.byref(h))
+        self.h = h
+        if rc:
+            msg = self.L.cube_last_error(h).decode() if h.value else ""
+            if h.value:
+                self.L.cube_destroy(h)
+            self.h = None
+            raise CubeError(rc, msg)
+
+    def _check(self, rc):
+        if rc:
+            raise CubeError(rc, self.L.cube_last_error(self.h).decode())
+
+    def close(self):
+        if self.h is not None and self.h.value:
+            self.L.cube_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- state
+    def upload(self, xp, vp, pid, rhoc, vfield):
+        p = self.p
+        xp = np.ascontiguousarray(xp, dtype=p.xdtype).reshape(-1, 3)
+        vp = np.ascontiguousarray(vp, dtype=p.vdtype).reshape(-1, 3)
+        pid = None if pid is None else np.ascontiguousarray(pid, dtype=np.int32)
+        rhoc = np.ascontiguousarray(rhoc, dtype=np.int32).reshape(-1)
+        vfield = np.ascontiguousarray(vfield, dtype=np.float32).reshape(-1, 3)
+        self._check(self.L.cube_upload_state(self.h, xp.shape[0], _ptr(xp), _ptr(vp), _ptr(pid), _ptr(rhoc),
+                                             _ptr(vfield)))
+
+    def nplocal(self):
+        return int(self.L.cube_nplocal(self.h))
+
+    def download(self, out=None):
+        """Disjoint state as host arrays; ``out`` may supply (pinned) arrays of
+        at least the right size to receive it."""
+        p = self.p
+        n = self.nplocal()
+        if out is not None:
+            xp, vp, pid = out["xp"][:n], out["vp"][:n], out["pid"][:n]
+            rhoc, vf = out["rhoc"], out["vfield"]
+        else:
+            xp = np.empty((n, 3), p.xdtype)
+            vp = np.empty((n, 3), p.vdtype)
+            pid = np.empty(n, np.int32)
+            rhoc = np.empty(p.nc ** 3, np.int32)
+            vf = np.empty((p.nc ** 3, 3), np.float32)
+        nn = ctypes.c_int64()
+        self._check(self.L.cube_download_state(self.h, ctypes.byref(nn), _ptr(xp), _ptr(vp), _ptr(pid), _ptr(rhoc),
+                                               _ptr(vf)))
+        return dict(xp=xp, vp=vp, pid=pid, rhoc=rhoc, vfield=vf)
+
+    def set_sigma(self, sigma_vi, sigma_vi_new=None):
+        sn = sigma_vi if sigma_vi_new is None else sigma_vi_new
+        self._check(self.L.cube_set_sigma(self.h, float(sigma_vi), float(sn)))
+
+    def get_sigma(self):
+        a, b = ctypes.c_float(), ctypes.c_float()
+        self._check(self.L.cube_get_sigma(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return np.float32(a.value), np.float32(b.value)
+
+    # ---- the reference's per-step call surface
+    def update_x(self, dt_old, dt, vz_max):
+        st = CubeStats()
+        self._check(self.L.cube_update_x(self.h, float(dt_old), float(dt), float(vz_max), ctypes.byref(st)))
+        return st.as_dict()
+
+    def buffer_grid(self):
+        self._check(self.L.cube_buffer_grid(self.h))
+
+    def buffer_x(self):
+        self._check(self.L.cube_buffer_x(self.h))
+
+    def buffer_v(self):
+        self._check(self.L.cube_buffer_v(self.h))
+
+    def ext_pp_force(self, a_mid, dt):
+        st = CubeStats()
+        self._check(self.L.cube_pp_force(self.h, float(a_mid), float(dt), ctypes.byref(st)))
+        return st.as_dict()
+
+    def particle_mesh(self, a_mid, dt):
+        st = CubeStats()
+        self._check(self.L.cube_particle_mesh(self.h, float(a_mid), float(dt), ctypes.byref(st)))
+        return st.as_dict()
+
+    # ---- stages (parity tests)
+    def fine_density(self):
+        st = CubeStats()
+        self._check(self.L.cube_pm_fine_density(self.h, ctypes.byref(st)))
+        return st.as_dict()
+
+    def coarse_density(self):
+        st = CubeStats()
+        self._check(self.L.cube_pm_coarse_density(self.h, ctypes.byref(st)))
+        return st.as_dict()
+
+    def fine_forces(self):
+        st = CubeStats()
+        self._check(self.L.cube_pm_fine_forces(self.h, ctypes.byref(st)))
+        return st.as_dict()
+
+    def fine_kick(self, a_mid, dt):
+        self._check(self.L.cube_pm_fine_kick(self.h, float(a_mid), float(dt)))
+
+    def coarse_forces(self):
+        st = CubeStats()
+        self._check(self.L.cube_pm_coarse_forces(self.h, ctypes.byref(st)))
+        return st.as_dict()
+
+    def coarse_kick(self, a_mid, dt):
+        st = CubeStats()
+        self._check(self.L.cube_pm_coarse_kick(self.h, float(a_mid), float(dt), ctypes.byref(st)))
+        return st.as_dict()
+
+    def synchronize(self):
+        self._check(self.L.cube_synchronize(self.h))
+
+    def stream(self):
+        """The cudaStream_t (as an int) every call of this context runs on."""
+        return int(self.L.cube_stream(self.h) or 0)
+
+    def timing(self, enable):
+        self._check(self.L.cube_timing(self.h, int(bool(enable))))
+
+    def timing_read(self):
+        """{phase: (total ms, launches)} accumulated since timing(True)."""
+        ms = (ctypes.c_double * NPHASE)()
+        cnt = (ctypes.c_int64 * NPHASE)()
+        self._check(self.L.cube_timing_read(self.h, ms, cnt, NPHASE))
+        return {self.L.cube_phase_name(i).decode(): (ms[i], int(cnt[i])) for i in range(NPHASE)}
+
+    def _field_shape(self, which):
+        nf, nc = self.p.nf, self.p.nc
+        return {FIELD_RHO_F: (nf, nf, nf), FIELD_FORCE_F: (3, nf, nf, nf), FIELD_RHO_C: (nc, nc, nc),
+                FIELD_FORCE_C: (3, nc, nc, nc), FIELD_KERN_F: (3, nf, nf, nf // 2 + 1),
+                FIELD_KERN_C: (3, nc, nc, nc // 2 + 1)}[which]
+
+    def get_field(self, which):
+        """Fields as numpy arrays indexed [.., z, y, x] (Fortran order of the reference)."""
+        a = np.empty(self._field_shape(which), np.float32)
+        self._check(self.L.cube_get_field(self.h, int(which), _ptr(a)))
+        return a
+
+    def set_field(self, which, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float32).reshape(self._field_shape(which))
+        self._check(self.L.cube_set_field(self.h, int(which), _ptr(a)))

@@ -1,0 +1,182 @@
+/*
+ * cube_gpu.h -- C ABI of the GB300 implementation of CUBE's per-step
+ * gravity/update path (drift + counting re-sort, PP kick, two-level PM kick).
+ *
+ * Each entry point replaces the body of one reference subroutine; the
+ * Fortran driver (CUBEnu/work/main/main.f90:88-145) keeps its loop and binds
+ * these functions with iso_c_binding.  All particle and mesh state stays
+ * resident in device memory between calls; host pointers are borrowed only
+ * for the duration of a call.  Every call returns an int status (CUBE_OK=0),
+ * replacing the reference's `stop` statements; cube_last_error() gives text.
+ * Threading: one CUDA stream per context, calls on one context must not
+ * overlap; independent contexts are independent.
+ *
+ * Array layouts are the reference's (Fortran, first index fastest):
+ *   xp(3,np)  int8 (izipx=1) or int16 (izipx=2)   variables.f90:44
+ *   vp(3,np)  int8 (izipv=1) or int16 (izipv=2)   variables.f90:45
+ *   pid(np)   int32                               variables.f90:47
+ *   rhoc(nt,nt,nt,nnt,nnt,nnt) int32  physical counts (checkpoint.f90:42)
+ *   vfield(3,nt,nt,nt,nnt,nnt,nnt) float          (checkpoint.f90:44)
+ * Particles are in the reference's disjoint order: tile (x fastest), then
+ * coarse cell (x fastest) inside the tile, then rank in cell
+ * (update_particle.f90:132-142).
+ */
+#ifndef CUBE_GPU_H
+#define CUBE_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes; each replaces a `stop` of the reference. */
+enum cube_status {
+  CUBE_OK = 0,
+  CUBE_ERR_ARG = 1,             /* bad argument or size */
+  CUBE_ERR_CUDA = 2,            /* CUDA / cuFFT failure */
+  CUBE_ERR_TILE_OVERFLOW = 3,   /* update_particle.f90:88-94 */
+  CUBE_ERR_IMAGE_OVERFLOW = 4,  /* buffer_grid.f90:148-154: particle capacity exceeded */
+  CUBE_ERR_PP_OVERFLOW = 5,     /* ext_pp_force.f90:41-45 */
+  CUBE_ERR_COUNT_MISMATCH = 6,  /* ext_pp_force.f90:156-160, update_particle.f90:245-250 */
+  CUBE_ERR_NONFINITE = 7,       /* a force or velocity became NaN/Inf */
+  CUBE_ERR_DISPLACEMENT = 8,    /* a particle left the double-buffer tile
+                                   (update_particle.f90:71 would index out of bounds) */
+  CUBE_ERR_NOMEM = 9,
+  CUBE_ERR_STATE = 10           /* call out of order (e.g. no state uploaded) */
+};
+
+/* Run-time image of the Fortran `parameter`s (parameters.f90:8-65). */
+typedef struct cube_params {
+  int32_t nc;         /* coarse cells per dim (nc) */
+  int32_t nnt;        /* tiles per dim (nnt); nt = nc/nnt */
+  int32_t ncell;      /* fine cells per coarse cell per dim (4) */
+  int32_t ncb;        /* buffer depth in coarse cells (6) */
+  int32_t izipx;      /* bytes per stored position component (1|2) */
+  int32_t izipv;      /* bytes per stored velocity component (1|2) */
+  int32_t nf_cutoff;  /* fine force table extent (16) */
+  int32_t pp_range;   /* PP neighbourhood in fine cells (1) */
+  int32_t pp_on;      /* Extended_pp_force */
+  int32_t with_pid;   /* -DPID: carry particle ids */
+  float rsoft;        /* PP hard cut radius, fine cells */
+  float mass_p;       /* sim%mass_p_cdm */
+  int64_t np_max;     /* particle capacity of the device arrays */
+  int32_t reserved[8];
+} cube_params;
+
+/* Scalars each call returns (the reference prints or stores these). */
+typedef struct cube_stats {
+  /* cube_update_x (update_particle.f90:16-256) */
+  int64_t nplocal;        /* sim%nplocal after the re-sort */
+  int64_t max_tile_np;    /* largest double-buffer tile count (overhead_tile numerator) */
+  int64_t nlost;          /* particles that landed in no physical cell */
+  int64_t ndup;           /* extra copies (landed in two frames) */
+  double sum_c, sum_r, sum_s; /* sigma_v sums (update_particle.f90:172-196) */
+  float sigma_vi_new;     /* std_vsim_res/sqrt(3.) */
+  int32_t nlayer;         /* layer count used for the visit order */
+  int32_t max_disp;       /* largest cell displacement seen */
+  int32_t pad0;
+  /* cube_pp_force (ext_pp_force.f90:10-162) */
+  float f2_max_pp;
+  int32_t pad1;
+  int64_t npairs;
+  int64_t itest1;
+  /* cube_particle_mesh (pm.f90:2-415) */
+  float f2_max_fine;
+  float f2_max_coarse;
+  float vmax[3];
+  int32_t pad2;
+  double testrhof, testrhoc;
+  int32_t flags;
+  int32_t pad3;
+} cube_stats;
+
+typedef struct cube_ctx cube_ctx;
+
+/* Fields for inspection / injection in parity tests. */
+enum cube_field {
+  CUBE_FIELD_RHO_F = 1,    /* fine density, nf^3 float, global periodic, Fortran order */
+  CUBE_FIELD_FORCE_F = 2,  /* fine force, 3 planes of nf^3 float (x, y, z) */
+  CUBE_FIELD_RHO_C = 3,    /* coarse density nc^3 float */
+  CUBE_FIELD_FORCE_C = 4,  /* coarse force, 3 planes of nc^3 float */
+  CUBE_FIELD_KERN_F = 5,   /* fine kernel Im part, 3 planes of (nf/2+1)*nf*nf float (unscaled) */
+  CUBE_FIELD_KERN_C = 6    /* coarse kernel, 3 planes of (nc/2+1)*nc*nc float (unscaled) */
+};
+
+/* Build a context on `device`: allocates every device buffer for the given
+   sizes and builds the fine and coarse Green's functions from the force
+   tables (replaces initialize + kernel_f + kernel_c, initialize.f90:21-38,
+   kernel_f.f90:14-37, kernel_c.f90:16-117).
+   fine_table: fk_table(i,j,k,d), 16x16x16x3 float, Fortran order.
+   coarse_table: ck_table(d,i,j,k), 3x4x4x4 float, Fortran order. */
+int cube_create(const cube_params* p, const float* fine_table, const float* coarse_table, int device,
+                cube_ctx** out);
+int cube_destroy(cube_ctx* ctx);
+const char* cube_last_error(const cube_ctx* ctx);
+
+/* Upload / download the disjoint state (particle_initialization.f90:34-78,
+   checkpoint.f90:36-47).  nplocal <= np_max. pid may be NULL. */
+int cube_upload_state(cube_ctx* ctx, int64_t nplocal, const void* xp, const void* vp, const int32_t* pid,
+                      const int32_t* rhoc, const float* vfield);
+int cube_download_state(cube_ctx* ctx, int64_t* nplocal, void* xp, void* vp, int32_t* pid, int32_t* rhoc,
+                        float* vfield);
+
+/* sigma_vi / sigma_vi_new module variables (variables.f90:36). */
+int cube_set_sigma(cube_ctx* ctx, float sigma_vi, float sigma_vi_new);
+int cube_get_sigma(const cube_ctx* ctx, float* sigma_vi, float* sigma_vi_new);
+
+/* update_x -> update_xp (update_particle.f90:5-256): drift by
+   dt_mid=(dt_old+dt)/2, counting re-sort in the reference's layered visit
+   order, new rhoc/vfield, sigma_v statistics; sets sigma_vi_new.
+   vz_max is sim%vz_max (pm.f90:398). */
+int cube_update_x(cube_ctx* ctx, float dt_old, float dt, float vz_max, cube_stats* st);
+
+/* buffer_grid / buffer_x / buffer_v (buffer_grid.f90:5-26,
+   buffer_particle.f90:5-25): the device kernels index the periodic
+   neighbours directly, so these only validate the context. */
+int cube_buffer_grid(cube_ctx* ctx);
+int cube_buffer_x(cube_ctx* ctx);
+int cube_buffer_v(cube_ctx* ctx);
+
+/* ext_pp_force (ext_pp_force.f90:10-162): pair force within +-pp_range fine
+   cells with the hard cut rsoft, kick v by F*a_mid*dt/(6 pi). */
+int cube_pp_force(cube_ctx* ctx, float a_mid, float dt, cube_stats* st);
+
+/* particle_mesh (pm.f90:2-415): fine PM kick (decode sigma_vi, encode
+   sigma_vi_new), then sigma_vi=sigma_vi_new, then coarse PM kick; returns
+   the force maxima and vmax. */
+int cube_particle_mesh(cube_ctx* ctx, float a_mid, float dt, cube_stats* st);
+
+/* Stages of particle_mesh, for parity tests that inspect or inject fields:
+   density only (CIC deposit, pm.f90:52-107 / 205-267), forces (deposit +
+   Green's multiply + inverse FFT; the density buffer then holds the
+   spectrum) and kick only. */
+int cube_pm_fine_density(cube_ctx* ctx, cube_stats* st);
+int cube_pm_coarse_density(cube_ctx* ctx, cube_stats* st);
+int cube_pm_fine_forces(cube_ctx* ctx, cube_stats* st);
+int cube_pm_fine_kick(cube_ctx* ctx, float a_mid, float dt);
+int cube_pm_coarse_forces(cube_ctx* ctx, cube_stats* st);
+int cube_pm_coarse_kick(cube_ctx* ctx, float a_mid, float dt, cube_stats* st);
+
+int cube_get_field(cube_ctx* ctx, int field, void* host);
+int cube_set_field(cube_ctx* ctx, int field, const void* host);
+
+/* Number of particles currently resident. */
+int64_t cube_nplocal(const cube_ctx* ctx);
+int cube_synchronize(cube_ctx* ctx);
+
+/* Per-phase device timers (replace the reference's system_clock prints,
+   e.g. pm.f90:35-411): enable=1 resets and starts event pairs around every
+   phase on the context's stream, enable=0 stops; cube_timing_read harvests
+   the accumulated milliseconds and launch counts per phase. */
+#define CUBE_NPHASE 15
+int cube_timing(cube_ctx* ctx, int enable);
+int cube_timing_read(cube_ctx* ctx, double* ms, int64_t* count, int nphase);
+const char* cube_phase_name(int phase);
+/* The CUDA stream (cudaStream_t) all of the context's work is issued on. */
+void* cube_stream(cube_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CUBE_GPU_H */

@@ -1,0 +1,241 @@
+"""Known-answer tests that pin the CPU oracle to the reference's semantics.
+
+The reference ships no golden vectors for this path, so each test checks one
+documented behaviour of the Fortran loops with an answer derived by hand.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from cafproject_gb300 import params as P
+from cafproject_gb300 import synth
+from oracle import cube_oracle as O
+
+PI_F = np.float32(4.0) * np.arctan(np.float32(1.0))
+
+
+def one_tile(nc=24, **kw):
+    kw.setdefault("pp_on", True)
+    return P.CubeParams(nc=nc, nnt=1, rsoft=0.1, mass_p=8.0, **kw)
+
+
+def state_from(p, cells, xps, vps, vfield=None):
+    """Disjoint state with the given particles (global 0-based cells)."""
+    nt = p.nt
+    cid = [((cx % nt) + nt * ((cy % nt) + nt * ((cz % nt) + nt * ((cx // nt) + p.nnt * ((cy // nt) + p.nnt * (cz // nt))))))
+           for cx, cy, cz in cells]
+    order = np.argsort(cid, kind="stable")
+    rhoc = np.bincount(np.asarray(cid), minlength=p.nc ** 3).astype(np.int32)
+    xp = np.asarray(xps, p.xdtype)[order]
+    vp = np.asarray(vps, p.vdtype)[order]
+    vf = np.zeros((p.nc ** 3, 3), np.float32) if vfield is None else vfield
+    return dict(xp=xp, vp=vp, pid=(order + 1).astype(np.int32), rhoc=rhoc, vfield=vf)
+
+
+def test_position_decode_matches_paper_example():
+    # ms_caf.tex:78: chi=(-128,127,0,60), rho=(1,0,2,1) -> x=(0.001953125,
+    # 2.998046875, 2.501953125, 3.736328125) coarse cells.  The code stores
+    # chi+128 as a wrapped int8 and decodes (unsigned(xp)+0.5)/256
+    # (update_particle.f90:66, parameters.f90:16-18).
+    chi = np.array([-128, 127, 0, 60])
+    cells = np.array([1, 3, 3, 4])
+    stored = ((chi + 128 + 128) % 256 - 128).astype(np.int8)
+    u = stored.astype(np.int64) & 255
+    x = (cells - 1) + (u + 0.5) / 256.0
+    np.testing.assert_array_equal(x, [0.001953125, 2.998046875, 2.501953125, 3.736328125])
+
+
+def test_weight_v_is_a_single_precision_literal():
+    # real(8),parameter :: weight_v=0.1 (update_particle.f90:25) is (double)0.1f
+    assert float(np.float64(np.float32(0.1))) == 0.10000000149011612
+
+
+def test_tan_code_is_correctly_rounded():
+    mp = pytest.importorskip("mpmath")
+    mp.mp.prec = 120
+    for izipv, step in ((1, 1), (2, 37)):
+        nv = (1 << (8 * izipv)) - 1
+        for v in list(range(0, nv // 2 + 2, step)) + [nv // 2 - 1, nv // 2, nv // 2 + 1]:
+            arg = np.float32(np.float32(PI_F * np.float32(v)) / np.float32(nv))
+            ours = np.float32(np.tan(np.float64(arg)))
+            exact = mp.tan(mp.mpf(float(arg)))
+            cr = np.float32(float(exact))
+            # float(double(exact)) can only double-round on an exact tie; none occur here
+            assert ours == cr, (izipv, v)
+            assert np.float32(np.tan(np.float64(-arg))) == -ours
+
+
+def test_velocity_code_round_trip():
+    # encode (update_particle.f90:117) then decode (:67) returns the velocity to
+    # within half a code bin; the codec demo of CUBE/velocity_conversion/test.f90:28-35
+    sigma = np.float32(0.01)
+    v = np.linspace(-0.2, 0.2, 2001)
+    for izipv in (1, 2):
+        nv = (1 << (8 * izipv)) - 1
+        code = synth.encode(v, sigma, izipv)
+        assert np.all(np.abs(code) <= nv // 2)
+        t = np.tan(np.float32(np.float32(PI_F * code.astype(np.float32)) / np.float32(nv)).astype(np.float64))
+        back = t.astype(np.float32).astype(np.float64) / synth.vcoef(sigma)
+        c = synth.vcoef(sigma)
+        u = nv * np.arctan(c * v) / np.float64(PI_F)
+        assert np.all(np.abs(u - code) <= 0.5 + 1e-9)
+        # decode lands inside its own code bin: re-encoding is idempotent
+        np.testing.assert_array_equal(synth.encode(back, sigma, izipv), code)
+        # and the error is below one bin width
+        assert np.all(np.abs(back - v) <= np.abs(np.tan(np.float64(PI_F) * (np.abs(code) + 1) / nv) / c
+                                                 - np.tan(np.float64(PI_F) * np.abs(code) / nv) / c) + 1e-12)
+
+
+def test_cic_deposit_single_particle():
+    # one particle at fine coordinate tempx=4*(1-1)+4*(u+0.5)/256 in each dim
+    # (pm.f90:63-77): weights dx1=idx1-tempx on idx1=floor(tempx)+1
+    p = one_tile(nc=24, pp_on=False)
+    st = state_from(p, [(0, 0, 0)], [[0, 63, -1]], [[0, 0, 0]])
+    img = O.OracleImage(p)
+    img.load(**st)
+    rho = img.fine_density(0)
+    nfb = p.nfb
+    u = np.array([0, 63, 255]) + 0.5
+    tx = (4 * u / 256).astype(np.float32)
+    i1 = np.floor(tx).astype(int) + 1
+    d1 = (i1.astype(np.float32) - tx).astype(np.float32)
+    d2 = (np.float32(1) - d1).astype(np.float32)
+    for cz in range(2):
+        for cy in range(2):
+            for cx in range(2):
+                w = np.float32(np.float32(np.float32((d1[0], d2[0])[cx] * (d1[1], d2[1])[cy]) *
+                                          (d1[2], d2[2])[cz]) * np.float32(8.0))
+                z, y, x = i1[2] + cz + nfb - 1, i1[1] + cy + nfb - 1, i1[0] + cx + nfb - 1
+                assert rho[z, y, x] == w
+    # one tile of a periodic box: the buffer holds images; the physical region holds the mass once
+    phys = rho[nfb:nfb + p.nft, nfb:nfb + p.nft, nfb:nfb + p.nft]
+    assert abs(float(phys.sum(dtype=np.float64)) - 8.0) < 1e-6
+
+
+def test_two_particle_pp_force_known_answer():
+    # FORCETEST setup (main.f90:104-111): two particles one fine cell apart in x.
+    # Pair force m*r/r^3*pcut(r), pcut=1-7/4 rc^3+3/4 rc^5, rc=r/16
+    # (ext_pp_force.f90:103-110); kick F*a_mid*dt/6/pi then the atan code.
+    p = one_tile(nc=24)
+    sig = np.float32(0.05)
+    # offsets: x codes 0 and 64 -> fine x = 4*(0.5/256) and 4*(64.5/256): 1 fine cell apart
+    st = state_from(p, [(5, 5, 5), (5, 5, 5)], [[-128, 0, 0], [-64, 0, 0]], [[0, 0, 0], [0, 0, 0]])
+    img = O.OracleImage(p)
+    img.load(**st)
+    img.sigma_vi = img.sigma_vi_new = sig
+    a_mid, dt = np.float32(0.5), np.float32(0.02)
+    out = img.pp_force(a_mid, dt)
+    r = 1.0
+    pcut = 1 - 1.75 * (r / 16) ** 3 + 0.75 * (r / 16) ** 5
+    f = 8.0 / r ** 2 * pcut
+    assert out["npairs"] == 4 and out["itest1"] == 2
+    assert abs(float(out["f2_max_pp"]) - f * f) <= 1e-6 * f * f
+    vp = img.state()["vp"]
+    kick = f * float(a_mid) * float(dt) / 6 / float(PI_F)
+    c = synth.vcoef(sig)
+    expect = int(np.sign(kick) * np.floor(abs(65535 * np.arctan(c * kick) / np.float64(PI_F)) + 0.5))
+    # particle 0 (x smaller) is pulled to +x, particle 1 to -x
+    assert sorted([int(vp[0, 0]), int(vp[1, 0])]) == [-expect, expect]
+    assert np.all(vp[:, 1:] == 0)
+
+
+def test_pp_hard_cut_at_rsoft():
+    # pairs with |r| <= rsoft contribute nothing (merge(...,rmag>rsoft), ext_pp_force.f90:109)
+    p = one_tile(nc=24)
+    p.rsoft = 2.0
+    st = state_from(p, [(5, 5, 5), (5, 5, 5)], [[-128, 0, 0], [-64, 0, 0]], [[0, 0, 0], [0, 0, 0]])
+    img = O.OracleImage(p)
+    img.load(**st)
+    img.sigma_vi = img.sigma_vi_new = np.float32(0.05)
+    out = img.pp_force(0.5, 0.02)
+    assert out["f2_max_pp"] == 0
+    assert np.all(img.state()["vp"] == 0)
+
+
+def test_update_x_with_zero_dt_keeps_positions():
+    p = P.small(nc=24, nnt=2)
+    st = synth.random_state(p, seed=3)
+    img = O.OracleImage(p)
+    img.load(st["xp"], st["vp"], st["pid"], st["rhoc"], st["vfield"])
+    img.sigma_vi = np.float32(st["sigma_vi"])
+    out = img.update_x(0.0, 0.0, st["vz_max"])
+    s = img.state()
+    assert out["nplocal"] == st["xp"].shape[0]
+    np.testing.assert_array_equal(s["rhoc"], st["rhoc"])
+    np.testing.assert_array_equal(s["xp"], st["xp"])
+    np.testing.assert_array_equal(s["pid"], st["pid"])
+
+
+def test_update_x_rank_follows_layer_order():
+    # Two particles from source cells k=4 and k=6 (local) land in cell k=5.
+    # With nlayer=3 the layer of k is (k+ncb-1) mod 3: k=6 -> 2, k=4 -> 0,
+    # so k=4 is visited first (update_particle.f90:97-114); with nlayer=1 the
+    # plain k order gives the same answer; with nlayer=5 the layers are 4 and 1
+    # and the k=6 particle comes first.
+    p = P.CubeParams(nc=24, nnt=1, pp_on=False, mass_p=8.0)
+    sigma = np.float32(0.01)
+    # both at the same in-cell offset, moving +-1 cell in z
+    cells = [(3, 3, 5), (3, 3, 3)]  # 0-based: local k=6 and k=4
+    xps = [[0, 0, 0], [0, 0, 0]]
+    v = 0.5
+    code = int(synth.encode(np.array([v]), sigma, 2)[0])
+    vps = [[0, 0, -code], [0, 0, code]]
+    st = state_from(p, cells, xps, vps)
+    orders = {}
+    for vz_max, label in ((0.0, 1), (1.0, 3), (2.0, 5)):
+        img = O.OracleImage(p)
+        img.load(**st)
+        img.sigma_vi = sigma
+        # decoded |v| and the drift dt_mid*v/4 move exactly one cell
+        t = np.float32(np.tan(np.float64(np.float32(np.float32(PI_F * np.float32(code)) / np.float32(65535)))))
+        vv = float(t) / synth.vcoef(sigma)
+        dt = np.float32(4.0 / vv)
+        out = img.update_x(dt, dt, np.float32(vz_max) / dt * np.float32(4.0) * np.float32(0.999))
+        s = img.state()
+        assert out["nlayer"] == label
+        cell = 3 + 24 * (3 + 24 * 4)  # 0-based (x,y,z)=(3,3,4)
+        start = int(np.sum(s["rhoc"][:cell]))
+        assert s["rhoc"][cell] == 2
+        orders[label] = tuple(s["pid"][start:start + 2])
+    # pid 1 is the k=6 particle (sorted first by state_from? check via cells order)
+    k6 = int(st["pid"][np.nonzero(np.asarray(st["vp"])[:, 2] < 0)[0][0]])
+    k4 = int(st["pid"][np.nonzero(np.asarray(st["vp"])[:, 2] > 0)[0][0]])
+    assert orders[1] == (k4, k6)
+    assert orders[3] == (k4, k6)
+    assert orders[5] == (k6, k4)
+
+
+def test_mass_conservation():
+    p = P.small(nc=24, nnt=2)
+    st = synth.random_state(p, seed=4, clump=5)
+    img = O.OracleImage(p)
+    img.load(st["xp"], st["vp"], st["pid"], st["rhoc"], st["vfield"])
+    n = st["xp"].shape[0]
+    F, R = img.global_fine_force()
+    assert abs(float(R.sum(dtype=np.float64)) - n * 8.0) <= 1e-6 * n * 8.0
+    r3 = img.coarse_density()
+    assert abs(float(r3.sum(dtype=np.float64)) - n * 8.0) <= 1e-6 * n * 8.0
+
+
+def test_fine_kernel_is_odd_and_imaginary():
+    import scipy.fft as sfft
+    n = 48
+    k = O.kernel_f(n, 16, False)
+    for d in range(3):
+        # the real-space kernel is odd along d, so its transform is purely imaginary
+        box = sfft.irfftn(1j * k[d].astype(np.float64), s=(n, n, n)).astype(np.float64)
+        flipped = np.roll(np.flip(box, axis=2 - d), 1, axis=2 - d)
+        np.testing.assert_allclose(box, -flipped, atol=1e-6)
+        tab = O.fine_table()[d]
+        np.testing.assert_allclose(box[:16, :16, :16], tab, atol=2e-6)
+        # nothing outside the 31^3 support
+        assert np.abs(box[16:n - 15]).max() < 1e-6
+
+
+def test_coarse_kernel_lrck_modes():
+    nc = 32
+    k = O.kernel_c(nc, 4)
+    assert np.all(np.isfinite(k))
+    # the x kernel vanishes on kx=0 and kx=-nc/2 planes only through oddness
+    assert np.abs(k[0][:, :, 0]).max() < 1e-3 * np.abs(k[0]).max()
