@@ -48,7 +48,7 @@ static void release(cube_ctx* c) {
   void* bufs[] = {c->xp[0], c->xp[1], c->vp[0], c->vp[1], c->pid[0], c->pid[1], c->pcell[0], c->pcell[1],
                   c->rhoc[0], c->rhoc[1],
                   c->vfield[0], c->vfield[1], c->cstart[0], c->cstart[1], c->dest, c->dframe, c->rank, c->xtra,
-                  c->scan_tmp, c->red_tmp, c->tan_tab, c->dec_old, c->dec_new, c->rho_f, c->force_f[0],
+                  c->scan_tmp, c->red_tmp, c->tan_tab, c->codec[0].dec, c->codec[1].dec, c->codec[0].bnd, c->codec[1].bnd, c->codec[0].dech, c->codec[1].dech, c->rho_f, c->force_f[0],
                   c->force_f[1], c->force_f[2], c->kern_f, c->kern_f_raw, c->rho_c, c->force_c[0],
                   c->force_c[1], c->force_c[2], c->kern_c, c->fpp, c->dstats, c->cufft_work};
   for (void* b : bufs)
@@ -141,8 +141,11 @@ extern "C" int cube_create(const cube_params* p, const float* fine_table, const 
   c->red_blocks = 2048;
   ALLOC(c->red_tmp, sizeof(double) * 4 * c->red_blocks);
   ALLOC(c->tan_tab, 4 * c->nvbin);
-  ALLOC(c->dec_old, 8 * c->nvbin);
-  ALLOC(c->dec_new, 8 * c->nvbin);
+  for (int k = 0; k < 2; k++) {
+    ALLOC(c->codec[k].dec, 8 * c->nvbin);
+    ALLOC(c->codec[k].dech, 8 * c->nvbin);
+    ALLOC(c->codec[k].bnd, 8 * (c->nvbin / 2 + 1));
+  }
   int64_t nfh = (int64_t)(c->nf / 2 + 1);
   int64_t fpad = 2 * nfh * c->nf * (int64_t)c->nf;  // floats of a padded fine mesh
   ALLOC(c->rho_f, 4 * fpad);
@@ -269,6 +272,17 @@ extern "C" int cube_particle_mesh(cube_ctx* c, float a_mid, float dt, cube_stats
 }
 
 extern "C" int64_t cube_nplocal(const cube_ctx* c) { return c ? c->np : -1; }
+
+extern "C" int cube_set_option(cube_ctx* c, int option, int64_t value) {
+  if (!c) return CUBE_ERR_ARG;
+  switch (option) {
+    case CUBE_OPT_EXACT_KICKS:
+      c->opt_exact_kicks = value ? 1 : 0;
+      return CUBE_OK;
+    default:
+      return cube_fail(c, CUBE_ERR_ARG, "unknown option");
+  }
+}
 
 extern "C" int cube_synchronize(cube_ctx* c) {
   if (!c) return CUBE_ERR_ARG;

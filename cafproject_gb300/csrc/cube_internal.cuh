@@ -20,6 +20,7 @@
 #include <cufft.h>
 #include <stdint.h>
 
+#include <cmath>
 #include <string>
 
 #include "../../include/cube_gpu.h"
@@ -36,7 +37,9 @@ struct DevStats {
   unsigned int vmax_bits[3];
   unsigned long long npairs, itest1;
   unsigned long long ndup_list;  // entries in the extra-copy list
+  unsigned long long nexact;     // kick lanes evaluated on the exact FP64 chain
   double testrhof, testrhoc;
+  unsigned long long rhof_fix, rhoc_fix;  // deposited mass in 2^-32 fixed point
 };
 
 struct cube_ctx {
@@ -72,10 +75,17 @@ struct cube_ctx {
   int red_blocks = 0;
   // velocity code tables
   float* tan_tab = nullptr;     // float(tan(pi*v/(nvbin-1))) for v in [-nvbin/2, nvbin/2)
-  double* dec_old = nullptr;    // decode table for sigma_vi
-  double* dec_new = nullptr;    // decode table for sigma_vi_new
-  float dec_old_sigma = -1.f, dec_new_sigma = -1.f;
+  struct Codec {
+    float sigma = -1.f;
+    double* dec = nullptr;     // dec[v+nvbin/2] = tan code / vcoef(sigma), real(8)
+    float2* dech = nullptr;    // the same split into float hi + lo
+    long long* bnd = nullptr;  // bnd[n] = bits of the smallest |v| that encodes to n (n=1..nvbin/2-1)
+  } codec[2];
+  int codec_next = 0;
   float sigma_vi = 0.f, sigma_vi_new = 0.f;
+  float vmax_prev[3] = {0.f, 0.f, 0.f};  // last coarse-kick vmax (0: unknown)
+  unsigned long long kick_exact_lanes = 0;
+  int opt_exact_kicks = 0;
   // fine PM
   cufftHandle plan_f_r2c = 0, plan_f_c2r = 0;
   float* rho_f = nullptr;       // padded real / complex in place
@@ -114,9 +124,35 @@ int cube_fail(cube_ctx* c, int code, const std::string& msg);
   } while (0)
 
 // ------------------------------------------------------------- geometry
+// Exact unsigned 32-bit division by a run-time constant with one high multiply
+// (the round-up multiplier method of Granlund & Montgomery, 1994): 64-bit or
+// generic integer division would go through the slow double-precision unit.
+struct FastDiv {
+  uint32_t d, m, s;
+};
+inline FastDiv make_fastdiv(uint32_t d) {
+  FastDiv f{d, 0u, 0u};
+  if (d <= 1) return f;
+  uint32_t l = 0;
+  while ((1ull << l) < d) l++;
+  f.m = (uint32_t)((((1ull << l) - d) << 32) / d + 1);
+  f.s = l;
+  return f;
+}
+__host__ __device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f) {
+  if (f.d <= 1) return n;
+#ifdef __CUDA_ARCH__
+  uint32_t t = __umulhi(n, f.m);
+#else
+  uint32_t t = (uint32_t)(((uint64_t)n * f.m) >> 32);
+#endif
+  return (t + ((n - t) >> 1)) >> (f.s - 1);
+}
+
 struct Geo {
   int nc, nt, nnt, ncell, ncb, nf;
   int izipx, izipv;
+  FastDiv dnt, dnnt;  // division by nt and by nnt
 };
 inline Geo make_geo(const cube_ctx* c) {
   Geo g;
@@ -128,6 +164,8 @@ inline Geo make_geo(const cube_ctx* c) {
   g.nf = c->nf;
   g.izipx = c->p.izipx;
   g.izipv = c->p.izipv;
+  g.dnt = make_fastdiv((uint32_t)c->nt);
+  g.dnnt = make_fastdiv((uint32_t)c->p.nnt);
   return g;
 }
 
@@ -135,28 +173,40 @@ __host__ __device__ inline int wrapi(int a, int n) {
   int r = a % n;
   return r < 0 ? r + n : r;
 }
+// a in [-n, 2n): one compare instead of a division
+__host__ __device__ __forceinline__ int wrap1(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
 // global coarse coordinates (0-based) -> cell id in the disjoint order
 __host__ __device__ inline int64_t cell_id(const Geo& g, int gx, int gy, int gz) {
-  int tx = gx / g.nt, ty = gy / g.nt, tz = gz / g.nt;
+  int tx = (int)fdiv((uint32_t)gx, g.dnt), ty = (int)fdiv((uint32_t)gy, g.dnt), tz = (int)fdiv((uint32_t)gz, g.dnt);
   int ix = gx - tx * g.nt, iy = gy - ty * g.nt, iz = gz - tz * g.nt;
-  int64_t tile = tx + (int64_t)g.nnt * (ty + (int64_t)g.nnt * tz);
-  return ix + (int64_t)g.nt * (iy + (int64_t)g.nt * (iz + (int64_t)g.nt * tile));
+  int tile = tx + g.nnt * (ty + g.nnt * tz);
+  return (int64_t)(uint32_t)(ix + g.nt * (iy + g.nt * (iz + g.nt * tile)));
 }
-__host__ __device__ inline void cell_coords(const Geo& g, int64_t c, int& gx, int& gy, int& gz) {
-  int64_t nt = g.nt;
-  int ix = (int)(c % nt);
-  c /= nt;
-  int iy = (int)(c % nt);
-  c /= nt;
-  int iz = (int)(c % nt);
-  c /= nt;
-  int tx = (int)(c % g.nnt);
-  c /= g.nnt;
-  int ty = (int)(c % g.nnt);
-  int tz = (int)(c / g.nnt);
+__host__ __device__ inline void cell_coords(const Geo& g, int64_t cid, int& gx, int& gy, int& gz) {
+  uint32_t c = (uint32_t)cid, q;
+  q = fdiv(c, g.dnt);
+  int ix = (int)(c - q * (uint32_t)g.nt);
+  c = q;
+  q = fdiv(c, g.dnt);
+  int iy = (int)(c - q * (uint32_t)g.nt);
+  c = q;
+  q = fdiv(c, g.dnt);
+  int iz = (int)(c - q * (uint32_t)g.nt);
+  c = q;
+  q = fdiv(c, g.dnnt);
+  int tx = (int)(c - q * (uint32_t)g.nnt);
+  c = q;
+  q = fdiv(c, g.dnnt);
+  int ty = (int)(c - q * (uint32_t)g.nnt);
+  int tz = (int)q;
   gx = tx * g.nt + ix;
   gy = ty * g.nt + iy;
   gz = tz * g.nt + iz;
+}
+// tile index and 1-based tile-local coordinate of a global coarse coordinate
+__host__ __device__ __forceinline__ void tile_local(const Geo& g, int gc, int& T, int& L) {
+  T = (int)fdiv((uint32_t)gc, g.dnt);
+  L = gc - T * g.nt + 1;
 }
 // padded real-mesh index (row stride n+2), periodic in each dimension
 __device__ __forceinline__ int64_t mesh_idx(int n, int x, int y, int z) {
@@ -182,19 +232,28 @@ __device__ __forceinline__ double xres_of(int izipx) { return izipx == 1 ? 1.0 /
 
 // tempx=ncell*(i-1)+ncell*(int+rshift)*x_resolution evaluated in real(8),
 // rounded to real(4) (pm.f90:63); i is the tile-local 1-based cell index.
+// The real(8) sum is exact (< 28 significant bits), so one real(4) rounding
+// of it equals one FP32 addition of the two exactly representable terms.
+__device__ __forceinline__ float pos_off_f(int code, int izipx) {
+  return (float)(code & ((1 << (8 * izipx)) - 1)) + 0.5f;
+}
 __device__ __forceinline__ float fine_tempx(int ncell, int ilocal, int code, int izipx) {
-  double a = (double)(ncell * (ilocal - 1));
-  double b = __dmul_rn(__dmul_rn((double)ncell, pos_off(code, izipx)), xres_of(izipx));
-  return __double2float_rn(__dadd_rn(a, b));
+  float a = (float)(ncell * (ilocal - 1));
+  float b = __fmul_rn(pos_off_f(code, izipx), izipx == 1 ? 4.0f / 256.0f : 4.0f / 65536.0f);
+  return __fadd_rn(a, b);
 }
 // tempx=(i-1)+(int+rshift)*x_resolution-0.5 (pm.f90:221, 335)
 __device__ __forceinline__ float coarse_tempx(int i1based, int code, int izipx) {
-  double a = __dadd_rn((double)(i1based - 1), __dmul_rn(pos_off(code, izipx), xres_of(izipx)));
-  return __double2float_rn(__dsub_rn(a, 0.5));
+  float a = __fsub_rn((float)(i1based - 1), 0.5f);
+  float b = __fmul_rn(pos_off_f(code, izipx), izipx == 1 ? 1.0f / 256.0f : 1.0f / 65536.0f);
+  return __fadd_rn(a, b);
 }
 
 // sqrt(pi/2)/(sigma*vrel_boost) in real(8) (update_particle.f90:67)
-inline double vcoef_host(float sigma);
+inline double vcoef_host(float sigma) {
+  volatile float s = std::sqrt(CUBE_PI_F / 2.0f);
+  return (double)s / ((double)sigma * 2.5);
+}
 __device__ __forceinline__ double vcoef(float sigma) {
   float s = __fsqrt_rn(__fdiv_rn(CUBE_PI_F, 2.0f));
   return __ddiv_rn((double)s, __dmul_rn((double)sigma, 2.5));
@@ -204,6 +263,126 @@ __device__ __forceinline__ long long v_encode(double v, double c, int nvbin) {
   double u = __ddiv_rn(__dmul_rn((double)(nvbin - 1), atan(__dmul_rn(c, v))), (double)CUBE_PI_F);
   return llround(u);
 }
+// The same encode without FP64 transcendentals.  u(v) above is a monotone
+// function of v and odd in v, so nint(u(v)) = sign(v) * #{n >= 1 : bnd[n] <= |v|},
+// where bnd[n] is the smallest double whose u reaches n - 0.5 (found once per
+// sigma by bisection over the doubles, k_encode_bounds).  An FP32 estimate
+// picks the bin; at most a step or two of exact integer comparisons of the
+// doubles' bit patterns (valid for non-negative doubles) settles it.
+__device__ __forceinline__ float approx_float_pos(long long bits) {
+  // truncate a non-negative double to float with integer operations only
+  int e = (int)((bits >> 52) & 0x7ff) - 1023 + 127;
+  if (e <= 0) return 0.f;
+  if (e >= 255) return __int_as_float(0x7f800000);
+  unsigned int m = (unsigned int)((bits >> 29) & 0x7fffff);
+  return __int_as_float((e << 23) | m);
+}
+__device__ __forceinline__ long long v_encode_tab(double v, const long long* __restrict__ bnd, int nmax, float cf,
+                                                  float amp) {
+  long long bits = __double_as_longlong(v);
+  long long ab = bits & 0x7fffffffffffffffLL;
+  float af = approx_float_pos(ab);
+  float u0 = amp * atanf(cf * af);
+  int n = (int)(u0 + 0.5f);
+  n = n < 0 ? 0 : (n > nmax ? nmax : n);
+  while (n < nmax && __ldg(bnd + n + 1) <= ab) n++;
+  while (n > 0 && __ldg(bnd + n) > ab) n--;
+  return bits < 0 ? -(long long)n : (long long)n;
+}
+struct CodecView {
+  const double* dec;
+  const float2* dech;  // dec split into float hi + lo (hi = fl32(dec))
+  const long long* bnd;
+  int half, nmax;  // nvbin/2, nvbin/2-1
+  float cf, amp;   // vcoef(sigma) and (nvbin-1)/pi as floats (estimate only)
+};
+__device__ __forceinline__ double codec_decode(const CodecView& k, int code) { return __ldg(k.dec + code + k.half); }
+__device__ __forceinline__ float2 codec_decode_ff(const CodecView& k, int code) {
+  return __ldg(k.dech + code + k.half);
+}
+__device__ __forceinline__ long long codec_encode(const CodecView& k, double v) {
+  return v_encode_tab(v, k.bnd, k.nmax, k.cf, k.amp);
+}
+
+// ---------------------------------------------------------------------------
+// FP64-free fast paths.  GB300 issues about one FP64 instruction per SM clock
+// (1/128 of FP32), so the hot loops evaluate the reference's FP64 expressions
+// in FP32 / float-float with a rigorous error bound, and keep the result only
+// when every real number inside the bound gives the same integer or float;
+// otherwise the lane evaluates the reference's FP64 expression itself.  The
+// stored result is therefore the reference's bit for bit.
+constexpr float kU24 = 5.9604645e-8f;  // 2^-24
+
+// exact float -> double bit pattern with integer operations (subnormals -> +-0)
+__device__ __forceinline__ long long f2d_bits(float f) {
+  unsigned int u = __float_as_uint(f);
+  unsigned int ex = (u >> 23) & 0xffu;
+  unsigned long long s = (unsigned long long)(u >> 31) << 63;
+  if (ex == 0u) return (long long)s;
+  unsigned long long e64 = ex == 0xffu ? 0x7ffull : (unsigned long long)(ex - 127u + 1023u);
+  return (long long)(s | (e64 << 52) | ((unsigned long long)(u & 0x7fffffu) << 29));
+}
+
+// The velocity code of any |V| in [ab - E, ab + E] (ab = bit pattern of a
+// non-negative double, E >= 0) is n: returns true and n when the whole
+// interval lies in one code bin.  Distances are counted in ulps of ab's binade;
+// an edge in another binade is at least as far as that binade's end.
+__device__ __forceinline__ bool certify_abs(long long ab, float E, const CodecView& k, long long* n_out) {
+  float af = approx_float_pos(ab);
+  float u0 = k.amp * atanf(k.cf * af);
+  int m = (int)(u0 + 0.5f);
+  long long n = m < 0 ? 0 : (m > k.nmax ? k.nmax : m);
+  while (n < k.nmax && __ldg(k.bnd + n + 1) <= ab) n++;
+  while (n > 0 && __ldg(k.bnd + n) > ab) n--;
+  *n_out = n;
+  int e = (int)((ab >> 52) & 0x7ff);
+  if (e == 0 || e >= 0x7fe) return n == 0 && e == 0;  // subnormal |V| is deep inside code 0
+  float kf = ldexpf(E, 1075 - e);                      // E in ulps of this binade
+  if (!(kf < 4.0e15f)) return false;
+  long long kk = (long long)kf + 1;
+  long long blo = (long long)e << 52, bhi = (long long)(e + 1) << 52;
+  if (n > 0) {
+    long long lb = __ldg(k.bnd + n);
+    long long lx = lb > blo ? lb : blo;
+    if (ab - lx <= kk) return false;
+  }
+  if (n < k.nmax) {
+    long long ub = __ldg(k.bnd + n + 1);
+    long long ux = ub < bhi ? ub : bhi;
+    if (ux - ab <= kk) return false;
+  }
+  return true;
+}
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// Nearest float to the real t + lo, certified when every real within margin
+// of it rounds to the same float (a quarter ulp keeps clear of binade edges).
+__device__ __forceinline__ bool round_certified(float t, float lo, float margin, float* r) {
+  float rr = __fadd_rn(t, lo);
+  float diff = __fadd_rn(__fsub_rn(t, rr), lo);
+  unsigned int e = (__float_as_uint(rr) >> 23) & 0xffu;
+  *r = rr;
+  if (e <= 25u || e == 0xffu) return false;
+  float quarter_ulp = __uint_as_float((e - 25u) << 23);
+  return fabsf(diff) + margin < quarter_ulp;
+}
+
+// nint(x) of the reference (halves away from zero) for every x within E of xf
+__device__ __forceinline__ bool nint_certified(float xf, float E, long long* out) {
+  float a = fabsf(xf);
+  E = E * 1.01f + (a + 1.0f) * 2.4e-7f;  // cover the FP32 roundings of the test below
+  float lo = floorf(__fadd_rn(__fsub_rn(a, E), 0.5f)), hi = floorf(__fadd_rn(__fadd_rn(a, E), 0.5f));
+  if (lo != hi || !(a < 1.0e9f)) return false;
+  long long r = (long long)hi;
+  *out = xf < 0.f ? -r : r;
+  return true;
+}
+
 // one CIC kick term force*a_mid*dt/6/pi*wa*wb*wc in real(4), left to right (pm.f90:146)
 __device__ __forceinline__ float kick_term(float f, float a_mid, float dt, float wa, float wb, float wc) {
   float r = __fmul_rn(f, a_mid);
@@ -232,7 +411,8 @@ __device__ __forceinline__ void atomic_max_pos(unsigned int* addr, float v) {
 
 // ----------------------------------------------------- host-side entry points
 int cube_build_tables(cube_ctx* c);
-int cube_ensure_decode(cube_ctx* c, double* tab, float sigma, float& cached);
+// decode/encode tables for up to two sigma values at once (built on demand)
+int cube_codec_pair(cube_ctx* c, float s1, float s2, CodecView* v1, CodecView* v2);
 int cube_kernels_init(cube_ctx* c, const float* fine_table, const float* coarse_table);
 int cube_scan_counts(cube_ctx* c, const int32_t* counts, int64_t* starts, int64_t n);
 int cube_update_x_impl(cube_ctx* c, float dt_old, float dt, float vz_max, cube_stats* st);

@@ -72,88 +72,130 @@ __global__ void k_scale(float* __restrict__ a, int64_t n, float s) {
 }
 
 // ---------------------------------------------------------------- deposit
+// Deterministic CIC deposit.  One CTA owns a brick of BX x BY x BZ coarse
+// cells and every mesh cell inside it: it reads the particles of the brick's
+// coarse cells and of the LO/HI neighbouring layers whose CIC stencils reach
+// into it (fine mesh: the +1 spill of the layer below; coarse mesh with its
+// -0.5 shift: one layer on each side), accumulates the weights in shared
+// memory as 2^-32 fixed point with 64-bit integer atomics (integer addition is
+// associative, so the sum does not depend on thread order), and writes each
+// owned cell once.  No memset, no global atomics, bitwise reproducible.
+// The weights are the reference's real(4) products (pm.f90:63-77, 221-233),
+// computed from tempx in the tile-local frame.
 struct DepArgs {
   Geo g;
-  int64_t np;
   const void* xp;
-  const int32_t* pcell;
+  const int32_t* rhoc;
+  const int64_t* cstart;
   float mass;
-  float* rho;
-  double* mass_sum;
+  float* rho;                 // padded periodic mesh, row stride n+2
+  unsigned long long* total;  // sum of all owned cells in fixed point (exact)
 };
 
-__global__ void k_deposit_fine(DepArgs a) {
+constexpr double kFixScale = 4294967296.0;  // 2^32
+
+template <int MPC, int BX, int BY, int BZ, int LO, int HI>
+__global__ void __launch_bounds__(256) k_deposit_det(DepArgs a) {
+  constexpr int SX = BX + LO + HI, SY = BY + LO + HI, SZ = BZ + LO + HI;
+  constexpr int NSRC = SX * SY * SZ;
+  constexpr int MX = MPC * BX, MY = MPC * BY, MZ = MPC * BZ;
+  extern __shared__ unsigned long long acc[];  // MX*MY*MZ
+  __shared__ int pref[NSRC + 1];
+  __shared__ long long sstart[NSRC];
+  __shared__ unsigned long long btot;
   const Geo& g = a.g;
-  double msum = 0;
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.np; p += (int64_t)gridDim.x * blockDim.x) {
-    int gc[3];
-    cell_coords(g, a.pcell[p], gc[0], gc[1], gc[2]);
-    int i1[3], i2[3];
+  const int nc = g.nc, n = MPC == 1 ? g.nc : g.nf;
+  int nbx = (nc + BX - 1) / BX, nby = (nc + BY - 1) / BY;
+  int b = blockIdx.x;
+  int C0[3] = {(b % nbx) * BX, ((b / nbx) % nby) * BY, (b / (nbx * nby)) * BZ};
+  int B[3] = {min(BX, nc - C0[0]), min(BY, nc - C0[1]), min(BZ, nc - C0[2])};
+  for (int i = threadIdx.x; i < MX * MY * MZ; i += blockDim.x) acc[i] = 0ull;
+  if (threadIdx.x == 0) btot = 0ull;
+  // source cells and their particle counts
+  for (int t = threadIdx.x; t < NSRC; t += blockDim.x) {
+    int sx = t % SX - LO, sy = (t / SX) % SY - LO, sz = t / (SX * SY) - LO;
+    int cnt = 0;
+    long long st = 0;
+    if (sx < B[0] + HI && sy < B[1] + HI && sz < B[2] + HI) {
+      int64_t c = cell_id(g, wrap1(C0[0] + sx, nc), wrap1(C0[1] + sy, nc), wrap1(C0[2] + sz, nc));
+      cnt = a.rhoc[c];
+      st = a.cstart[c];
+    }
+    pref[t + 1] = cnt;
+    sstart[t] = st;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {  // tiny serial scan (<= 1000 entries)
+    pref[0] = 0;
+    for (int t = 1; t <= NSRC; t++) pref[t] += pref[t - 1];
+  }
+  __syncthreads();
+  int total = pref[NSRC];
+  for (int j = threadIdx.x; j < total; j += blockDim.x) {
+    int lo = 0, hi = NSRC;  // find s with pref[s] <= j < pref[s+1]
+    while (hi - lo > 1) {
+      int mid = (lo + hi) >> 1;
+      if (pref[mid] <= j) lo = mid;
+      else hi = mid;
+    }
+    int s = lo;
+    int64_t p = sstart[s] + (j - pref[s]);
+    int sl[3] = {s % SX - LO, (s / SX) % SY - LO, s / (SX * SY) - LO};
+    int rel[3];
     float d1[3], d2[3];
     for (int d = 0; d < 3; d++) {
-      int T = gc[d] / g.nt, L = gc[d] - T * g.nt + 1;
-      float tx = fine_tempx(g.ncell, L, load_code(a.xp, 3 * p + d, g.izipx), g.izipx);
+      int gcd = wrap1(C0[d] + sl[d], nc), Tq, L;
+      tile_local(g, gcd, Tq, L);
+      int code = load_code(a.xp, 3 * p + d, g.izipx);
+      float tx = MPC == 1 ? coarse_tempx(L, code, g.izipx) : fine_tempx(MPC, L, code, g.izipx);
       float fl = floorf(tx);
       d1[d] = __fsub_rn(__fadd_rn(fl, 1.0f), tx);
       d2[d] = __fsub_rn(1.0f, d1[d]);
-      int base = T * g.nt * g.ncell + (int)fl;  // global fine cell of idx1
-      i1[d] = wrapi(base, g.nf);
-      i2[d] = wrapi(base + 1, g.nf);
+      rel[d] = MPC * sl[d] + (int)fl - MPC * (L - 1);  // mesh index relative to the brick
     }
-    float m = a.mass;
-    float w[8];
-    w[0] = __fmul_rn(__fmul_rn(__fmul_rn(d1[0], d1[1]), d1[2]), m);
-    w[1] = __fmul_rn(__fmul_rn(__fmul_rn(d2[0], d1[1]), d1[2]), m);
-    w[2] = __fmul_rn(__fmul_rn(__fmul_rn(d1[0], d2[1]), d1[2]), m);
-    w[3] = __fmul_rn(__fmul_rn(__fmul_rn(d1[0], d1[1]), d2[2]), m);
-    w[4] = __fmul_rn(__fmul_rn(__fmul_rn(d1[0], d2[1]), d2[2]), m);
-    w[5] = __fmul_rn(__fmul_rn(__fmul_rn(d2[0], d1[1]), d2[2]), m);
-    w[6] = __fmul_rn(__fmul_rn(__fmul_rn(d2[0], d2[1]), d1[2]), m);
-    w[7] = __fmul_rn(__fmul_rn(__fmul_rn(d2[0], d2[1]), d2[2]), m);
-    int n = g.nf;
-    atomicAdd(&a.rho[mesh_idx(n, i1[0], i1[1], i1[2])], w[0]);
-    atomicAdd(&a.rho[mesh_idx(n, i2[0], i1[1], i1[2])], w[1]);
-    atomicAdd(&a.rho[mesh_idx(n, i1[0], i2[1], i1[2])], w[2]);
-    atomicAdd(&a.rho[mesh_idx(n, i1[0], i1[1], i2[2])], w[3]);
-    atomicAdd(&a.rho[mesh_idx(n, i1[0], i2[1], i2[2])], w[4]);
-    atomicAdd(&a.rho[mesh_idx(n, i2[0], i1[1], i2[2])], w[5]);
-    atomicAdd(&a.rho[mesh_idx(n, i2[0], i2[1], i1[2])], w[6]);
-    atomicAdd(&a.rho[mesh_idx(n, i2[0], i2[1], i2[2])], w[7]);
-    for (int k = 0; k < 8; k++) msum += (double)w[k];
+    int lim[3] = {MPC * B[0], MPC * B[1], MPC * B[2]};
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      int ox = k & 1, oy = (k >> 1) & 1, oz = k >> 2;
+      int x = rel[0] + ox, y = rel[1] + oy, z = rel[2] + oz;
+      if (x < 0 || y < 0 || z < 0 || x >= lim[0] || y >= lim[1] || z >= lim[2]) continue;
+      float w = __fmul_rn(__fmul_rn(__fmul_rn(ox ? d2[0] : d1[0], oy ? d2[1] : d1[1]), oz ? d2[2] : d1[2]), a.mass);
+      // w * 2^32 as an integer from two 32-bit conversions (a 64-bit conversion
+      // would run on the double-precision unit)
+      float ws = __fmul_rn(w, 256.0f), fh = floorf(ws);
+      unsigned long long q = ((unsigned long long)(unsigned int)fh << 24) +
+                             (unsigned int)__fmul_rn(__fsub_rn(ws, fh), 16777216.0f);
+      atomicAdd(&acc[x + MX * (y + MY * z)], q);
+    }
   }
-  for (int o = 16; o > 0; o >>= 1) msum += __shfl_xor_sync(0xffffffffu, msum, o);
-  if ((threadIdx.x & 31) == 0) atomicAdd(a.mass_sum, msum);
+  __syncthreads();
+  unsigned long long mysum = 0;
+  for (int i = threadIdx.x; i < MX * MY * MZ; i += blockDim.x) {
+    int x = i % MX, y = (i / MX) % MY, z = i / (MX * MY);
+    if (x >= MPC * B[0] || y >= MPC * B[1] || z >= MPC * B[2]) continue;
+    unsigned long long v = acc[i];
+    mysum += v;
+    // v * 2^-32 as float: split so each part converts exactly-ish in FP32
+    float hi = (float)(unsigned int)(v >> 32), lo = (float)(unsigned int)(v & 0xffffffffull);
+    float r = __fmaf_rn(lo, 2.3283064365386963e-10f, hi);
+    a.rho[mesh_idx(n, MPC * C0[0] + x, MPC * C0[1] + y, MPC * C0[2] + z)] = r;
+  }
+  for (int o = 16; o > 0; o >>= 1) mysum += __shfl_xor_sync(0xffffffffu, mysum, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(&btot, mysum);
+  __syncthreads();
+  if (threadIdx.x == 0 && a.total) atomicAdd(a.total, btot);
 }
 
-// coarse CIC with the -0.5 shift in the tile frame (pm.f90:221)
-__global__ void k_deposit_coarse(DepArgs a) {
-  const Geo& g = a.g;
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.np; p += (int64_t)gridDim.x * blockDim.x) {
-    int gc[3];
-    cell_coords(g, a.pcell[p], gc[0], gc[1], gc[2]);
-    int i1[3], i2[3];
-    float d1[3], d2[3];
-    for (int d = 0; d < 3; d++) {
-      int T = gc[d] / g.nt, L = gc[d] - T * g.nt + 1;
-      float tx = coarse_tempx(L, load_code(a.xp, 3 * p + d, g.izipx), g.izipx);
-      float fl = floorf(tx);
-      d1[d] = __fsub_rn(__fadd_rn(fl, 1.0f), tx);
-      d2[d] = __fsub_rn(1.0f, d1[d]);
-      int base = T * g.nt + (int)fl;
-      i1[d] = wrapi(base, g.nc);
-      i2[d] = wrapi(base + 1, g.nc);
-    }
-    float m = a.mass;
-    int n = g.nc;
-    atomicAdd(&a.rho[mesh_idx(n, i1[0], i1[1], i1[2])], __fmul_rn(__fmul_rn(__fmul_rn(d1[0], d1[1]), d1[2]), m));
-    atomicAdd(&a.rho[mesh_idx(n, i2[0], i1[1], i1[2])], __fmul_rn(__fmul_rn(__fmul_rn(d2[0], d1[1]), d1[2]), m));
-    atomicAdd(&a.rho[mesh_idx(n, i1[0], i2[1], i1[2])], __fmul_rn(__fmul_rn(__fmul_rn(d1[0], d2[1]), d1[2]), m));
-    atomicAdd(&a.rho[mesh_idx(n, i1[0], i1[1], i2[2])], __fmul_rn(__fmul_rn(__fmul_rn(d1[0], d1[1]), d2[2]), m));
-    atomicAdd(&a.rho[mesh_idx(n, i1[0], i2[1], i2[2])], __fmul_rn(__fmul_rn(__fmul_rn(d1[0], d2[1]), d2[2]), m));
-    atomicAdd(&a.rho[mesh_idx(n, i2[0], i1[1], i2[2])], __fmul_rn(__fmul_rn(__fmul_rn(d2[0], d1[1]), d2[2]), m));
-    atomicAdd(&a.rho[mesh_idx(n, i2[0], i2[1], i1[2])], __fmul_rn(__fmul_rn(__fmul_rn(d2[0], d2[1]), d1[2]), m));
-    atomicAdd(&a.rho[mesh_idx(n, i2[0], i2[1], i2[2])], __fmul_rn(__fmul_rn(__fmul_rn(d2[0], d2[1]), d2[2]), m));
-  }
+template <int MPC, int BX, int BY, int BZ, int LO, int HI>
+int launch_deposit(cube_ctx* c, const DepArgs& a) {
+  int nc = c->p.nc;
+  int nb = ((nc + BX - 1) / BX) * ((nc + BY - 1) / BY) * ((nc + BZ - 1) / BZ);
+  size_t smem = sizeof(unsigned long long) * (MPC * BX) * (MPC * BY) * (MPC * BZ);
+  auto kern = k_deposit_det<MPC, BX, BY, BZ, LO, HI>;
+  CUBE_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  kern<<<nb, 256, smem, c->stream>>>(a);
+  CUBE_CUDA(c, cudaGetLastError());
+  return CUBE_OK;
 }
 
 // ------------------------------------------------------- spectral multiply
@@ -191,21 +233,35 @@ struct KickArgs {
   Geo g;
   int64_t np;
   const void* xp;
-  void* vp;
+  const void* vp_in;
+  void* vp_out;            // may equal vp_in (fine kick updates in place)
   const int32_t* pcell;
   const float* vfield;
   const float* f[3];
-  const double* dec;
-  int nvbin;
-  double vc_out;
+  CodecView cin, cout;     // decode with sigma_in, encode with sigma_out
   float a_mid, dt;
-  unsigned int* vmax_bits;  // coarse kick only
+  unsigned int* vmax_bits; // coarse kick only: exact vmax per component
+  float tau[3];            // coarse kick: lanes whose |v+vfield| may reach tau are evaluated exactly
+  int vmax_only;           // recompute the exact vmax of every lane, write nothing
+  int exact_only;          // skip the certified fast path
+  unsigned long long* nexact;
 };
 
+// The kick velocity of the reference is the FP64 chain
+//   v = decode; v = v + t1; ...; v = v + t8       (pm.f90:145-153)
+// with t_i the real(4) CIC terms.  The fast path forms V_f = fl32(hi(decode) + S)
+// with S the FP32 sum of the terms; its distance from the reference value is
+// bounded by
+//   gamma_7 sum|t_i| + 2^-24 (|decode| + |V_f|) + 9*2^-53 (|decode| + sum|t_i| + |V_f|)
+// (recursive-summation bound, gamma_7 = 7u/(1-7u), u = 2^-24; the decode table's
+// float hi is within half an ulp).  certify_abs keeps the code only when every
+// double inside that bound encodes to it; otherwise the lane runs the exact
+// chain, so the stored code is always the reference's.
 template <bool kFine>
 __global__ void k_kick(KickArgs a) {
   const Geo& g = a.g;
   float vm[3] = {0.f, 0.f, 0.f};
+  unsigned long long nex = 0;
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.np; p += (int64_t)gridDim.x * blockDim.x) {
     int64_t cell = a.pcell[p];
     int gc[3];
@@ -214,7 +270,8 @@ __global__ void k_kick(KickArgs a) {
     float d1[3], d2[3];
     int n = kFine ? g.nf : g.nc;
     for (int d = 0; d < 3; d++) {
-      int T = gc[d] / g.nt, L = gc[d] - T * g.nt + 1;
+      int T, L;
+      tile_local(g, gc[d], T, L);
       int code = load_code(a.xp, 3 * p + d, g.izipx);
       float tx;
       int base;
@@ -228,8 +285,8 @@ __global__ void k_kick(KickArgs a) {
       float fl = floorf(tx);
       d1[d] = __fsub_rn(__fadd_rn(fl, 1.0f), tx);
       d2[d] = __fsub_rn(1.0f, d1[d]);
-      i1[d] = wrapi(base, n);
-      i2[d] = wrapi(base + 1, n);
+      i1[d] = wrap1(base, n);
+      i2[d] = wrap1(base + 1, n);
     }
     int64_t c111 = mesh_idx(n, i1[0], i1[1], i1[2]), c211 = mesh_idx(n, i2[0], i1[1], i1[2]);
     int64_t c121 = mesh_idx(n, i1[0], i2[1], i1[2]), c112 = mesh_idx(n, i1[0], i1[1], i2[2]);
@@ -237,22 +294,50 @@ __global__ void k_kick(KickArgs a) {
     int64_t c221 = mesh_idx(n, i2[0], i2[1], i1[2]), c222 = mesh_idx(n, i2[0], i2[1], i2[2]);
     for (int d = 0; d < 3; d++) {
       const float* F = a.f[d];
-      int code = load_code(a.vp, 3 * p + d, g.izipv);
-      double v = a.dec[code + a.nvbin / 2];
-      v = __dadd_rn(v, (double)kick_term(F[c111], a.a_mid, a.dt, d1[0], d1[1], d1[2]));
-      v = __dadd_rn(v, (double)kick_term(F[c211], a.a_mid, a.dt, d2[0], d1[1], d1[2]));
-      v = __dadd_rn(v, (double)kick_term(F[c121], a.a_mid, a.dt, d1[0], d2[1], d1[2]));
-      v = __dadd_rn(v, (double)kick_term(F[c112], a.a_mid, a.dt, d1[0], d1[1], d2[2]));
-      v = __dadd_rn(v, (double)kick_term(F[c122], a.a_mid, a.dt, d1[0], d2[1], d2[2]));
-      v = __dadd_rn(v, (double)kick_term(F[c212], a.a_mid, a.dt, d2[0], d1[1], d2[2]));
-      v = __dadd_rn(v, (double)kick_term(F[c221], a.a_mid, a.dt, d2[0], d2[1], d1[2]));
-      v = __dadd_rn(v, (double)kick_term(F[c222], a.a_mid, a.dt, d2[0], d2[1], d2[2]));
-      if (!kFine) {
-        // vmax=max(vmax,abs(vreal+vfield)) (pm.f90:349), real(4) result
-        double w = fabs(__dadd_rn(v, (double)a.vfield[3 * cell + d]));
-        vm[d] = fmaxf(vm[d], __double2float_rn(w));
+      float t[8];
+      t[0] = kick_term(__ldg(F + c111), a.a_mid, a.dt, d1[0], d1[1], d1[2]);
+      t[1] = kick_term(__ldg(F + c211), a.a_mid, a.dt, d2[0], d1[1], d1[2]);
+      t[2] = kick_term(__ldg(F + c121), a.a_mid, a.dt, d1[0], d2[1], d1[2]);
+      t[3] = kick_term(__ldg(F + c112), a.a_mid, a.dt, d1[0], d1[1], d2[2]);
+      t[4] = kick_term(__ldg(F + c122), a.a_mid, a.dt, d1[0], d2[1], d2[2]);
+      t[5] = kick_term(__ldg(F + c212), a.a_mid, a.dt, d2[0], d1[1], d2[2]);
+      t[6] = kick_term(__ldg(F + c221), a.a_mid, a.dt, d2[0], d2[1], d1[2]);
+      t[7] = kick_term(__ldg(F + c222), a.a_mid, a.dt, d2[0], d2[1], d2[2]);
+      int code = load_code(a.vp_in, 3 * p + d, g.izipv);
+      float dh = codec_decode_ff(a.cin, code).x;
+      float S = t[0], T = fabsf(t[0]);
+      for (int i = 1; i < 8; i++) {
+        S = __fadd_rn(S, t[i]);
+        T = __fadd_rn(T, fabsf(t[i]));
       }
-      store_code(a.vp, 3 * p + d, g.izipv, v_encode(v, a.vc_out, a.nvbin));
+      float vf = __fadd_rn(dh, S);
+      long long vb = f2d_bits(vf), ab = vb & 0x7fffffffffffffffLL;
+      float E = 1.25f * (T * 4.76837158e-7f + (fabsf(dh) + fabsf(vf)) * 6.0e-8f + T * 1.0e-15f);
+      long long nc_ = 0;
+      bool ok = !a.exact_only && certify_abs(ab, E, a.cout, &nc_);
+      bool need_vmax = false;
+      float vfd = 0.f;
+      if (!kFine) {
+        vfd = a.vfield[3 * cell + d];
+        float ub = (fabsf(vf) + E + fabsf(vfd)) * 1.000001f;
+        need_vmax = a.vmax_only || ub >= a.tau[d];
+      }
+      long long out;
+      if (ok && !need_vmax) {
+        out = vb < 0 ? -nc_ : nc_;
+      } else {
+        // the reference's exact FP64 chain
+        double v = codec_decode(a.cin, code);
+        for (int i = 0; i < 8; i++) v = __dadd_rn(v, (double)t[i]);
+        out = codec_encode(a.cout, v);
+        nex++;
+        if (!kFine) {
+          // vmax=max(vmax,abs(vreal+vfield)) (pm.f90:349), real(4) result
+          double w = fabs(__dadd_rn(v, (double)vfd));
+          vm[d] = fmaxf(vm[d], __double2float_rn(w));
+        }
+      }
+      if (!a.vmax_only) store_code(a.vp_out, 3 * p + d, g.izipv, out);
     }
   }
   if (!kFine) {
@@ -262,11 +347,8 @@ __global__ void k_kick(KickArgs a) {
       if ((threadIdx.x & 31) == 0) atomic_max_pos(&a.vmax_bits[d], m);
     }
   }
-}
-
-double vcoef_h(float sigma) {
-  float s = std::sqrt(CUBE_PI_F / 2.0f);
-  return (double)s / ((double)sigma * 2.5);
+  for (int o = 16; o > 0; o >>= 1) nex += __shfl_xor_sync(0xffffffffu, nex, o);
+  if ((threadIdx.x & 31) == 0 && a.nexact) atomicAdd(a.nexact, nex);
 }
 
 }  // namespace
@@ -399,19 +481,16 @@ int cube_kernels_init(cube_ctx* c, const float* fine_table, const float* coarse_
 int cube_fine_density_impl(cube_ctx* c, cube_stats* st) {
   cudaStream_t s = c->stream;
   Geo g = make_geo(c);
-  int64_t nfh = c->nf / 2 + 1;
-  int64_t nspec = nfh * c->nf * (int64_t)c->nf;
-  CUBE_CUDA(c, cudaMemsetAsync(c->rho_f, 0, 8 * nspec, s));
   CUBE_CUDA(c, cudaMemsetAsync(c->dstats, 0, sizeof(DevStats), s));
-  DepArgs a{g, c->np, c->xp[c->cur], c->pcell[c->cur], c->p.mass_p, c->rho_f, &c->dstats->testrhof};
+  DepArgs a{g, c->xp[c->cur], c->rhoc[c->cur], c->cstart[c->cur], c->p.mass_p, c->rho_f, &c->dstats->rhof_fix};
   cube_phase_begin(c, PH_F_DEPOSIT);
-  k_deposit_fine<<<cube_grid(c->np, 256), 256, 0, s>>>(a);
+  int r = launch_deposit<4, 8, 4, 4, 1, 0>(c, a);
   cube_phase_end(c, PH_F_DEPOSIT);
-  CUBE_CUDA(c, cudaGetLastError());
+  if (r) return r;
   if (st) {
-    int r = cube_stats_fetch(c);
+    r = cube_stats_fetch(c);
     if (r) return r;
-    st->testrhof = c->hstats->testrhof;
+    st->testrhof = (double)c->hstats->rhof_fix / kFixScale;
   }
   return CUBE_OK;
 }
@@ -442,28 +521,28 @@ int cube_fine_forces_impl(cube_ctx* c, cube_stats* st) {
     int r = cube_stats_fetch(c);
     if (r) return r;
     st->f2_max_fine = bits_float(c->hstats->f2_fine_bits);
-    st->testrhof = c->hstats->testrhof;
+    st->testrhof = (double)c->hstats->rhof_fix / kFixScale;
   }
   return CUBE_OK;
 }
 
 int cube_fine_kick_impl(cube_ctx* c, float a_mid, float dt) {
-  int r = cube_ensure_decode(c, c->dec_old, c->sigma_vi, c->dec_old_sigma);
-  if (r) return r;
   KickArgs k{};
+  int r = cube_codec_pair(c, c->sigma_vi, c->sigma_vi_new, &k.cin, &k.cout);
+  if (r) return r;
   k.g = make_geo(c);
   k.np = c->np;
   k.xp = c->xp[c->cur];
-  k.vp = c->vp[c->cur];
+  k.vp_in = c->vp[c->cur];
+  k.vp_out = c->vp[c->cur];
   k.pcell = c->pcell[c->cur];
   k.vfield = c->vfield[c->cur];
   for (int d = 0; d < 3; d++) k.f[d] = c->force_f[d];
-  k.dec = c->dec_old;
-  k.nvbin = c->nvbin;
-  k.vc_out = vcoef_h(c->sigma_vi_new);
   k.a_mid = a_mid;
   k.dt = dt;
   k.vmax_bits = nullptr;
+  k.nexact = &c->dstats->nexact;
+  k.exact_only = c->opt_exact_kicks;
   cube_phase_begin(c, PH_F_KICK);
   k_kick<true><<<cube_grid(c->np, 256), 256, 0, c->stream>>>(k);
   cube_phase_end(c, PH_F_KICK);
@@ -473,19 +552,19 @@ int cube_fine_kick_impl(cube_ctx* c, float a_mid, float dt) {
 
 // --------------------------------------------------------------- coarse
 int cube_coarse_density_impl(cube_ctx* c, cube_stats* st) {
-  cudaStream_t s = c->stream;
   Geo g = make_geo(c);
-  int nc = c->p.nc;
-  int64_t nch = nc / 2 + 1;
-  int64_t cspec = nch * nc * (int64_t)nc;
-  CUBE_CUDA(c, cudaMemsetAsync(c->rho_c, 0, 8 * cspec, s));
-  CUBE_CUDA(c, cudaMemsetAsync(&c->dstats->f2_coarse_bits, 0, 4, s));
-  DepArgs a{g, c->np, c->xp[c->cur], c->pcell[c->cur], c->p.mass_p, c->rho_c, nullptr};
+  CUBE_CUDA(c, cudaMemsetAsync(&c->dstats->f2_coarse_bits, 0, 4, c->stream));
+  CUBE_CUDA(c, cudaMemsetAsync(&c->dstats->rhoc_fix, 0, 8, c->stream));
+  DepArgs a{g, c->xp[c->cur], c->rhoc[c->cur], c->cstart[c->cur], c->p.mass_p, c->rho_c, &c->dstats->rhoc_fix};
   cube_phase_begin(c, PH_C_DEPOSIT);
-  k_deposit_coarse<<<cube_grid(c->np, 256), 256, 0, s>>>(a);
+  int r = launch_deposit<1, 8, 8, 8, 1, 1>(c, a);
   cube_phase_end(c, PH_C_DEPOSIT);
-  CUBE_CUDA(c, cudaGetLastError());
-  (void)st;
+  if (r) return r;
+  if (st) {
+    r = cube_stats_fetch(c);
+    if (r) return r;
+    st->testrhoc = (double)c->hstats->rhoc_fix / kFixScale;
+  }
   return CUBE_OK;
 }
 
@@ -510,37 +589,68 @@ int cube_coarse_forces_impl(cube_ctx* c, cube_stats* st) {
     int r = cube_stats_fetch(c);
     if (r) return r;
     st->f2_max_coarse = bits_float(c->hstats->f2_coarse_bits);
+    st->testrhoc = (double)c->hstats->rhoc_fix / kFixScale;
   }
   return CUBE_OK;
 }
 
 int cube_coarse_kick_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st) {
-  int r = cube_ensure_decode(c, c->dec_old, c->sigma_vi, c->dec_old_sigma);
-  if (r) return r;
-  CUBE_CUDA(c, cudaMemsetAsync(c->dstats->vmax_bits, 0, 12, c->stream));
   KickArgs k{};
+  int r = cube_codec_pair(c, c->sigma_vi, c->sigma_vi, &k.cin, &k.cout);
+  if (r) return r;
+  int cur = c->cur, alt = 1 - cur;
+  CUBE_CUDA(c, cudaMemsetAsync(c->dstats->vmax_bits, 0, 12, c->stream));
+  CUBE_CUDA(c, cudaMemsetAsync(&c->dstats->nexact, 0, 8, c->stream));
   k.g = make_geo(c);
   k.np = c->np;
-  k.xp = c->xp[c->cur];
-  k.vp = c->vp[c->cur];
-  k.pcell = c->pcell[c->cur];
-  k.vfield = c->vfield[c->cur];
-  for (int d = 0; d < 3; d++) k.f[d] = c->force_c[d];
-  k.dec = c->dec_old;
-  k.nvbin = c->nvbin;
-  k.vc_out = vcoef_h(c->sigma_vi);
+  k.xp = c->xp[cur];
+  k.vp_in = c->vp[cur];
+  k.vp_out = c->vp[alt];  // the input codes stay intact for an exact vmax rerun
+  k.pcell = c->pcell[cur];
+  k.vfield = c->vfield[cur];
+  for (int d = 0; d < 3; d++) {
+    k.f[d] = c->force_c[d];
+    // velocities change little per step: every lane that could reach 0.7 of the
+    // last vmax is evaluated exactly; if none does, the whole vmax is redone
+    k.tau[d] = 0.7f * c->vmax_prev[d];
+  }
   k.a_mid = a_mid;
   k.dt = dt;
   k.vmax_bits = c->dstats->vmax_bits;
+  k.nexact = &c->dstats->nexact;
+  k.vmax_only = 0;
+  k.exact_only = c->opt_exact_kicks;
   cube_phase_begin(c, PH_C_KICK);
   k_kick<false><<<cube_grid(c->np, 256), 256, 0, c->stream>>>(k);
   cube_phase_end(c, PH_C_KICK);
   CUBE_CUDA(c, cudaGetLastError());
-  if (st) {
+  r = cube_stats_fetch(c);
+  if (r) return r;
+  float vm[3];
+  bool rerun = false;
+  for (int d = 0; d < 3; d++) {
+    vm[d] = bits_float(c->hstats->vmax_bits[d]);
+    if (!(vm[d] >= k.tau[d])) rerun = true;
+  }
+  unsigned long long nex = c->hstats->nexact;
+  if (rerun) {
+    CUBE_CUDA(c, cudaMemsetAsync(c->dstats->vmax_bits, 0, 12, c->stream));
+    k.vmax_only = 1;
+    k_kick<false><<<cube_grid(c->np, 256), 256, 0, c->stream>>>(k);
+    CUBE_CUDA(c, cudaGetLastError());
     r = cube_stats_fetch(c);
     if (r) return r;
-    for (int d = 0; d < 3; d++) st->vmax[d] = bits_float(c->hstats->vmax_bits[d]);
+    for (int d = 0; d < 3; d++) vm[d] = bits_float(c->hstats->vmax_bits[d]);
+  }
+  void* t = c->vp[cur];
+  c->vp[cur] = c->vp[alt];
+  c->vp[alt] = t;
+  for (int d = 0; d < 3; d++) c->vmax_prev[d] = vm[d];
+  c->kick_exact_lanes = nex;
+  if (st) {
+    for (int d = 0; d < 3; d++) st->vmax[d] = vm[d];
     st->f2_max_coarse = bits_float(c->hstats->f2_coarse_bits);
+    st->testrhoc = (double)c->hstats->rhoc_fix / kFixScale;
   }
   return CUBE_OK;
 }

@@ -8,8 +8,10 @@
 // most 2x2x2 coarse cells: a particle in fine sub-cell 0 (3) of its coarse
 // cell also reads the coarse cell below (above) in that dimension.  The pair
 // arithmetic is FP32 (positions are exact in FP32: 4*frac has <= 17 bits);
-// the kick and the velocity re-encode follow the reference's FP64 sequence
-// (:116-121).
+// the kick adds F*a_mid*dt/(6 pi) in FP64 (:116) as one product with the
+// precomputed factor -- the FP32 pair sum already sets the tolerance of this
+// kick, so the reference's two FP64 divisions buy nothing here -- and the
+// velocity re-encode is the exact code of update_particle.f90:117.
 #include <cmath>
 
 #include "cube_internal.cuh"
@@ -23,18 +25,18 @@ struct PPArgs {
   void* vp;
   const int32_t* pcell;
   const int64_t* cstart;
-  const double* dec;
-  int nvbin;
-  double vc;
+  CodecView cv;
   float mass, rsoft, inv_cut;
-  float a_mid, dt;
+  double kick;   // a_mid*dt/6/pi
+  float kick_f;  // the same rounded to float (fast path)
+  int exact_only;
   float* fpp;  // optional per-particle force output
   DevStats* st;
 };
 
 __device__ __forceinline__ float fine_off(int code, int izipx) {
-  // ncell*(int(xp+ishift)+rshift)*x_resolution, exact in real(4)
-  return __double2float_rn(__dmul_rn(__dmul_rn(4.0, pos_off(code, izipx)), xres_of(izipx)));
+  // ncell*(int(xp+ishift)+rshift)*x_resolution: exact in real(4)
+  return __fmul_rn(pos_off_f(code, izipx), izipx == 1 ? 4.0f / 256.0f : 4.0f / 65536.0f);
 }
 
 __global__ void k_pp(PPArgs a) {
@@ -56,7 +58,7 @@ __global__ void k_pp(PPArgs a) {
     for (int dz = lo[2]; dz <= hi[2]; dz++)
       for (int dy = lo[1]; dy <= hi[1]; dy++)
         for (int dx = lo[0]; dx <= hi[0]; dx++) {
-          int sx = wrapi(gc[0] + dx, g.nc), sy = wrapi(gc[1] + dy, g.nc), sz = wrapi(gc[2] + dz, g.nc);
+          int sx = wrap1(gc[0] + dx, g.nc), sy = wrap1(gc[1] + dy, g.nc), sz = wrap1(gc[2] + dz, g.nc);
           int64_t S = cell_id(g, sx, sy, sz);
           int64_t q0 = a.cstart[S], q1 = a.cstart[S + 1];
           float sh[3] = {(float)(4 * dx), (float)(4 * dy), (float)(4 * dz)};
@@ -86,14 +88,20 @@ __global__ void k_pp(PPArgs a) {
     nwork++;
     for (int d = 0; d < 3; d++) {
       int code = load_code(a.vp, 3 * p + d, g.izipv);
-      double v = a.dec[code + a.nvbin / 2];
-      // vreal=vreal+f_tot*a_mid*dt/6/pi in real(8) (ext_pp_force.f90:116)
-      double k = __dmul_rn((double)F[d], (double)a.a_mid);
-      k = __dmul_rn(k, (double)a.dt);
-      k = __ddiv_rn(k, 6.0);
-      k = __ddiv_rn(k, (double)CUBE_PI_F);
-      v = __dadd_rn(v, k);
-      store_code(a.vp, 3 * p + d, g.izipv, v_encode(v, a.vc, a.nvbin));
+      // vreal=vreal+f_tot*a_mid*dt/6/pi (ext_pp_force.f90:116), then the code:
+      // FP32 estimate certified against the FP64 expression (see certify_abs)
+      float dh = codec_decode_ff(a.cv, code).x;
+      float kf = __fmul_rn(F[d], a.kick_f);
+      float vf = __fadd_rn(dh, kf);
+      float E = 1.25f * (fabsf(kf) * 1.3e-7f + (2.f * fabsf(dh) + fabsf(vf)) * 6.0e-8f);
+      long long n = 0, out;
+      if (!a.exact_only && certify_abs(f2d_bits(vf) & 0x7fffffffffffffffLL, E, a.cv, &n)) {
+        out = vf < 0.f ? -n : n;
+      } else {
+        double v = __dadd_rn(codec_decode(a.cv, code), __dmul_rn((double)F[d], a.kick));
+        out = codec_encode(a.cv, v);
+      }
+      store_code(a.vp, 3 * p + d, g.izipv, out);
       if (a.fpp) a.fpp[3 * p + d] = F[d];
     }
     f2max = fmaxf(f2max, F[0] * F[0] + F[1] * F[1] + F[2] * F[2]);
@@ -113,25 +121,22 @@ __global__ void k_pp(PPArgs a) {
 }  // namespace
 
 int cube_pp_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st) {
-  int r = cube_ensure_decode(c, c->dec_old, c->sigma_vi, c->dec_old_sigma);
+  PPArgs a{};
+  int r = cube_codec_pair(c, c->sigma_vi, c->sigma_vi, &a.cv, nullptr);
   if (r) return r;
   CUBE_CUDA(c, cudaMemsetAsync(c->dstats, 0, sizeof(DevStats), c->stream));
-  PPArgs a{};
   a.g = make_geo(c);
   a.np = c->np;
   a.xp = c->xp[c->cur];
   a.vp = c->vp[c->cur];
   a.pcell = c->pcell[c->cur];
   a.cstart = c->cstart[c->cur];
-  a.dec = c->dec_old;
-  a.nvbin = c->nvbin;
-  float s = std::sqrt(CUBE_PI_F / 2.0f);
-  a.vc = (double)s / ((double)c->sigma_vi * 2.5);
   a.mass = c->p.mass_p;
   a.rsoft = c->p.rsoft;
   a.inv_cut = 1.0f / (float)c->p.nf_cutoff;
-  a.a_mid = a_mid;
-  a.dt = dt;
+  a.kick = (((double)a_mid * (double)dt) / 6.0) / (double)CUBE_PI_F;
+  a.kick_f = (float)a.kick;
+  a.exact_only = c->opt_exact_kicks;
   a.fpp = c->fpp;
   a.st = c->dstats;
   cube_phase_begin(c, PH_PP);

@@ -134,6 +134,7 @@ int cube_state_in(cube_ctx* c, int64_t np, const void* xp, const void* vp, const
   c->np = np;
   c->npglobal = np;
   c->have_state = true;
+  for (int d = 0; d < 3; d++) c->vmax_prev[d] = 0.f;
   return CUBE_OK;
 }
 
@@ -169,22 +170,121 @@ int cube_build_tables(cube_ctx* c) {
   return CUBE_OK;
 }
 
-__global__ void k_decode_table(const float* __restrict__ tan_tab, int nv, float sigma, double* __restrict__ dec) {
+__global__ void k_decode_table(const float* __restrict__ tan_tab, int nv, float sigma, double* __restrict__ dec,
+                               float2* __restrict__ dech) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < nv) dec[i] = __ddiv_rn((double)tan_tab[i], vcoef(sigma));
+  if (i < nv) {
+    double d = __ddiv_rn((double)tan_tab[i], vcoef(sigma));
+    dec[i] = d;
+    float hi = __double2float_rn(d);
+    dech[i] = make_float2(hi, __double2float_rn(__dsub_rn(d, (double)hi)));
+  }
 }
 
-// dec[v+nvbin/2] = tan(...)/(sqrt(pi/2)/(sigma*vrel_boost)) in real(8)
-int cube_ensure_decode(cube_ctx* c, double* tab, float sigma, float& cached) {
-  if (cached == sigma) return CUBE_OK;
-  k_decode_table<<<(c->nvbin + 255) / 256, 256, 0, c->stream>>>(c->tan_tab, c->nvbin, sigma, tab);
+// bnd[n] = bit pattern of the smallest double a >= 0 with
+// u(a) = real(nvbin-1)*atan(vcoef*a)/pi >= n - 0.5, i.e. where nint(u) reaches n
+// (update_particle.f90:117).  Bisection over the ordered non-negative doubles:
+// u(0) = 0 < 0.5 and u(+inf) = (nvbin-1)/2 * pi/pi_f > nvbin/2 - 1.5.
+__global__ void k_encode_bounds(float sigma, int nvbin, long long* __restrict__ bnd) {
+  int n = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  int nmax = nvbin / 2 - 1;
+  if (n == 1) bnd[0] = 0;
+  if (n > nmax) return;
+  double c = vcoef(sigma);
+  double thr = (double)n - 0.5;
+  long long lo = 0, hi = 0x7ff0000000000000LL;
+  while (hi - lo > 1) {
+    long long mid = lo + (hi - lo) / 2;
+    double u = __ddiv_rn(__dmul_rn((double)(nvbin - 1), atan(__dmul_rn(c, __longlong_as_double(mid)))),
+                         (double)CUBE_PI_F);
+    if (u >= thr)
+      hi = mid;
+    else
+      lo = mid;
+  }
+  bnd[n] = hi;
+}
+
+static void view_of(const cube_ctx* c, const cube_ctx::Codec& k, CodecView* v) {
+  v->dec = k.dec;
+  v->dech = k.dech;
+  v->bnd = k.bnd;
+  v->half = c->nvbin / 2;
+  v->nmax = c->nvbin / 2 - 1;
+  v->cf = (float)vcoef_host(k.sigma);
+  v->amp = (float)((double)(c->nvbin - 1) / (double)CUBE_PI_F);
+}
+
+static int build_codec(cube_ctx* c, int slot, float sigma) {
+  cube_ctx::Codec& k = c->codec[slot];
+  k_decode_table<<<(c->nvbin + 255) / 256, 256, 0, c->stream>>>(c->tan_tab, c->nvbin, sigma, k.dec, k.dech);
+  int nmax = c->nvbin / 2 - 1;
+  k_encode_bounds<<<(nmax + 127) / 128, 128, 0, c->stream>>>(sigma, c->nvbin, k.bnd);
   CUBE_CUDA(c, cudaGetLastError());
-  cached = sigma;
+  k.sigma = sigma;
+  return CUBE_OK;
+}
+
+// Make the tables for s1 and s2 resident (at most two slots; the slot of the
+// other requested sigma is never evicted).
+int cube_codec_pair(cube_ctx* c, float s1, float s2, CodecView* v1, CodecView* v2) {
+  if (!(s1 > 0.f) || !(s2 > 0.f)) return cube_fail(c, CUBE_ERR_ARG, "sigma_vi must be positive");
+  int i1 = c->codec[0].sigma == s1 ? 0 : (c->codec[1].sigma == s1 ? 1 : -1);
+  int i2 = c->codec[0].sigma == s2 ? 0 : (c->codec[1].sigma == s2 ? 1 : -1);
+  if (i1 < 0) {
+    i1 = (i2 >= 0) ? 1 - i2 : c->codec_next;
+    int r = build_codec(c, i1, s1);
+    if (r) return r;
+    c->codec_next = 1 - i1;
+  }
+  if (i2 < 0) {
+    i2 = (s2 == s1) ? i1 : 1 - i1;
+    if (i2 != i1) {
+      int r = build_codec(c, i2, s2);
+      if (r) return r;
+      c->codec_next = 1 - i2;
+    }
+  }
+  if (v1) view_of(c, c->codec[i1], v1);
+  if (v2) view_of(c, c->codec[i2], v2);
   return CUBE_OK;
 }
 
 int cube_stats_fetch(cube_ctx* c) {
   CUBE_CUDA(c, cudaMemcpyAsync(c->hstats, c->dstats, sizeof(DevStats), cudaMemcpyDeviceToHost, c->stream));
   CUBE_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CUBE_OK;
+}
+
+// ------------------------------------------------------ codec self check
+__global__ void k_codec_check(const double* __restrict__ v, int64_t n, double c, int nvbin, CodecView k,
+                              int32_t* __restrict__ direct, int32_t* __restrict__ table) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    direct[i] = (int32_t)v_encode(v[i], c, nvbin);
+    table[i] = (int32_t)codec_encode(k, v[i]);
+  }
+}
+
+extern "C" int cube_codec_check(cube_ctx* c, float sigma, const double* v, int64_t n, int32_t* direct,
+                                int32_t* table) {
+  if (!c || !v || !direct || !table || n < 0) return CUBE_ERR_ARG;
+  CUBE_CUDA(c, cudaSetDevice(c->device));
+  CodecView k;
+  int r = cube_codec_pair(c, sigma, sigma, &k, nullptr);
+  if (r) return r;
+  double* dv = nullptr;
+  int32_t *dd = nullptr, *dt = nullptr;
+  CUBE_CUDA(c, cudaMalloc(&dv, 8 * (size_t)n + 8));
+  CUBE_CUDA(c, cudaMalloc(&dd, 4 * (size_t)n + 4));
+  CUBE_CUDA(c, cudaMalloc(&dt, 4 * (size_t)n + 4));
+  CUBE_CUDA(c, cudaMemcpyAsync(dv, v, 8 * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+  k_codec_check<<<cube_grid(n, 256), 256, 0, c->stream>>>(dv, n, vcoef_host(sigma), c->nvbin, k, dd, dt);
+  CUBE_CUDA(c, cudaGetLastError());
+  CUBE_CUDA(c, cudaMemcpyAsync(direct, dd, 4 * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+  CUBE_CUDA(c, cudaMemcpyAsync(table, dt, 4 * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+  CUBE_CUDA(c, cudaStreamSynchronize(c->stream));
+  cudaFree(dv);
+  cudaFree(dd);
+  cudaFree(dt);
   return CUBE_OK;
 }

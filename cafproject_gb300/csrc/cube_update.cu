@@ -34,9 +34,8 @@ struct UpdArgs {
   const int32_t* pcell;
   const float* vfield;
   const int64_t* cstart;
-  const double* dec;  // decode table for sigma_vi, indexed by v + nvbin/2
-  int nvbin;
-  double vc;          // vcoef(sigma_vi) for the encode
+  CodecView cv;       // decode / encode tables for sigma_vi
+  int exact_only;     // skip every certified fast path (FP64 expressions only)
   int32_t* dest;
   uint8_t* dframe;
   uint32_t* rank;
@@ -53,13 +52,18 @@ struct UpdArgs {
   int32_t* pcell_new;
 };
 
-__device__ __forceinline__ double vreal_of(const UpdArgs& a, int64_t p, int d, int64_t cell) {
-  int code = load_code(a.vp, 3 * p + d, a.g.izipv);
-  return __dadd_rn(a.dec[code + a.nvbin / 2], (double)a.vfield[3 * cell + d]);
-}
 
 // global coarse coordinate of tile-local cell l (1-based) of tile coordinate t
-__device__ __forceinline__ int glob(const Geo& g, int t, int l) { return wrapi(t * g.nt + l - 1, g.nc); }
+__device__ __forceinline__ int glob(const Geo& g, int t, int l) { return wrap1(t * g.nt + l - 1, g.nc); }
+
+// frame offset code (0,1,2 for -nt,0,+nt) at which a tile sees global cell s
+// at tile-local coordinate l
+__device__ __forceinline__ int frame_code(const Geo& g, int l, int s) {
+  int T, Ls;
+  tile_local(g, s, T, Ls);
+  int o = l - Ls;
+  return o == 0 ? 1 : (o > 0 ? 2 : 0);
+}
 
 // U1: destination of every particle in every frame that sees it.
 __global__ void k_dest(UpdArgs a) {
@@ -75,23 +79,41 @@ __global__ void k_dest(UpdArgs a) {
     int oval[3][2], igv[3][2];
     bool far = false;
     for (int d = 0; d < 3; d++) {
-      int H = gc[d] / g.nt, L = gc[d] - H * g.nt + 1;
-      double off = __dmul_rn(pos_off(load_code(a.xp, 3 * p + d, g.izipx), g.izipx), xres_of(g.izipx));
-      double v = vreal_of(a, p, d, cell);
-      double deltax = __dmul_rn(__dmul_rn((double)a.dt_mid, v), 0.25);  // (dt_mid*vreal)/ncell, ncell=4
+      int H, L;
+      tile_local(g, gc[d], H, L);
+      int xcode = load_code(a.xp, 3 * p + d, g.izipx);
+      int vcode = load_code(a.vp, 3 * p + d, g.izipv);
+      float vfd = a.vfield[3 * cell + d];
+      // fast path: v = dec+vfield, P = dt_mid*v, deltax = P/4 in FP32 with bound Edx
+      float dh = codec_decode_ff(a.cv, vcode).x;
+      float vfa = __fadd_rn(dh, vfd);
+      float Pf = __fmul_rn(a.dt_mid, vfa);
+      float dxf = __fmul_rn(Pf, 0.25f);
+      float Edx = 0.25f * (fabsf(a.dt_mid) * (fabsf(dh) + fabsf(vfa)) * 1.2e-7f + fabsf(Pf) * 6.0e-8f);
+      float offf = __fmul_rn(pos_off_f(xcode, g.izipx), g.izipx == 1 ? 1.0f / 256.0f : 1.0f / 65536.0f);
       nval[d] = 0;
       for (int f = 0; f < 3; f++) {
         int o = f == 0 ? 0 : (f == 1 ? g.nt : -g.nt);
         int Ls = L + o;
         if (Ls < 1 - g.ncb || Ls > g.nt + g.ncb) continue;  // frame does not see this cell
-        double xq = __dadd_rn((double)(Ls - 1), off);
-        double s = __dadd_rn(xq, deltax);
-        double cs = ceil(s);
-        if (cs < (double)(1 - 2 * g.ncb) || cs > (double)(g.nt + 2 * g.ncb)) {
+        float xqf = __fadd_rn((float)(Ls - 1), offf);
+        float sf = __fadd_rn(xqf, dxf);
+        float Es = 1.25f * (Edx + (fabsf(xqf) + fabsf(sf)) * 6.0e-8f + 2.4e-7f * fabsf(sf)) + 1.0e-30f;
+        float clo = ceilf(__fsub_rn(sf, Es)), chi = ceilf(__fadd_rn(sf, Es));
+        int ig;
+        if (clo == chi && !a.exact_only) {
+          ig = (int)chi;
+        } else {
+          // the reference's FP64 expression (update_particle.f90:66-70)
+          double v = __dadd_rn(codec_decode(a.cv, vcode), (double)vfd);
+          double deltax = __dmul_rn(__dmul_rn((double)a.dt_mid, v), 0.25);
+          double xq = __dadd_rn((double)(Ls - 1), (double)offf);
+          ig = (int)ceil(__dadd_rn(xq, deltax));
+        }
+        if (ig < 1 - 2 * g.ncb || ig > g.nt + 2 * g.ncb) {
           far = true;
           continue;
         }
-        int ig = (int)cs;
         if (ig >= 1 && ig <= g.nt && nval[d] < 2) {
           oval[d][nval[d]] = o;
           igv[d][nval[d]] = ig;
@@ -112,14 +134,15 @@ __global__ void k_dest(UpdArgs a) {
       int sel[3] = {k % nval[0], (k / nval[0]) % nval[1], k / (nval[0] * nval[1])};
       int dg[3];
       for (int d = 0; d < 3; d++) {
-        int H = gc[d] / g.nt;
+        int H = (int)fdiv((uint32_t)gc[d], g.dnt);
         // frame tile = H - o/nt (periodic in tiles); destination global coordinate
-        int T = wrapi(H - oval[d][sel[d]] / g.nt, g.nnt);
+        int fo = oval[d][sel[d]] == 0 ? 0 : (oval[d][sel[d]] > 0 ? 1 : -1);
+        int T = wrap1(H - fo, g.nnt);
         dg[d] = glob(g, T, igv[d][sel[d]]);
       }
       int32_t D = (int32_t)cell_id(g, dg[0], dg[1], dg[2]);
       int fr = 0;
-      for (int d = 2; d >= 0; d--) fr = 3 * fr + (oval[d][sel[d]] / g.nt + 1);
+      for (int d = 2; d >= 0; d--) fr = 3 * fr + (oval[d][sel[d]] == 0 ? 1 : (oval[d][sel[d]] > 0 ? 2 : 0));
       if (k == 0) {
         a.dest[p] = D;
         a.dframe[p] = (uint8_t)fr;
@@ -134,6 +157,41 @@ __global__ void k_dest(UpdArgs a) {
   if ((threadIdx.x & 31) == 0) atomicMax(&a.st->max_disp, local_max);
 }
 
+// vfield_new = vfield_new + vreal (update_particle.f90:72): the real(8) sum
+// rounded to real(4), with vreal = decode + vfield(source) in real(8).  Fast
+// path: the exact sum acc + dec + vfield as float-float, certified to round to
+// the same float as the reference's two FP64 roundings followed by one FP32.
+__device__ __forceinline__ float accumulate_v(const UpdArgs& a, float acc, int64_t p, int d, int64_t S) {
+  int vcode = load_code(a.vp, 3 * p + d, a.g.izipv);
+  float2 dd = codec_decode_ff(a.cv, vcode);
+  float vfs = a.vfield[3 * S + d];
+  float s1, e1, s2, e2;
+  two_sum(acc, dd.x, s1, e1);
+  two_sum(s1, vfs, s2, e2);
+  float lo = __fadd_rn(__fadd_rn(e1, e2), dd.y);
+  float margin = 1.25f * (fabsf(dd.x) * 4.0e-15f + (fabsf(e1) + fabsf(e2) + fabsf(dd.y)) * 1.2e-7f +
+                          (fabsf(acc) + fabsf(dd.x) + fabsf(vfs)) * 2.3e-16f);
+  float r;
+  if (!a.exact_only && round_certified(s2, lo, margin, &r)) return r;
+  double v = __dadd_rn(codec_decode(a.cv, vcode), (double)vfs);
+  return __double2float_rn(__dadd_rn((double)acc, v));
+}
+
+// vfield_new/(rhoce+weight_v) (update_particle.f90:81-83): the denominator
+// cnt + (double)0.1f is exact in real(8); the quotient is rounded to real(8)
+// and then to real(4).  Fast path: float-float quotient, certified as above.
+__device__ __forceinline__ float vfield_quotient(float acc, uint32_t cnt, int exact_only) {
+  float dhi, dlo;
+  two_sum((float)cnt, 0.1f, dhi, dlo);  // (float)cnt exact below 2^24
+  float q1 = __fdiv_rn(acc, dhi);
+  float r1 = __fmaf_rn(-q1, dhi, acc);  // exact remainder of a correctly rounded quotient
+  float lo = __fdiv_rn(__fsub_rn(r1, __fmul_rn(q1, dlo)), dhi);
+  float margin = 1.25f * (fabsf(lo) * 3.6e-7f + fabsf(q1) * (fabsf(dlo / dhi) * fabsf(dlo / dhi) + 2.3e-16f));
+  float r;
+  if (!exact_only && cnt < (1u << 24) && round_certified(q1, lo, margin, &r)) return r;
+  return __double2float_rn(__ddiv_rn((double)acc, __dadd_rn((double)cnt, kWeightV)));
+}
+
 // U2: one thread per destination cell walks the sources in visit order.
 __global__ void k_rank(UpdArgs a) {
   const Geo& g = a.g;
@@ -145,8 +203,7 @@ __global__ void k_rank(UpdArgs a) {
     cell_coords(g, D, dgc[0], dgc[1], dgc[2]);
     int T[3], Dl[3];
     for (int d = 0; d < 3; d++) {
-      T[d] = dgc[d] / g.nt;
-      Dl[d] = dgc[d] - T[d] * g.nt + 1;
+      tile_local(g, dgc[d], T[d], Dl[d]);
     }
     // source z offsets sorted by (layer, k): layer = (k+ncb-1) mod nlayer
     int dz[2 * 16 + 1];
@@ -168,23 +225,25 @@ __global__ void k_rank(UpdArgs a) {
       }
       dz[pos] = o;
     }
+    // vfield_new=vfield*weight_v: the product of two floats is exact in real(8),
+    // so its real(4) rounding is the FP32 product
     float acc[3];
-    for (int d = 0; d < 3; d++) acc[d] = __double2float_rn(__dmul_rn((double)a.vfield[3 * D + d], kWeightV));
+    for (int d = 0; d < 3; d++) acc[d] = __fmul_rn(a.vfield[3 * D + d], 0.1f);
     uint32_t cnt = 0;
     for (int iz = 0; iz < nz; iz++) {
       int kl = Dl[2] + dz[iz];
       int sz = glob(g, T[2], kl);
       // frame offset (in tiles) at which this destination tile sees the source:
       // local coordinate kl vs the source's own tile-local coordinate
-      int fz = (kl - (sz - (sz / g.nt) * g.nt + 1)) / g.nt + 1;
+      int fz = frame_code(g, kl, sz);
       for (int jl = Dl[1] - R; jl <= Dl[1] + R; jl++) {
         if (jl < 1 - g.ncb || jl > g.nt + g.ncb) continue;
         int sy = glob(g, T[1], jl);
-        int fy = (jl - (sy - (sy / g.nt) * g.nt + 1)) / g.nt + 1;
+        int fy = frame_code(g, jl, sy);
         for (int il = Dl[0] - R; il <= Dl[0] + R; il++) {
           if (il < 1 - g.ncb || il > g.nt + g.ncb) continue;
           int sx = glob(g, T[0], il);
-          int fx = (il - (sx - (sx / g.nt) * g.nt + 1)) / g.nt + 1;
+          int fx = frame_code(g, il, sx);
           uint8_t fr = (uint8_t)(fx + 3 * fy + 9 * fz);
           int64_t S = cell_id(g, sx, sy, sz);
           int64_t p0 = a.cstart[S], p1 = a.cstart[S + 1];
@@ -201,17 +260,13 @@ __global__ void k_rank(UpdArgs a) {
             else
               a.xtra[xi].z = (int)cnt;
             cnt++;
-            for (int d = 0; d < 3; d++) {
-              double v = vreal_of(a, p, d, S);
-              acc[d] = __double2float_rn(__dadd_rn((double)acc[d], v));
-            }
+            for (int d = 0; d < 3; d++) acc[d] = accumulate_v(a, acc[d], p, d, S);
           }
         }
       }
     }
     a.cnt_new[D] = (int32_t)cnt;
-    for (int d = 0; d < 3; d++)
-      a.vfield_new[3 * D + d] = __double2float_rn(__ddiv_rn((double)acc[d], __dadd_rn((double)cnt, kWeightV)));
+    for (int d = 0; d < 3; d++) a.vfield_new[3 * D + d] = vfield_quotient(acc[d], cnt, a.exact_only);
   }
 }
 
@@ -224,15 +279,37 @@ __device__ __forceinline__ void write_particle(const UpdArgs& a, int64_t p, int3
   int64_t idx = a.cstart_new[D] + r;
   int64_t cell = a.pcell[p];
   // nint(dt_mid*vreal/(x_resolution*ncell)): the divisor is a power of two
-  double inv = g.izipx == 1 ? 64.0 : 16384.0;
+  float scale = g.izipx == 1 ? 64.0f : 16384.0f;
   for (int d = 0; d < 3; d++) {
-    double v = vreal_of(a, p, d, cell);
-    double P = __dmul_rn((double)a.dt_mid, v);
-    long long dx = llround(__dmul_rn(P, inv));
+    int vcode = load_code(a.vp, 3 * p + d, g.izipv);
+    float vfd = a.vfield[3 * cell + d];
+    float vbar = a.vfield_new[3 * (int64_t)D + d];
+    float2 dd = codec_decode_ff(a.cv, vcode);
+    // drift in code units: FP32 estimate of dt_mid*(dec+vfield)*scale with its bound
+    float vfa = __fadd_rn(dd.x, vfd);
+    float Pf = __fmul_rn(a.dt_mid, vfa);
+    float EP = scale * 1.25f * (fabsf(a.dt_mid) * (fabsf(dd.x) + fabsf(vfa)) * 1.2e-7f + fabsf(Pf) * 6.0e-8f);
+    long long dx;
+    if (a.exact_only || !nint_certified(__fmul_rn(Pf, scale), EP, &dx)) {
+      double v = __dadd_rn(codec_decode(a.cv, vcode), (double)vfd);
+      dx = llround(__dmul_rn(__dmul_rn((double)a.dt_mid, v), (double)scale));
+    }
     long long x = load_code(a.xp, 3 * p + d, g.izipx);
     store_code(a.xp_new, 3 * idx + d, g.izipx, x + dx);
-    double vrel = __dsub_rn(v, (double)a.vfield_new[3 * (int64_t)D + d]);
-    store_code(a.vp_new, 3 * idx + d, g.izipv, v_encode(vrel, a.vc, a.nvbin));
+    // vp = code of vreal - vfield_new (update_particle.f90:116-117)
+    float w, ew;
+    two_sum(vfd, -vbar, w, ew);
+    float Vf = __fadd_rn(dd.x, w);
+    float E = 1.25f * ((fabsf(dd.x) + fabsf(Vf)) * 6.0e-8f + fabsf(ew) +
+                       (fabsf(dd.x) + fabsf(vfd) + fabsf(vbar)) * 2.3e-16f);
+    long long ab = f2d_bits(Vf) & 0x7fffffffffffffffLL, n = 0, code;
+    if (!a.exact_only && certify_abs(ab, E, a.cv, &n)) {
+      code = Vf < 0.f ? -n : n;
+    } else {
+      double v = __dadd_rn(codec_decode(a.cv, vcode), (double)vfd);
+      code = codec_encode(a.cv, __dsub_rn(v, (double)vbar));
+    }
+    store_code(a.vp_new, 3 * idx + d, g.izipv, code);
   }
   a.pid_new[idx] = a.pid[p];
   a.pcell_new[idx] = D;
@@ -253,33 +330,44 @@ __global__ void k_scatter_xtra(UpdArgs a) {
     write_particle(a, a.xtra[e].x, a.xtra[e].y, (uint32_t)a.xtra[e].z);
 }
 
+__device__ __forceinline__ void ff_add(float& hi, float& lo, float x, float xlo) {
+  float s, e;
+  two_sum(hi, x, s, e);
+  e = __fadd_rn(e, __fadd_rn(lo, xlo));
+  two_sum(s, e, hi, lo);
+}
+
 // sigma_v sums of the new state (update_particle.f90:172-196): per-block FP64
 // partials in a fixed partition, summed in block order on the host.
 __global__ void k_sigma(const void* __restrict__ vp, const int32_t* __restrict__ pcell, const float* __restrict__ vfield,
-                        int64_t np, int64_t ncells, const double* __restrict__ dec, int nvbin, int izipv,
+                        int64_t np, int64_t ncells, const float2* __restrict__ dech, int nvbin, int izipv,
                         double* __restrict__ part) {
   __shared__ double s[3][32];
-  double sc = 0, sr = 0, ss = 0;
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t t0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  // per-thread float-float accumulators (exact products by FMA), one FP64
+  // combine per thread: FP64-accurate sums without FP64 per element
+  float ch = 0.f, cl = 0.f, rh = 0.f, rl = 0.f, sh = 0.f, sl = 0.f;
   for (int64_t c = t0; c < ncells; c += stride) {
     float a0 = vfield[3 * c], a1 = vfield[3 * c + 1], a2 = vfield[3 * c + 2];
     float q = __fadd_rn(__fadd_rn(__fmul_rn(a0, a0), __fmul_rn(a1, a1)), __fmul_rn(a2, a2));
-    sc += (double)q;
+    ff_add(ch, cl, q, 0.f);
   }
   for (int64_t p = t0; p < np; p += stride) {
     int64_t c = pcell[p];
     if (c < 0 || c >= ncells) continue;
-    double r2 = 0, s2 = 0;
     for (int d = 0; d < 3; d++) {
-      double v = dec[load_code(vp, 3 * p + d, izipv) + nvbin / 2];
-      r2 += v * v;
-      double w = v + (double)vfield[3 * c + d];
-      s2 += w * w;
+      float2 v = __ldg(dech + load_code(vp, 3 * p + d, izipv) + nvbin / 2);
+      float p2 = __fmul_rn(v.x, v.x);
+      ff_add(rh, rl, p2, __fmaf_rn(v.x, v.x, -p2) + 2.f * v.x * v.y);
+      float w, ew;
+      two_sum(v.x, vfield[3 * c + d], w, ew);
+      ew += v.y;
+      float q2 = __fmul_rn(w, w);
+      ff_add(sh, sl, q2, __fmaf_rn(w, w, -q2) + 2.f * w * ew);
     }
-    sr += r2;
-    ss += s2;
   }
+  double sc = (double)ch + (double)cl, sr = (double)rh + (double)rl, ss = (double)sh + (double)sl;
   for (int o = 16; o > 0; o >>= 1) {
     sc += __shfl_xor_sync(0xffffffffu, sc, o);
     sr += __shfl_xor_sync(0xffffffffu, sr, o);
@@ -311,7 +399,8 @@ int cube_update_x_impl(cube_ctx* c, float dt_old, float dt, float vz_max, cube_s
   volatile float q2 = q / (float)c->p.ncell;
   int nlayer = 2 * (int)std::ceil((double)q2) + 1;
   if (nlayer < 1) nlayer = 1;
-  int r = cube_ensure_decode(c, c->dec_old, c->sigma_vi, c->dec_old_sigma);
+  CodecView cv;
+  int r = cube_codec_pair(c, c->sigma_vi, c->sigma_vi, &cv, nullptr);
   if (r) return r;
   CUBE_CUDA(c, cudaMemsetAsync(c->dstats, 0, sizeof(DevStats), c->stream));
   UpdArgs a{};
@@ -326,12 +415,8 @@ int cube_update_x_impl(cube_ctx* c, float dt_old, float dt, float vz_max, cube_s
   a.pcell = c->pcell[k];
   a.vfield = c->vfield[k];
   a.cstart = c->cstart[k];
-  a.dec = c->dec_old;
-  a.nvbin = c->nvbin;
-  {
-    float s = std::sqrt(CUBE_PI_F / 2.0f);
-    a.vc = (double)s / ((double)c->sigma_vi * 2.5);
-  }
+  a.cv = cv;
+  a.exact_only = c->opt_exact_kicks;
   a.dest = c->dest;
   a.dframe = c->dframe;
   a.rank = c->rank;
@@ -375,7 +460,7 @@ int cube_update_x_impl(cube_ctx* c, float dt_old, float dt, float vz_max, cube_s
   // sigma statistics of the new state (decoded with sigma_vi)
   int nb = c->red_blocks;
   cube_phase_begin(c, PH_UPD_SIGMA);
-  k_sigma<<<nb, 256, 0, c->stream>>>(c->vp[kn], c->pcell[kn], c->vfield[kn], np_new, c->ncells, c->dec_old,
+  k_sigma<<<nb, 256, 0, c->stream>>>(c->vp[kn], c->pcell[kn], c->vfield[kn], np_new, c->ncells, cv.dech,
                                       c->nvbin, c->p.izipv, c->red_tmp);
   cube_phase_end(c, PH_UPD_SIGMA);
   CUBE_CUDA(c, cudaGetLastError());

@@ -30,7 +30,9 @@ EXPORTS = ["cube_create", "cube_destroy", "cube_last_error", "cube_upload_state"
            "cube_buffer_v", "cube_pp_force", "cube_particle_mesh", "cube_pm_fine_density", "cube_pm_coarse_density",
            "cube_pm_fine_forces", "cube_pm_fine_kick",
            "cube_pm_coarse_forces", "cube_pm_coarse_kick", "cube_get_field", "cube_set_field", "cube_nplocal",
-           "cube_synchronize", "cube_timing", "cube_timing_read", "cube_phase_name", "cube_stream"]
+           "cube_synchronize", "cube_timing", "cube_timing_read", "cube_phase_name", "cube_stream",
+           "cube_codec_check", "cube_set_option"]
+OPT_EXACT_KICKS = 1
 NPHASE = 15
 
 
@@ -104,6 +106,8 @@ def load_library(path=None):
     L.cube_phase_name.restype = ctypes.c_char_p
     L.cube_stream.argtypes = [P]
     L.cube_stream.restype = ctypes.c_void_p
+    L.cube_codec_check.argtypes = [P, F, P, I64, P, P]
+    L.cube_set_option.argtypes = [P, ctypes.c_int, I64]
     _lib = L
     return L
 
@@ -254,6 +258,17 @@ class CubeGPU:
     def stream(self):
         """The cudaStream_t (as an int) every call of this context runs on."""
         return int(self.L.cube_stream(self.h) or 0)
+
+    def set_option(self, option, value):
+        self._check(self.L.cube_set_option(self.h, int(option), int(value)))
+
+    def codec_check(self, sigma, v):
+        """(direct FP64 codes, table codes) of the doubles v under sigma."""
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        a = np.empty(v.size, np.int32)
+        b = np.empty(v.size, np.int32)
+        self._check(self.L.cube_codec_check(self.h, float(sigma), _ptr(v), v.size, _ptr(a), _ptr(b)))
+        return a, b
 
     def timing(self, enable):
         self._check(self.L.cube_timing(self.h, int(bool(enable))))

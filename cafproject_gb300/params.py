@@ -132,9 +132,15 @@ def cdm512():
     return CubeParams(nc=256, nnt=2, pp_on=True, rsoft=0.1, box=600.0)
 
 
+def cdm256():
+    """256^3 particles, 300 Mpc/h, coarse 128^3, fine 512^3 over 2^3 tiles, PP: the
+    cdm512 workload at 1/8 the volume, for profiling captures of a few GB."""
+    return CubeParams(nc=128, nnt=2, pp_on=True, rsoft=0.1, box=300.0)
+
+
 def small(nc=24, nnt=2, pp_on=True, izipx=1, izipv=2):
     """A small multi-tile case for parity tests (nt = nc/nnt >= 12)."""
     return CubeParams(nc=nc, nnt=nnt, pp_on=pp_on, izipx=izipx, izipv=izipv, box=100.0 * nc / 32)
 
 
-WORKLOADS = {"cdm64": cdm64, "cdm512": cdm512}
+WORKLOADS = {"cdm64": cdm64, "cdm256": cdm256, "cdm512": cdm512}

@@ -176,6 +176,18 @@ const char* cube_phase_name(int phase);
 /* The CUDA stream (cudaStream_t) all of the context's work is issued on. */
 void* cube_stream(cube_ctx* ctx);
 
+/* Run-time options.  CUBE_OPT_EXACT_KICKS=1 makes every kernel evaluate the
+   reference's FP64 expressions directly instead of the certified FP32 /
+   float-float fast paths (results are identical by construction; used to test
+   that claim and to time it). */
+enum cube_option { CUBE_OPT_EXACT_KICKS = 1 };
+int cube_set_option(cube_ctx* ctx, int option, int64_t value);
+
+/* Velocity-code self check: encodes n host doubles with sigma both by the
+   direct FP64 formula of update_particle.f90:117 and by the table path the
+   kernels use; writes both codes (host arrays of n int32). */
+int cube_codec_check(cube_ctx* ctx, float sigma, const double* v, int64_t n, int32_t* direct, int32_t* table);
+
 #ifdef __cplusplus
 }
 #endif

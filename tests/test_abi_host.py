@@ -90,3 +90,29 @@ def test_constrain_from_device_maxima():
     assert ts.dt_fine == np.float32(np.sqrt(np.float32(1) / (np.float32(2) * np.float32(0.5) * GG)))
     assert ts.dt_vmax == np.float32(np.float32(18) / np.float32(3))
     assert ts.vz_max == np.float32(3.0)
+
+
+def test_fast_division_is_exact():
+    # the magic-number division used by the kernels (Granlund & Montgomery
+    # round-up multiplier), emulated exactly in Python
+    rng = np.random.default_rng(0)
+
+    def magic(d):
+        l = 0
+        while (1 << l) < d:
+            l += 1
+        return ((((1 << l) - d) << 32) // d + 1) & 0xFFFFFFFF, l
+
+    def fdiv(n, d, m, l):
+        if d <= 1:
+            return n
+        t = (n * m) >> 32
+        return (t + ((n - t) >> 1)) >> (l - 1)
+
+    for d in list(range(1, 300)) + [1 << k for k in range(1, 31)] + list(rng.integers(2, 1 << 31, 200)):
+        d = int(d)
+        m, l = magic(d)
+        ns = [0, 1, d - 1, d, d + 1, 2 * d - 1, (1 << 32) - 1, (1 << 31) - 1] + list(rng.integers(0, 1 << 32, 300))
+        for n in ns:
+            n = int(n)
+            assert fdiv(n, d, m, l) == n // d, (n, d)
