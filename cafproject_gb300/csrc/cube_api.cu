@@ -50,10 +50,12 @@ static void release(cube_ctx* c) {
                   c->vfield[0], c->vfield[1], c->cstart[0], c->cstart[1], c->dest, c->dframe, c->rank, c->xtra,
                   c->scan_tmp, c->red_tmp, c->tan_tab, c->codec[0].dec, c->codec[1].dec, c->codec[0].bnd, c->codec[1].bnd, c->codec[0].dech, c->codec[1].dech, c->rho_f, c->force_f[0],
                   c->force_f[1], c->force_f[2], c->kern_f, c->kern_f_raw, c->rho_c, c->force_c[0],
-                  c->force_c[1], c->force_c[2], c->kern_c, c->fpp, c->dstats, c->cufft_work};
+                  c->force_c[1], c->force_c[2], c->kern_c, c->fpp, c->pp_ovf_brick, c->pp_ovf_cell, c->pp_novf, c->dstats,
+                  c->cufft_work};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (c->hstats) cudaFreeHost(c->hstats);
+  if (c->pp_novf_host) cudaFreeHost(c->pp_novf_host);
   if (c->plan_f_r2c) cufftDestroy(c->plan_f_r2c);
   if (c->plan_f_c2r) cufftDestroy(c->plan_f_c2r);
   if (c->plan_c_r2c) cufftDestroy(c->plan_c_r2c);
@@ -156,6 +158,15 @@ extern "C" int cube_create(const cube_params* p, const float* fine_table, const 
   ALLOC(c->rho_c, 4 * cpad);
   for (int d = 0; d < 3; d++) ALLOC(c->force_c[d], 4 * cpad);
   ALLOC(c->kern_c, 4 * 3 * nch * p->nc * (int64_t)p->nc);
+  {
+    int nb = (p->nc + 3) / 4;
+    c->pp_brick_cap = nb * nb * nb;
+    ALLOC(c->pp_ovf_brick, 4 * (size_t)c->pp_brick_cap);
+    ALLOC(c->pp_ovf_cell, 4 * (size_t)c->ncells);
+    ALLOC(c->pp_novf, 8);
+    CUBE_CUDA(c, cudaMallocHost((void**)&c->pp_novf_host, 8));
+    c->pp_novf_host[0] = c->pp_novf_host[1] = 0;
+  }
   ALLOC(c->dstats, sizeof(DevStats));
   CUBE_CUDA(c, cudaMallocHost((void**)&c->hstats, sizeof(DevStats)));
   int r = make_plans(c);
@@ -278,6 +289,10 @@ extern "C" int cube_set_option(cube_ctx* c, int option, int64_t value) {
   switch (option) {
     case CUBE_OPT_EXACT_KICKS:
       c->opt_exact_kicks = value ? 1 : 0;
+      return CUBE_OK;
+    case CUBE_OPT_PP_LEVEL:
+      if (value < 0 || value > 2) return cube_fail(c, CUBE_ERR_ARG, "PP level must be 0, 1 or 2");
+      c->opt_pp_level = (int)value;
       return CUBE_OK;
     default:
       return cube_fail(c, CUBE_ERR_ARG, "unknown option");

@@ -86,6 +86,7 @@ struct cube_ctx {
   float vmax_prev[3] = {0.f, 0.f, 0.f};  // last coarse-kick vmax (0: unknown)
   unsigned long long kick_exact_lanes = 0;
   int opt_exact_kicks = 0;
+  int opt_pp_level = 0;  // first PP level (0 bricks, 1 single cells, 2 global memory)
   // fine PM
   cufftHandle plan_f_r2c = 0, plan_f_c2r = 0;
   float* rho_f = nullptr;       // padded real / complex in place
@@ -99,6 +100,11 @@ struct cube_ctx {
   float* kern_c = nullptr;      // scaled by 1/nc^3 (exact: power of two)
   // PP
   float* fpp = nullptr;         // optional per-particle PP force (3*np), debug only
+  int* pp_ovf_brick = nullptr;      // bricks too dense to stage (ceil(nc/4)^3 entries)
+  int* pp_ovf_cell = nullptr;       // cells too dense to stage (nc^3 entries)
+  int* pp_novf = nullptr;           // [0] listed bricks, [1] listed cells
+  int* pp_novf_host = nullptr;      // pinned copy of the last call's counts
+  int pp_brick_cap = 0;             // ceil(nc/4)^3
   // per-phase timers (null when disabled)
   struct CubeTimers* timers = nullptr;
   // stats

@@ -3,34 +3,61 @@
 // The reference threads a linked list through the fine cells of each tile
 // (hoc/ll, ext_pp_force.f90:53-75) and, for every particle of a physical fine
 // cell, sums m*r/|r|^3*pcut(|r|) over the particles of the 3^3 neighbouring
-// fine cells, skipping pairs with |r| <= rsoft (:94-110), in FP64.  Here the
-// particles are already sorted by coarse cell, so a fine neighbourhood is at
-// most 2x2x2 coarse cells: a particle in fine sub-cell 0 (3) of its coarse
-// cell also reads the coarse cell below (above) in that dimension.  The pair
-// arithmetic is FP32 (positions are exact in FP32: 4*frac has <= 17 bits);
-// the kick adds F*a_mid*dt/(6 pi) in FP64 (:116) as one product with the
-// precomputed factor -- the FP32 pair sum already sets the tolerance of this
-// kick, so the reference's two FP64 divisions buy nothing here -- and the
-// velocity re-encode is the exact code of update_particle.f90:117.
+// fine cells, skipping pairs with |r| <= rsoft (:94-110), in FP64.
+//
+// Here a block of coarse cells is staged in shared memory: the particles of
+// the block and of the one-fine-cell layer around it, read from the block's
+// cells and its ring of coarse cells (storage is ordered by coarse cell), as
+// FP32 positions relative to the block (exact: 4*frac has at most 17 bits),
+// then counting-sorted by fine cell, so each particle of the block walks
+// exactly its 27 neighbouring fine cells, as the linked list does.  Pair
+// forces are FP32, each component summed in 2^-32 fixed point (int64) so the
+// sum does not depend on the visit order (bitwise reproducible whichever
+// kernel handles a particle).
+//
+// Three levels keep dense regions correct without a host round trip:
+//   0. one CTA per brick of 4^3 coarse cells;
+//   1. bricks whose staged set exceeds PP_CAP are listed and redone one coarse
+//      cell at a time (persistent CTAs walking the list);
+//   2. cells still too dense are listed and done from global memory, one CTA
+//      per cell.
+// The kick adds F*a_mid*dt/(6 pi) in FP64 as one product with the precomputed
+// factor -- the FP32 pair sum already sets this kick's tolerance against the
+// reference's FP64 sum -- and the velocity code is the exact code of
+// update_particle.f90:117 (certified FP32 fast path, FP64 when ambiguous).
 #include <cmath>
 
 #include "cube_internal.cuh"
 
 namespace {
 
+constexpr int PB = 4;                          // coarse cells per brick edge
+constexpr int PS_MAX = PB + 2;                 // staged coarse cells per edge
+constexpr int PNS_MAX = PS_MAX * PS_MAX * PS_MAX;
+constexpr int PNCORE_MAX = PB * PB * PB;
+constexpr int PNF_MAX = (4 * PB + 2) * (4 * PB + 2) * (4 * PB + 2);
+constexpr int PP_CAP = 1536;                   // staged particles per block
+constexpr int PP_THREADS = 256;
+constexpr size_t PP_SMEM = (sizeof(float4) + sizeof(unsigned) + sizeof(unsigned short)) * PP_CAP +
+                           sizeof(int) * (PNF_MAX + 1);
+
 struct PPArgs {
   Geo g;
   int64_t np;
   const void* xp;
   void* vp;
-  const int32_t* pcell;
+  const int32_t* rhoc;
   const int64_t* cstart;
   CodecView cv;
   float mass, rsoft, inv_cut;
   double kick;   // a_mid*dt/6/pi
   float kick_f;  // the same rounded to float (fast path)
   int exact_only;
-  float* fpp;  // optional per-particle force output
+  float* fpp;    // optional per-particle force output
+  int nb;        // bricks per dimension
+  int* ovf_brick;  // level-1 list: bricks too dense to stage
+  int* ovf_cell;   // level-2 list: cells too dense to stage
+  int* novf;       // [0] listed bricks, [1] listed cells
   DevStats* st;
 };
 
@@ -39,73 +66,64 @@ __device__ __forceinline__ float fine_off(int code, int izipx) {
   return __fmul_rn(pos_off_f(code, izipx), izipx == 1 ? 4.0f / 256.0f : 4.0f / 65536.0f);
 }
 
-__global__ void k_pp(PPArgs a) {
+// v*2^32 as a two's-complement int64 from 32-bit conversions only (|v| < 2^23)
+__device__ __forceinline__ long long to_fix(float v) {
+  float a = fabsf(v);
+  float ws = __fmul_rn(a, 256.0f), fh = floorf(ws);
+  long long q = ((long long)(unsigned int)fh << 24) + (unsigned int)__fmul_rn(__fsub_rn(ws, fh), 16777216.0f);
+  return v < 0.f ? -q : q;
+}
+__device__ __forceinline__ float from_fix(long long q) {
+  bool neg = q < 0;
+  unsigned long long u = neg ? (unsigned long long)(-q) : (unsigned long long)q;
+  float hi = (float)(unsigned int)(u >> 32), lo = (float)(unsigned int)(u & 0xffffffffull);
+  float r = __fmaf_rn(lo, 2.3283064365386963e-10f, hi);
+  return neg ? -r : r;
+}
+
+// one pair: accumulate the force of a particle at offset r (FP32)
+__device__ __forceinline__ void pair_force(const PPArgs& a, float rx, float ry, float rz, long long* acc) {
+  // explicit roundings: every kernel evaluates the same bits for a pair
+  float r2 = __fmaf_rn(rx, rx, __fmaf_rn(ry, ry, __fmul_rn(rz, rz)));
+  float rm = __fsqrt_rn(r2);
+  if (!(rm > a.rsoft)) return;  // merge(force,0,rmag>rsoft); self pairs have rm=0
+  float rc = __fmul_rn(rm, a.inv_cut);
+  float rc3 = __fmul_rn(__fmul_rn(rc, rc), rc);
+  // pcut = 1 - 1.75 rc^3 + 0.75 rc^5  (ext_pp_force.f90:107)
+  float pcut = __fmaf_rn(__fmul_rn(0.75f, rc3), __fmul_rn(rc, rc), __fmaf_rn(-1.75f, rc3, 1.0f));
+  float s = __fdiv_rn(__fmul_rn(a.mass, pcut), __fmul_rn(r2, rm));
+  acc[0] += to_fix(__fmul_rn(s, rx));
+  acc[1] += to_fix(__fmul_rn(s, ry));
+  acc[2] += to_fix(__fmul_rn(s, rz));
+}
+
+// kick + exact velocity code of one particle; returns |F|^2
+__device__ __forceinline__ float pp_kick(const PPArgs& a, int64_t p, const long long* acc) {
   const Geo& g = a.g;
-  unsigned long long npairs = 0, nwork = 0;
-  float f2max = 0.f;
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.np; p += (int64_t)gridDim.x * blockDim.x) {
-    int gc[3];
-    cell_coords(g, a.pcell[p], gc[0], gc[1], gc[2]);
-    float x1[3];
-    int fi[3], lo[3], hi[3];
-    for (int d = 0; d < 3; d++) {
-      x1[d] = fine_off(load_code(a.xp, 3 * p + d, g.izipx), g.izipx);
-      fi[d] = (int)floorf(x1[d]);
-      lo[d] = fi[d] == 0 ? -1 : 0;
-      hi[d] = fi[d] == g.ncell - 1 ? 1 : 0;
+  float F[3];
+  for (int d = 0; d < 3; d++) F[d] = from_fix(acc[d]);
+  for (int d = 0; d < 3; d++) {
+    int code = load_code(a.vp, 3 * p + d, g.izipv);
+    // vreal=vreal+f_tot*a_mid*dt/6/pi (ext_pp_force.f90:116), then the code
+    float dh = codec_decode_ff(a.cv, code).x;
+    float kf = __fmul_rn(F[d], a.kick_f);
+    float vf = __fadd_rn(dh, kf);
+    float E = 1.25f * (fabsf(kf) * 1.3e-7f + (2.f * fabsf(dh) + fabsf(vf)) * 6.0e-8f);
+    long long n = 0, out;
+    if (!a.exact_only && certify_abs(f2d_bits(vf) & 0x7fffffffffffffffLL, E, a.cv, &n)) {
+      out = vf < 0.f ? -n : n;
+    } else {
+      double v = __dadd_rn(codec_decode(a.cv, code), __dmul_rn((double)F[d], a.kick));
+      out = codec_encode(a.cv, v);
     }
-    float F[3] = {0.f, 0.f, 0.f};
-    for (int dz = lo[2]; dz <= hi[2]; dz++)
-      for (int dy = lo[1]; dy <= hi[1]; dy++)
-        for (int dx = lo[0]; dx <= hi[0]; dx++) {
-          int sx = wrap1(gc[0] + dx, g.nc), sy = wrap1(gc[1] + dy, g.nc), sz = wrap1(gc[2] + dz, g.nc);
-          int64_t S = cell_id(g, sx, sy, sz);
-          int64_t q0 = a.cstart[S], q1 = a.cstart[S + 1];
-          float sh[3] = {(float)(4 * dx), (float)(4 * dy), (float)(4 * dz)};
-          for (int64_t q = q0; q < q1; q++) {
-            float r[3];
-            bool near = true;
-            for (int d = 0; d < 3; d++) {
-              float x2 = sh[d] + fine_off(load_code(a.xp, 3 * q + d, g.izipx), g.izipx);
-              int f2 = (int)floorf(x2);
-              near = near && abs(f2 - fi[d]) <= 1;
-              r[d] = x2 - x1[d];
-            }
-            if (!near) continue;
-            npairs++;
-            float r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
-            float rm = sqrtf(r2);
-            if (!(rm > a.rsoft)) continue;  // merge(force,0,rmag>rsoft); self pairs have rm=0
-            float rc = rm * a.inv_cut;
-            float rc2 = rc * rc;
-            float pcut = 1.0f - 1.75f * rc2 * rc + 0.75f * rc2 * rc2 * rc;
-            float s = a.mass * pcut / (r2 * rm);
-            F[0] += s * r[0];
-            F[1] += s * r[1];
-            F[2] += s * r[2];
-          }
-        }
-    nwork++;
-    for (int d = 0; d < 3; d++) {
-      int code = load_code(a.vp, 3 * p + d, g.izipv);
-      // vreal=vreal+f_tot*a_mid*dt/6/pi (ext_pp_force.f90:116), then the code:
-      // FP32 estimate certified against the FP64 expression (see certify_abs)
-      float dh = codec_decode_ff(a.cv, code).x;
-      float kf = __fmul_rn(F[d], a.kick_f);
-      float vf = __fadd_rn(dh, kf);
-      float E = 1.25f * (fabsf(kf) * 1.3e-7f + (2.f * fabsf(dh) + fabsf(vf)) * 6.0e-8f);
-      long long n = 0, out;
-      if (!a.exact_only && certify_abs(f2d_bits(vf) & 0x7fffffffffffffffLL, E, a.cv, &n)) {
-        out = vf < 0.f ? -n : n;
-      } else {
-        double v = __dadd_rn(codec_decode(a.cv, code), __dmul_rn((double)F[d], a.kick));
-        out = codec_encode(a.cv, v);
-      }
-      store_code(a.vp, 3 * p + d, g.izipv, out);
-      if (a.fpp) a.fpp[3 * p + d] = F[d];
-    }
-    f2max = fmaxf(f2max, F[0] * F[0] + F[1] * F[1] + F[2] * F[2]);
+    store_code(a.vp, 3 * p + d, g.izipv, out);
+    if (a.fpp) a.fpp[3 * p + d] = F[d];
   }
+  return F[0] * F[0] + F[1] * F[1] + F[2] * F[2];
+}
+
+__device__ __forceinline__ void pp_reduce(const PPArgs& a, unsigned long long npairs, unsigned long long nwork,
+                                          float f2max) {
   for (int o = 16; o > 0; o >>= 1) {
     npairs += __shfl_xor_sync(0xffffffffu, npairs, o);
     nwork += __shfl_xor_sync(0xffffffffu, nwork, o);
@@ -116,6 +134,228 @@ __global__ void k_pp(PPArgs a) {
     atomicAdd(&a.st->itest1, nwork);
     atomic_max_pos(&a.st->f2_pp_bits, f2max);
   }
+}
+
+// In-place exclusive scan of n ints by a block of 256 threads; returns the
+// total to every thread.  Each thread scans a contiguous run, the run sums are
+// scanned across warps.
+__device__ int block_exclusive_scan(int* v, int n) {
+  __shared__ int wsum[8];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const int per = (n + 255) / 256;
+  const int b0 = min(n, t * per), b1 = min(n, b0 + per);
+  int s = 0;
+  for (int i = b0; i < b1; i++) s += v[i];
+  int inc = s;
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += y;
+  }
+  if (lane == 31) wsum[w] = inc;
+  __syncthreads();
+  int wbase = 0, total = 0;
+  for (int k = 0; k < 8; k++) {
+    int x = wsum[k];
+    if (k < w) wbase += x;
+    total += x;
+  }
+  int run = wbase + inc - s;
+  for (int i = b0; i < b1; i++) {
+    int x = v[i];
+    v[i] = run;
+    run += x;
+  }
+  __syncthreads();
+  return total;
+}
+
+// largest k in [0,n) with pref[k] <= j (pref non-decreasing, pref[0]=0)
+__device__ __forceinline__ int upper_index(const int* pref, int n, int j) {
+  int lo = 0, hi = n;
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (pref[mid] <= j) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+struct PPSmem {
+  int pref[PNS_MAX + 1];         // ring-and-block particles before each staged cell
+  long long sstart[PNS_MAX];     // first particle of each staged cell
+  int nst;                       // staged particles
+};
+
+struct PPAcc {
+  unsigned long long npairs = 0, nwork = 0;
+  float f2max = 0.f;
+};
+
+// Pair forces + kicks for the B[0]xB[1]xB[2] coarse cells starting at C0.
+// The particles of the block and of the fine-cell layer around it are staged
+// (compacted), binned by fine cell (counting sort of slot numbers), and every
+// particle of the block then walks its 27 neighbouring fine-cell bins.
+// Returns false (nothing kicked) when more than PP_CAP particles would be
+// staged.  Block-uniform control flow; ends with a barrier.
+__device__ bool pp_block(const PPArgs& a, const int C0[3], const int B[3], PPSmem& sm, float4* dyn, PPAcc& acc) {
+  const Geo& g = a.g;
+  const int nc = g.nc;
+  const int S0 = B[0] + 2, S1 = B[1] + 2, S2 = B[2] + 2, NS = S0 * S1 * S2;
+  const int F0 = 4 * B[0] + 2, F1 = 4 * B[1] + 2, F2 = 4 * B[2] + 2, NF = F0 * F1 * F2;
+  float4* pts = dyn;                                              // x, y, z, particle index
+  unsigned* kinfo = reinterpret_cast<unsigned*>(pts + PP_CAP);    // bin | rank in bin << 13
+  unsigned short* order = reinterpret_cast<unsigned short*>(kinfo + PP_CAP);  // slots by bin
+  int* bins = reinterpret_cast<int*>(order + PP_CAP);             // NF+1 bin offsets
+  for (int t = threadIdx.x; t < NS; t += blockDim.x) {
+    int sx = t % S0, sy = (t / S0) % S1, sz = t / (S0 * S1);
+    int64_t c = cell_id(g, wrap1(C0[0] + sx - 1, nc), wrap1(C0[1] + sy - 1, nc), wrap1(C0[2] + sz - 1, nc));
+    sm.pref[t] = a.rhoc[c];
+    sm.sstart[t] = a.cstart[c];
+  }
+  for (int t = threadIdx.x; t < NF; t += blockDim.x) bins[t] = 0;
+  if (threadIdx.x == 0) sm.nst = 0;
+  __syncthreads();
+  const int total = block_exclusive_scan(sm.pref, NS);
+  // stage the particles whose fine cell lies in the block or its fine ring
+  for (int j = threadIdx.x; j < total; j += blockDim.x) {
+    int s = upper_index(sm.pref, NS, j);
+    int64_t p = sm.sstart[s] + (j - sm.pref[s]);
+    int sl[3] = {s % S0 - 1, (s / S0) % S1 - 1, s / (S0 * S1) - 1};
+    float x[3];
+    int fi[3];
+    bool in = true;
+    for (int d = 0; d < 3; d++) {
+      x[d] = __fadd_rn((float)(4 * sl[d]), fine_off(load_code(a.xp, 3 * p + d, g.izipx), g.izipx));
+      fi[d] = (int)floorf(x[d]) + 1;  // 0 .. 4B+1 inside the staged region
+      in = in && fi[d] >= 0 && fi[d] <= 4 * B[d] + 1;
+    }
+    if (!in) continue;
+    int slot = atomicAdd(&sm.nst, 1);
+    if (slot >= PP_CAP) continue;
+    int f = fi[0] + F0 * (fi[1] + F1 * fi[2]);
+    int r = atomicAdd(&bins[f], 1);
+    pts[slot] = make_float4(x[0], x[1], x[2], __int_as_float((int)p));
+    kinfo[slot] = (unsigned)f | ((unsigned)r << 13);
+  }
+  __syncthreads();
+  const int nst = sm.nst;
+  if (nst > PP_CAP) return false;
+  block_exclusive_scan(bins, NF);
+  if (threadIdx.x == 0) bins[NF] = nst;
+  for (int t = threadIdx.x; t < nst; t += blockDim.x) {
+    unsigned k = kinfo[t];
+    order[bins[k & 8191u] + (int)(k >> 13)] = (unsigned short)t;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < nst; t += blockDim.x) {
+    float4 q = pts[t];
+    int fx = (int)floorf(q.x) + 1, fy = (int)floorf(q.y) + 1, fz = (int)floorf(q.z) + 1;
+    if (fx < 1 || fy < 1 || fz < 1 || fx > 4 * B[0] || fy > 4 * B[1] || fz > 4 * B[2]) continue;  // ring
+    int f = (int)(kinfo[t] & 8191u);
+    long long F[3] = {0, 0, 0};
+    for (int dz = -1; dz <= 1; dz++)
+      for (int dy = -1; dy <= 1; dy++)
+        for (int dx = -1; dx <= 1; dx++) {
+          int f2 = f + dx + F0 * (dy + F1 * dz);
+          int k1 = bins[f2 + 1];
+          for (int k = bins[f2]; k < k1; k++) {
+            float4 o = pts[order[k]];
+            acc.npairs++;
+            pair_force(a, o.x - q.x, o.y - q.y, o.z - q.z, F);
+          }
+        }
+    acc.nwork++;
+    acc.f2max = fmaxf(acc.f2max, pp_kick(a, (int64_t)__float_as_int(q.w), F));
+  }
+  __syncthreads();
+  return true;
+}
+
+// level 0: one CTA per 4^3 brick
+__global__ void __launch_bounds__(PP_THREADS) k_pp_bricks(PPArgs a) {
+  __shared__ PPSmem sm;
+  extern __shared__ float4 pts[];
+  const int nc = a.g.nc;
+  int b = blockIdx.x;
+  int C0[3] = {(b % a.nb) * PB, ((b / a.nb) % a.nb) * PB, (b / (a.nb * a.nb)) * PB};
+  int B[3] = {min(PB, nc - C0[0]), min(PB, nc - C0[1]), min(PB, nc - C0[2])};
+  PPAcc acc;
+  if (!pp_block(a, C0, B, sm, pts, acc) && threadIdx.x == 0) a.ovf_brick[atomicAdd(&a.novf[0], 1)] = b;
+  pp_reduce(a, acc.npairs, acc.nwork, acc.f2max);
+}
+
+// level 1: the cells of listed bricks, one at a time (persistent CTAs)
+__global__ void __launch_bounds__(PP_THREADS) k_pp_cells(PPArgs a) {
+  __shared__ PPSmem sm;
+  extern __shared__ float4 pts[];
+  const Geo& g = a.g;
+  const int nc = g.nc;
+  const int n = a.novf[0] * PNCORE_MAX;
+  PPAcc acc;
+  for (int it = blockIdx.x; it < n; it += gridDim.x) {
+    int b = a.ovf_brick[it / PNCORE_MAX], l = it % PNCORE_MAX;
+    int C0[3] = {(b % a.nb) * PB + l % PB, ((b / a.nb) % a.nb) * PB + (l / PB) % PB,
+                 (b / (a.nb * a.nb)) * PB + l / (PB * PB)};
+    if (C0[0] >= nc || C0[1] >= nc || C0[2] >= nc) continue;
+    const int B[3] = {1, 1, 1};
+    if (!pp_block(a, C0, B, sm, pts, acc)) {
+      if (threadIdx.x == 0) a.ovf_cell[atomicAdd(&a.novf[1], 1)] = (int)cell_id(g, C0[0], C0[1], C0[2]);
+      __syncthreads();
+    }
+  }
+  pp_reduce(a, acc.npairs, acc.nwork, acc.f2max);
+}
+
+// level 2: listed cells from global memory, one CTA per cell (persistent)
+__global__ void __launch_bounds__(PP_THREADS) k_pp_dense(PPArgs a) {
+  const Geo& g = a.g;
+  const int n = a.novf[1];
+  PPAcc acc;
+  for (int it = blockIdx.x; it < n; it += gridDim.x) {
+    int64_t c = a.ovf_cell[it];
+    int gc[3];
+    cell_coords(g, c, gc[0], gc[1], gc[2]);
+    int64_t p1 = a.cstart[c + 1];
+    for (int64_t p = a.cstart[c] + threadIdx.x; p < p1; p += blockDim.x) {
+      float x1[3];
+      int fi[3], lo[3], hi[3];
+      for (int d = 0; d < 3; d++) {
+        x1[d] = fine_off(load_code(a.xp, 3 * p + d, g.izipx), g.izipx);
+        fi[d] = (int)floorf(x1[d]);
+        lo[d] = fi[d] == 0 ? -1 : 0;
+        hi[d] = fi[d] == g.ncell - 1 ? 1 : 0;
+      }
+      long long f[3] = {0, 0, 0};
+      for (int dz = lo[2]; dz <= hi[2]; dz++)
+        for (int dy = lo[1]; dy <= hi[1]; dy++)
+          for (int dx = lo[0]; dx <= hi[0]; dx++) {
+            int64_t S = cell_id(g, wrap1(gc[0] + dx, g.nc), wrap1(gc[1] + dy, g.nc), wrap1(gc[2] + dz, g.nc));
+            int64_t q1 = a.cstart[S + 1];
+            float sh[3] = {(float)(4 * dx), (float)(4 * dy), (float)(4 * dz)};
+            for (int64_t q = a.cstart[S]; q < q1; q++) {
+              float r[3];
+              bool near = true;
+              for (int d = 0; d < 3; d++) {
+                float x2 = __fadd_rn(sh[d], fine_off(load_code(a.xp, 3 * q + d, g.izipx), g.izipx));
+                near = near && abs((int)floorf(x2) - fi[d]) <= 1;
+                r[d] = x2 - x1[d];
+              }
+              if (!near) continue;
+              acc.npairs++;
+              pair_force(a, r[0], r[1], r[2], f);
+            }
+          }
+      acc.nwork++;
+      acc.f2max = fmaxf(acc.f2max, pp_kick(a, p, f));
+    }
+  }
+  pp_reduce(a, acc.npairs, acc.nwork, acc.f2max);
+}
+
+// forced start level (tests): list every brick, or every cell
+__global__ void k_pp_list_all(int* list, int n, int* count) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) list[i] = i;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *count = n;
 }
 
 }  // namespace
@@ -129,7 +369,7 @@ int cube_pp_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st) {
   a.np = c->np;
   a.xp = c->xp[c->cur];
   a.vp = c->vp[c->cur];
-  a.pcell = c->pcell[c->cur];
+  a.rhoc = c->rhoc[c->cur];
   a.cstart = c->cstart[c->cur];
   a.mass = c->p.mass_p;
   a.rsoft = c->p.rsoft;
@@ -139,10 +379,31 @@ int cube_pp_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st) {
   a.exact_only = c->opt_exact_kicks;
   a.fpp = c->fpp;
   a.st = c->dstats;
+  a.nb = (c->p.nc + PB - 1) / PB;
+  int64_t nbrick = (int64_t)a.nb * a.nb * a.nb;
+  if (nbrick > c->pp_brick_cap) return cube_fail(c, CUBE_ERR_ARG, "PP brick list too small");
+  a.ovf_brick = c->pp_ovf_brick;
+  a.ovf_cell = c->pp_ovf_cell;
+  a.novf = c->pp_novf;
+  CUBE_CUDA(c, cudaMemsetAsync(c->pp_novf, 0, 2 * sizeof(int), c->stream));
+  for (auto k : {k_pp_bricks, k_pp_cells})
+    CUBE_CUDA(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PP_SMEM));
+  int persist = cube_grid((int64_t)1 << 40, 1, 4);
   cube_phase_begin(c, PH_PP);
-  k_pp<<<cube_grid(c->np, 256), 256, 0, c->stream>>>(a);
-  cube_phase_end(c, PH_PP);
+  if (c->opt_pp_level == 1) {
+    k_pp_list_all<<<cube_grid(nbrick, 256), 256, 0, c->stream>>>(c->pp_ovf_brick, (int)nbrick, c->pp_novf);
+  } else if (c->opt_pp_level == 2) {
+    k_pp_list_all<<<cube_grid(c->ncells, 256), 256, 0, c->stream>>>(c->pp_ovf_cell, (int)c->ncells, c->pp_novf + 1);
+  } else {
+    k_pp_bricks<<<(unsigned)nbrick, PP_THREADS, PP_SMEM, c->stream>>>(a);
+  }
   CUBE_CUDA(c, cudaGetLastError());
+  k_pp_cells<<<persist, PP_THREADS, PP_SMEM, c->stream>>>(a);
+  CUBE_CUDA(c, cudaGetLastError());
+  k_pp_dense<<<persist, PP_THREADS, 0, c->stream>>>(a);
+  CUBE_CUDA(c, cudaGetLastError());
+  cube_phase_end(c, PH_PP);
+  CUBE_CUDA(c, cudaMemcpyAsync(c->pp_novf_host, c->pp_novf, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   r = cube_stats_fetch(c);
   if (r) return r;
   if ((int64_t)c->hstats->itest1 != c->np)
@@ -151,6 +412,7 @@ int cube_pp_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st) {
     st->f2_max_pp = bits_float(c->hstats->f2_pp_bits);
     st->npairs = (int64_t)c->hstats->npairs;
     st->itest1 = (int64_t)c->hstats->itest1;
+    st->pp_dense_bricks = c->pp_novf_host[0];
   }
   return CUBE_OK;
 }

@@ -33,6 +33,7 @@ EXPORTS = ["cube_create", "cube_destroy", "cube_last_error", "cube_upload_state"
            "cube_synchronize", "cube_timing", "cube_timing_read", "cube_phase_name", "cube_stream",
            "cube_codec_check", "cube_set_option"]
 OPT_EXACT_KICKS = 1
+OPT_PP_LEVEL = 2
 NPHASE = 15
 
 
@@ -49,7 +50,7 @@ class CubeStats(ctypes.Structure):
                 ("ndup", ctypes.c_int64), ("sum_c", ctypes.c_double), ("sum_r", ctypes.c_double),
                 ("sum_s", ctypes.c_double), ("sigma_vi_new", ctypes.c_float), ("nlayer", ctypes.c_int32),
                 ("max_disp", ctypes.c_int32), ("pad0", ctypes.c_int32), ("f2_max_pp", ctypes.c_float),
-                ("pad1", ctypes.c_int32), ("npairs", ctypes.c_int64), ("itest1", ctypes.c_int64),
+                ("pp_dense_bricks", ctypes.c_int32), ("npairs", ctypes.c_int64), ("itest1", ctypes.c_int64),
                 ("f2_max_fine", ctypes.c_float), ("f2_max_coarse", ctypes.c_float),
                 ("vmax", ctypes.c_float * 3), ("pad2", ctypes.c_int32), ("testrhof", ctypes.c_double),
                 ("testrhoc", ctypes.c_double), ("flags", ctypes.c_int32), ("pad3", ctypes.c_int32)]

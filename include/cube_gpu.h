@@ -78,7 +78,7 @@ typedef struct cube_stats {
   int32_t pad0;
   /* cube_pp_force (ext_pp_force.f90:10-162) */
   float f2_max_pp;
-  int32_t pad1;
+  int32_t pp_dense_bricks; /* bricks redone cell by cell (too dense to stage) */
   int64_t npairs;
   int64_t itest1;
   /* cube_particle_mesh (pm.f90:2-415) */
@@ -179,8 +179,13 @@ void* cube_stream(cube_ctx* ctx);
 /* Run-time options.  CUBE_OPT_EXACT_KICKS=1 makes every kernel evaluate the
    reference's FP64 expressions directly instead of the certified FP32 /
    float-float fast paths (results are identical by construction; used to test
-   that claim and to time it). */
-enum cube_option { CUBE_OPT_EXACT_KICKS = 1 };
+   that claim and to time it).  CUBE_OPT_PP_LEVEL=2 sets the first of the
+   three PP levels (0: 4^3-cell bricks staged in shared memory, the default;
+   1: single cells staged; 2: global memory, one CTA per cell), which
+   otherwise serve only regions too dense for the level before.  The pair sums
+   are order-independent, so every level gives bitwise the same result; used
+   to test the dense-region paths. */
+enum cube_option { CUBE_OPT_EXACT_KICKS = 1, CUBE_OPT_PP_LEVEL = 2 };
 int cube_set_option(cube_ctx* ctx, int option, int64_t value);
 
 /* Velocity-code self check: encodes n host doubles with sigma both by the

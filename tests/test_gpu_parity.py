@@ -178,6 +178,46 @@ def test_pp_force(name, pk, sk):
     g.close()
 
 
+def test_pp_dense_bricks_match_oracle():
+    # two cells hold ~3000 particles each: their bricks exceed the shared-memory
+    # staging capacity and are redone cell by cell, and those cells go through
+    # the global-memory kernel
+    p = _params(dict(nc=24, nnt=2))
+    st = synth.random_state(p, mean_per_cell=3, seed=21, clump=2, clump_mult=1000)
+    g, o = make_pair(p, st)
+    a = g.ext_pp_force(A_MID, DT)
+    b = o.pp_force(A_MID, DT)
+    assert a["pp_dense_bricks"] > 0
+    assert a["npairs"] == b["npairs"]
+    assert a["itest1"] == b["itest1"] == st["xp"].shape[0]
+    assert abs(a["f2_max_pp"] - b["f2_max_pp"]) <= 1e-5 * b["f2_max_pp"]
+    d = np.abs(g.download()["vp"].astype(np.int64) - o.state()["vp"].astype(np.int64))
+    assert d.max() <= MAX_CODE_DIFF and (d > 0).mean() < MAX_DIFF_FRAC
+    g.close()
+
+
+@pytest.mark.parametrize("clump", [0, 2])
+def test_pp_levels_agree_bitwise(clump):
+    # fixed-point pair sums make the result independent of which kernel (staged
+    # brick, staged cell, global memory) handles a particle
+    p = _params(dict(nc=24, nnt=2))
+    st = synth.random_state(p, mean_per_cell=6, seed=22, clump=clump, clump_mult=600)
+    outs = []
+    for level in (0, 1, 2):
+        g = C.CubeGPU(p)
+        g.upload(st["xp"], st["vp"], st["pid"], st["rhoc"], st["vfield"])
+        s = np.float32(st["sigma_vi"])
+        g.set_sigma(s, s)
+        g.set_option(C.OPT_PP_LEVEL, level)
+        outs.append((g.ext_pp_force(A_MID, DT), g.download()["vp"]))
+        g.close()
+    if clump:
+        assert outs[0][0]["pp_dense_bricks"] > 0
+    for sb, vb in outs[1:]:
+        assert np.array_equal(outs[0][1], vb)
+        assert sb["npairs"] == outs[0][0]["npairs"] and sb["f2_max_pp"] == outs[0][0]["f2_max_pp"]
+
+
 def test_particle_mesh_step_matches_oracle():
     p = _params(dict(nc=24, nnt=2))
     st = synth.random_state(p, seed=11, clump=10)
