@@ -55,8 +55,10 @@ def dist_init():
     rank = int(os.environ.get("RANK", "0"))
     lrank = int(os.environ.get("LOCAL_RANK", "0"))
     if ws > 1:
+        import torch
         import torch.distributed as dist
-        dist.init_process_group("nccl")
+        # one process per GPU over NCCL; gloo where there is no GPU (host tests)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     return ws, rank, lrank
 
 
@@ -84,6 +86,12 @@ def allreduce_sum(x, ws, device):
     t = torch.tensor([x], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.SUM)
     return float(t.item())
+
+
+def replica_throughput(units, seconds, ws, device):
+    """Whole-job throughput of ws independent replicas (no data-path
+    collective): the units all ranks processed over the slowest rank's time."""
+    return allreduce_sum(float(units), ws, device) / allreduce_max(float(seconds), ws, device)
 
 
 class ClockSampler:
@@ -222,7 +230,7 @@ def run_gb300(args, ws, rank, lrank):
     barrier(ws)
     ms_max = allreduce_max(ms, ws, dev)
     ntot = allreduce_sum(float(n0), ws, dev)
-    value = ntot * args.steps / (ms_max / 1000.0)
+    value = replica_throughput(n0 * args.steps, ms / 1000.0, ws, dev)
 
     # per-phase device time (timers on, a separate pass so the headline is unperturbed)
     g.timing(True)
@@ -290,7 +298,7 @@ def run_gb300(args, ws, rank, lrank):
 def gpu_launches(p, steps):
     """Launches of this library's kernels per step (cuFFT kernels not counted)."""
     upd = 2 + 3 + 1 + 1        # dest, rank, scan x3, scatter, sigma
-    pp = 1 if p.pp_on else 0
+    pp = 3 if p.pp_on else 0   # staged bricks, staged cells, dense cells
     fine = 1 + 1 + 1 + 1       # deposit, green, f2max, kick
     coarse = 1 + 1 + 1 + 1
     dec = 1                    # decode table when sigma changes
