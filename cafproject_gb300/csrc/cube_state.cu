@@ -2,6 +2,7 @@
 // velocity-code tables, the deterministic exclusive scan (the spine of
 // variables.f90:96-211) and the statistics read-back.
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "cube_internal.cuh"
@@ -286,5 +287,75 @@ extern "C" int cube_codec_check(cube_ctx* c, float sigma, const double* v, int64
   cudaFree(dv);
   cudaFree(dd);
   cudaFree(dt);
+  return CUBE_OK;
+}
+
+// ------------------------------------------------- codec check, static scratch
+// cube_codec_check_static: the same check with its device scratch in a
+// file-scope array instead of per-call cudaMalloc/cudaFree.  It serves callers
+// that must not allocate device memory: a production run sizes np_max to fill
+// most of HBM, so a mid-run cudaMalloc can fail or fragment the pool, and
+// cudaFree synchronises the whole device, which stalls a monitoring thread's
+// caller and every other stream.  The array is CUBE_CODEC_STATIC_MAX doubles of
+// input followed by two CUBE_CODEC_STATIC_MAX int32 outputs (256 KiB); nothing
+// in it needs to start at zero (the kernel writes every output it reads back).
+// All contexts on one device share the array, so two calls whose device work
+// overlapped would race; each call holds a per-device host lock from its
+// first copy until its stream has drained.
+constexpr int64_t kCodecStaticBytes = CUBE_CODEC_STATIC_MAX * (8 + 4 + 4);
+static __device__ __align__(256) unsigned char g_codec_scratch[kCodecStaticBytes];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_codec_scratch_mu[kMaxDevices];
+unsigned char* g_codec_scratch_ptr[kMaxDevices] = {};  // device address, per device
+}  // namespace
+
+// First call on a device (with that device current) resolves the array's
+// device address; that resolution may load this module's device code, so the
+// first call belongs before any stream capture.
+static int codec_scratch_address(cube_ctx* c, unsigned char** out) {
+  if (!g_codec_scratch_ptr[c->device]) {
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_codec_scratch);
+    if (e != cudaSuccess || !ptr)
+      return cube_fail(c, CUBE_ERR_CUDA, std::string("cudaGetSymbolAddress(codec scratch): ") + cudaGetErrorString(e));
+    g_codec_scratch_ptr[c->device] = static_cast<unsigned char*>(ptr);
+  }
+  *out = g_codec_scratch_ptr[c->device];
+  return CUBE_OK;
+}
+
+extern "C" int cube_codec_check_static(cube_ctx* c, float sigma, const double* v, int64_t n, int32_t* direct,
+                                       int32_t* table) {
+  if (!c || !v || !direct || !table || n < 0) return CUBE_ERR_ARG;
+  if (n > CUBE_CODEC_STATIC_MAX)
+    return cube_fail(c, CUBE_ERR_ARG, "n = " + std::to_string(n) + " exceeds the static scratch maximum of " +
+                                          std::to_string((long long)CUBE_CODEC_STATIC_MAX) + " values");
+  CUBE_CUDA(c, cudaSetDevice(c->device));
+  if (c->device < 0 || c->device >= kMaxDevices) return cube_fail(c, CUBE_ERR_ARG, "device ordinal out of range");
+  std::lock_guard<std::mutex> lock(g_codec_scratch_mu[c->device]);
+  unsigned char* base = nullptr;
+  int r = codec_scratch_address(c, &base);
+  if (r) return r;
+  CodecView k;
+  r = cube_codec_pair(c, sigma, sigma, &k, nullptr);
+  if (r) return r;
+  if (n == 0) return CUBE_OK;
+  double* dv = reinterpret_cast<double*>(base);
+  int32_t* dd = reinterpret_cast<int32_t*>(base + 8 * CUBE_CODEC_STATIC_MAX);
+  int32_t* dt = reinterpret_cast<int32_t*>(base + 12 * CUBE_CODEC_STATIC_MAX);
+  // every early return below first drains the stream, so the lock is never
+  // released with work on the shared array still in flight
+  cudaError_t e = cudaMemcpyAsync(dv, v, 8 * (size_t)n, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) {
+    k_codec_check<<<cube_grid(n, 256), 256, 0, c->stream>>>(dv, n, vcoef_host(sigma), c->nvbin, k, dd, dt);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(direct, dd, 4 * (size_t)n, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(table, dt, 4 * (size_t)n, cudaMemcpyDeviceToHost, c->stream);
+  cudaError_t es = cudaStreamSynchronize(c->stream);
+  if (e == cudaSuccess) e = es;
+  if (e != cudaSuccess) return cube_fail(c, CUBE_ERR_CUDA, std::string("codec check (static scratch): ") + cudaGetErrorString(e));
   return CUBE_OK;
 }

@@ -31,7 +31,8 @@ EXPORTS = ["cube_create", "cube_destroy", "cube_last_error", "cube_upload_state"
            "cube_pm_fine_forces", "cube_pm_fine_kick",
            "cube_pm_coarse_forces", "cube_pm_coarse_kick", "cube_get_field", "cube_set_field", "cube_nplocal",
            "cube_synchronize", "cube_timing", "cube_timing_read", "cube_phase_name", "cube_stream",
-           "cube_codec_check", "cube_set_option"]
+           "cube_codec_check", "cube_codec_check_static", "cube_set_option"]
+CODEC_STATIC_MAX = 16384
 OPT_EXACT_KICKS = 1
 OPT_PP_LEVEL = 2
 NPHASE = 15
@@ -108,6 +109,7 @@ def load_library(path=None):
     L.cube_stream.argtypes = [P]
     L.cube_stream.restype = ctypes.c_void_p
     L.cube_codec_check.argtypes = [P, F, P, I64, P, P]
+    L.cube_codec_check_static.argtypes = [P, F, P, I64, P, P]
     L.cube_set_option.argtypes = [P, ctypes.c_int, I64]
     _lib = L
     return L
@@ -269,6 +271,15 @@ class CubeGPU:
         a = np.empty(v.size, np.int32)
         b = np.empty(v.size, np.int32)
         self._check(self.L.cube_codec_check(self.h, float(sigma), _ptr(v), v.size, _ptr(a), _ptr(b)))
+        return a, b
+
+    def codec_check_static(self, sigma, v):
+        """codec_check through the entry point whose device scratch is a fixed
+        array (at most CODEC_STATIC_MAX values, no device allocation)."""
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        a = np.empty(v.size, np.int32)
+        b = np.empty(v.size, np.int32)
+        self._check(self.L.cube_codec_check_static(self.h, float(sigma), _ptr(v), v.size, _ptr(a), _ptr(b)))
         return a, b
 
     def timing(self, enable):

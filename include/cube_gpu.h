@@ -193,6 +193,19 @@ int cube_set_option(cube_ctx* ctx, int option, int64_t value);
    kernels use; writes both codes (host arrays of n int32). */
 int cube_codec_check(cube_ctx* ctx, float sigma, const double* v, int64_t n, int32_t* direct, int32_t* table);
 
+/* cube_codec_check without any device allocation (no counterpart in the
+   reference): the device scratch is a fixed file-scope array of
+   CUBE_CODEC_STATIC_MAX input values, shared by every call on a device, for
+   callers that must not allocate (a run whose particle arrays fill HBM; a
+   monitoring thread that must not trigger cudaFree's device-wide
+   synchronisation).  n > CUBE_CODEC_STATIC_MAX returns CUBE_ERR_ARG.  The
+   first call on each device resolves the array's address and should come
+   before any stream capture.  Calls are serialised per device by a host lock;
+   each returns after its stream has drained. */
+#define CUBE_CODEC_STATIC_MAX 16384
+int cube_codec_check_static(cube_ctx* ctx, float sigma, const double* v, int64_t n, int32_t* direct,
+                            int32_t* table);
+
 #ifdef __cplusplus
 }
 #endif
