@@ -389,12 +389,28 @@ __device__ __forceinline__ bool nint_certified(float xf, float E, long long* out
   return true;
 }
 
+// x/c correctly rounded, for a constant c with rc = RN(1/c): q = RN(x*rc), the
+// residual x - q*c is exact in one FMA, and q + residual*rc rounds to RN(x/c)
+// (Markstein's correction step, IBM J. Res. Dev. 34(1), 1990).  For c = 6 and
+// c = pi_f the identity with __fdiv_rn is checked for every float in the
+// window below by cube_arith_check; zeros, tiny, huge and non-finite x take
+// the IEEE division.
+constexpr float kDivLo = 7.888609052210118e-31f;  // 2^-100
+constexpr float kDivHi = 1.2676506002282294e30f;  // 2^100
+__device__ __forceinline__ float div_const(float x, float c, float rc) {
+  float ax = fabsf(x);
+  if (!(ax >= kDivLo && ax <= kDivHi)) return __fdiv_rn(x, c);
+  float q = __fmul_rn(x, rc);
+  float r = __fmaf_rn(-q, c, x);
+  return __fmaf_rn(r, rc, q);
+}
+
 // one CIC kick term force*a_mid*dt/6/pi*wa*wb*wc in real(4), left to right (pm.f90:146)
 __device__ __forceinline__ float kick_term(float f, float a_mid, float dt, float wa, float wb, float wc) {
   float r = __fmul_rn(f, a_mid);
   r = __fmul_rn(r, dt);
-  r = __fdiv_rn(r, 6.0f);
-  r = __fdiv_rn(r, CUBE_PI_F);
+  r = div_const(r, 6.0f, 0.16666667163372040f);         // RN(1/6)
+  r = div_const(r, CUBE_PI_F, 0.31830987334251404f);    // RN(1/pi_f)
   r = __fmul_rn(r, wa);
   r = __fmul_rn(r, wb);
   return __fmul_rn(r, wc);

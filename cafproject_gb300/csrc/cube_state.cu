@@ -290,6 +290,45 @@ extern "C" int cube_codec_check(cube_ctx* c, float sigma, const double* v, int64
   return CUBE_OK;
 }
 
+// ------------------------------------------------------ arithmetic self check
+// Every float bit pattern x (NaN excluded): div_const(x, c, RN(1/c)) against
+// the IEEE division __fdiv_rn(x, c) for c = 6 and c = pi_f, the two divisors of
+// the kick terms.  Counts differing results (bitwise) per divisor.
+__global__ void k_arith_check(unsigned long long* mism) {
+  unsigned long long m6 = 0, mpi = 0;
+  const float r6 = __frcp_rn(6.0f), rpi = __frcp_rn(CUBE_PI_F);
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < (1ull << 32);
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    float x = __uint_as_float((unsigned int)i);
+    if (x != x) continue;
+    m6 += __float_as_uint(div_const(x, 6.0f, r6)) != __float_as_uint(__fdiv_rn(x, 6.0f));
+    mpi += __float_as_uint(div_const(x, CUBE_PI_F, rpi)) != __float_as_uint(__fdiv_rn(x, CUBE_PI_F));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    m6 += __shfl_xor_sync(0xffffffffu, m6, o);
+    mpi += __shfl_xor_sync(0xffffffffu, mpi, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(mism, m6);
+    atomicAdd(mism + 1, mpi);
+  }
+}
+
+extern "C" int cube_arith_check(cube_ctx* c, int64_t* mismatches) {
+  if (!c || !mismatches) return CUBE_ERR_ARG;
+  CUBE_CUDA(c, cudaSetDevice(c->device));
+  unsigned long long* d = reinterpret_cast<unsigned long long*>(c->red_tmp);  // >= 2 doubles of scratch
+  CUBE_CUDA(c, cudaMemsetAsync(d, 0, 2 * sizeof(unsigned long long), c->stream));
+  k_arith_check<<<cube_grid((int64_t)1 << 32, 256, 8), 256, 0, c->stream>>>(d);
+  CUBE_CUDA(c, cudaGetLastError());
+  unsigned long long h[2] = {0, 0};
+  CUBE_CUDA(c, cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  CUBE_CUDA(c, cudaStreamSynchronize(c->stream));
+  mismatches[0] = (int64_t)h[0];
+  mismatches[1] = (int64_t)h[1];
+  return CUBE_OK;
+}
+
 // ------------------------------------------------- codec check, static scratch
 // cube_codec_check_static: the same check with its device scratch in a
 // file-scope array instead of per-call cudaMalloc/cudaFree.  It serves callers

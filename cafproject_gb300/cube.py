@@ -31,7 +31,7 @@ EXPORTS = ["cube_create", "cube_destroy", "cube_last_error", "cube_upload_state"
            "cube_pm_fine_forces", "cube_pm_fine_kick",
            "cube_pm_coarse_forces", "cube_pm_coarse_kick", "cube_get_field", "cube_set_field", "cube_nplocal",
            "cube_synchronize", "cube_timing", "cube_timing_read", "cube_phase_name", "cube_stream",
-           "cube_codec_check", "cube_codec_check_static", "cube_set_option"]
+           "cube_codec_check", "cube_codec_check_static", "cube_arith_check", "cube_set_option"]
 CODEC_STATIC_MAX = 16384
 OPT_EXACT_KICKS = 1
 OPT_PP_LEVEL = 2
@@ -110,6 +110,7 @@ def load_library(path=None):
     L.cube_stream.restype = ctypes.c_void_p
     L.cube_codec_check.argtypes = [P, F, P, I64, P, P]
     L.cube_codec_check_static.argtypes = [P, F, P, I64, P, P]
+    L.cube_arith_check.argtypes = [P, P]
     L.cube_set_option.argtypes = [P, ctypes.c_int, I64]
     _lib = L
     return L
@@ -272,6 +273,13 @@ class CubeGPU:
         b = np.empty(v.size, np.int32)
         self._check(self.L.cube_codec_check(self.h, float(sigma), _ptr(v), v.size, _ptr(a), _ptr(b)))
         return a, b
+
+    def arith_check(self):
+        """Mismatches of the fast division by 6 and by pi_f against the IEEE
+        division over every float (expected (0, 0))."""
+        m = np.zeros(2, np.int64)
+        self._check(self.L.cube_arith_check(self.h, _ptr(m)))
+        return int(m[0]), int(m[1])
 
     def codec_check_static(self, sigma, v):
         """codec_check through the entry point whose device scratch is a fixed

@@ -193,6 +193,12 @@ int cube_set_option(cube_ctx* ctx, int option, int64_t value);
    kernels use; writes both codes (host arrays of n int32). */
 int cube_codec_check(cube_ctx* ctx, float sigma, const double* v, int64_t n, int32_t* direct, int32_t* table);
 
+/* Arithmetic self check: the kick terms divide by 6 and by pi_f with an
+   FMA-corrected reciprocal product instead of the IEEE division; this runs
+   both over every float bit pattern (NaN excluded) and writes the number of
+   differing results for each divisor into mismatches[0..1] (expected 0). */
+int cube_arith_check(cube_ctx* ctx, int64_t* mismatches);
+
 /* cube_codec_check without any device allocation (no counterpart in the
    reference): the device scratch is a fixed file-scope array of
    CUBE_CODEC_STATIC_MAX input values, shared by every call on a device, for

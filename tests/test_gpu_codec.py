@@ -121,3 +121,12 @@ def test_fast_paths_equal_fp64_expressions_over_full_steps():
         for k in ("nplocal", "nlost", "ndup", "nlayer", "npairs", "f2_max_fine", "f2_max_coarse", "vmax",
                   "sigma_vi_new"):
             assert x[k] == y[k], k
+
+
+def test_kick_division_by_constant_is_ieee_for_every_float():
+    # the kick terms' /6 and /pi use an FMA-corrected reciprocal product
+    g = C.CubeGPU(P.CubeParams(nc=24, nnt=2, pp_on=True))
+    try:
+        assert g.arith_check() == (0, 0)
+    finally:
+        g.close()
