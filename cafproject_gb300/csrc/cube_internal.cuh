@@ -338,22 +338,29 @@ __device__ __forceinline__ bool certify_abs(long long ab, float E, const CodecVi
   float u0 = k.amp * atanf(k.cf * af);
   int m = (int)(u0 + 0.5f);
   long long n = m < 0 ? 0 : (m > k.nmax ? k.nmax : m);
-  while (n < k.nmax && __ldg(k.bnd + n + 1) <= ab) n++;
-  while (n > 0 && __ldg(k.bnd + n) > ab) n--;
+  // the FP32 estimate is within a few hundredths of a code: probe its bin with
+  // two independent loads, walk only when it fell on the wrong side of an edge
+  long long lb = n > 0 ? __ldg(k.bnd + n) : 0;
+  long long ub = n < k.nmax ? __ldg(k.bnd + n + 1) : 0x7fffffffffffffffLL;
+  if (ab < lb || ab >= ub) {
+    while (n < k.nmax && __ldg(k.bnd + n + 1) <= ab) n++;
+    while (n > 0 && __ldg(k.bnd + n) > ab) n--;
+    lb = n > 0 ? __ldg(k.bnd + n) : 0;
+    ub = n < k.nmax ? __ldg(k.bnd + n + 1) : 0x7fffffffffffffffLL;
+  }
   *n_out = n;
   int e = (int)((ab >> 52) & 0x7ff);
   if (e == 0 || e >= 0x7fe) return n == 0 && e == 0;  // subnormal |V| is deep inside code 0
-  float kf = ldexpf(E, 1075 - e);                      // E in ulps of this binade
+  int sh = 1075 - e;                                   // E in ulps of this binade: E * 2^sh
+  float kf = (sh >= -126 && sh <= 127) ? __fmul_rn(E, __int_as_float((127 + sh) << 23)) : ldexpf(E, sh);
   if (!(kf < 4.0e15f)) return false;
-  long long kk = (long long)kf + 1;
+  long long kk = (kf < 2147483648.0f ? (long long)(unsigned int)kf : (long long)kf) + 1;
   long long blo = (long long)e << 52, bhi = (long long)(e + 1) << 52;
   if (n > 0) {
-    long long lb = __ldg(k.bnd + n);
     long long lx = lb > blo ? lb : blo;
     if (ab - lx <= kk) return false;
   }
   if (n < k.nmax) {
-    long long ub = __ldg(k.bnd + n + 1);
     long long ux = ub < bhi ? ub : bhi;
     if (ux - ab <= kk) return false;
   }

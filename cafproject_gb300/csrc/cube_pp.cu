@@ -216,26 +216,44 @@ __device__ bool pp_block(const PPArgs& a, const int C0[3], const int B[3], PPSme
   if (threadIdx.x == 0) sm.nst = 0;
   __syncthreads();
   const int total = block_exclusive_scan(sm.pref, NS);
-  // stage the particles whose fine cell lies in the block or its fine ring
-  for (int j = threadIdx.x; j < total; j += blockDim.x) {
-    int s = upper_index(sm.pref, NS, j);
-    int64_t p = sm.sstart[s] + (j - sm.pref[s]);
-    int sl[3] = {s % S0 - 1, (s / S0) % S1 - 1, s / (S0 * S1) - 1};
-    float x[3];
-    int fi[3];
-    bool in = true;
-    for (int d = 0; d < 3; d++) {
-      x[d] = __fadd_rn((float)(4 * sl[d]), fine_off(load_code(a.xp, 3 * p + d, g.izipx), g.izipx));
-      fi[d] = (int)floorf(x[d]) + 1;  // 0 .. 4B+1 inside the staged region
-      in = in && fi[d] >= 0 && fi[d] <= 4 * B[d] + 1;
+  // stage the particles whose fine cell lies in the block or its fine ring;
+  // one warp per row of S0 cells along x (a contiguous range of j), the cell of
+  // each j found by comparing against the row's prefix values in registers
+  const int lane = threadIdx.x & 31;
+  for (int row = threadIdx.x >> 5; row < S1 * S2; row += blockDim.x >> 5) {
+    const int t0 = row * S0;
+    int rp[PS_MAX];
+#pragma unroll
+    for (int q = 0; q < PS_MAX; q++) rp[q] = q < S0 ? sm.pref[t0 + q] : 0x7fffffff;
+    const int jend = t0 + S0 < NS ? sm.pref[t0 + S0] : total;
+    const int sy = row % S1 - 1, sz = row / S1 - 1;
+    for (int j = rp[0] + lane; j < jend; j += 32) {
+      int cs = rp[0], sxl = 0;
+#pragma unroll
+      for (int q = 1; q < PS_MAX; q++)
+        if (rp[q] <= j) {
+          cs = rp[q];
+          sxl = q;
+        }
+      int64_t p = sm.sstart[t0 + sxl] + (j - cs);
+      const int sl[3] = {sxl - 1, sy, sz};
+      float x[3];
+      int fi[3];
+      bool in = true;
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        x[d] = __fadd_rn((float)(4 * sl[d]), fine_off(load_code(a.xp, 3 * p + d, g.izipx), g.izipx));
+        fi[d] = (int)floorf(x[d]) + 1;  // 0 .. 4B+1 inside the staged region
+        in = in && fi[d] >= 0 && fi[d] <= 4 * B[d] + 1;
+      }
+      if (!in) continue;
+      int slot = atomicAdd(&sm.nst, 1);
+      if (slot >= PP_CAP) continue;
+      int f = fi[0] + F0 * (fi[1] + F1 * fi[2]);
+      int r = atomicAdd(&bins[f], 1);
+      pts[slot] = make_float4(x[0], x[1], x[2], __int_as_float((int)p));
+      kinfo[slot] = (unsigned)f | ((unsigned)r << 13);
     }
-    if (!in) continue;
-    int slot = atomicAdd(&sm.nst, 1);
-    if (slot >= PP_CAP) continue;
-    int f = fi[0] + F0 * (fi[1] + F1 * fi[2]);
-    int r = atomicAdd(&bins[f], 1);
-    pts[slot] = make_float4(x[0], x[1], x[2], __int_as_float((int)p));
-    kinfo[slot] = (unsigned)f | ((unsigned)r << 13);
   }
   __syncthreads();
   const int nst = sm.nst;
