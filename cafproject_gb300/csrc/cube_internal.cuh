@@ -438,6 +438,69 @@ __device__ __forceinline__ void atomic_max_pos(unsigned int* addr, float v) {
   atomicMax(addr, __float_as_uint(v));
 }
 
+// ------------------------------------------------------- block helpers
+// In-place exclusive scan of n ints by the whole block (blockDim.x a multiple
+// of 32, at most 1024); returns the total to every thread.  Each thread scans a
+// contiguous run, the run sums are scanned across warps.  Ends with a barrier.
+__device__ __forceinline__ int block_exclusive_scan(int* v, int n) {
+  __shared__ int wsum[32];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5, nw = blockDim.x >> 5;
+  const int per = (n + blockDim.x - 1) / blockDim.x;
+  const int b0 = min(n, t * per), b1 = min(n, b0 + per);
+  int s = 0;
+  for (int i = b0; i < b1; i++) s += v[i];
+  int inc = s;
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += y;
+  }
+  if (lane == 31) wsum[w] = inc;
+  __syncthreads();
+  int wbase = 0, total = 0;
+  for (int k = 0; k < nw; k++) {
+    int x = wsum[k];
+    if (k < w) wbase += x;
+    total += x;
+  }
+  int run = wbase + inc - s;
+  for (int i = b0; i < b1; i++) {
+    int x = v[i];
+    v[i] = run;
+    run += x;
+  }
+  __syncthreads();
+  return total;
+}
+
+// Visit every particle of a box of source cells: cell t = sx + S0*row has
+// pref[t] particles before it (exclusive scan over the box, pref[ns] not
+// needed) and its first particle at sstart[t].  One warp per row of S0 <= S0MAX
+// cells along x: the row's particles are consecutive in j, and the cell of
+// each j is found by comparing with the row's prefix values held in registers.
+// f(p, sx, row) is called once per particle (p its storage index).
+template <int S0MAX, class F>
+__device__ __forceinline__ void for_box_particles(const int* pref, const long long* sstart, int S0, int nrows,
+                                                  int total, F&& f) {
+  const int lane = threadIdx.x & 31;
+  for (int row = threadIdx.x >> 5; row < nrows; row += blockDim.x >> 5) {
+    const int t0 = row * S0;
+    int rp[S0MAX];
+#pragma unroll
+    for (int q = 0; q < S0MAX; q++) rp[q] = q < S0 ? pref[t0 + q] : 0x7fffffff;
+    const int jend = row + 1 < nrows ? pref[t0 + S0] : total;
+    for (int j = rp[0] + lane; j < jend; j += 32) {
+      int cs = rp[0], sx = 0;
+#pragma unroll
+      for (int q = 1; q < S0MAX; q++)
+        if (rp[q] <= j) {
+          cs = rp[q];
+          sx = q;
+        }
+      f((int64_t)(sstart[t0 + sx] + (j - cs)), sx, row);
+    }
+  }
+}
+
 // ----------------------------------------------------- host-side entry points
 int cube_build_tables(cube_ctx* c);
 // decode/encode tables for up to two sigma values at once (built on demand)

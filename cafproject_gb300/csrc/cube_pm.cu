@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(256) k_deposit_det(DepArgs a) {
   constexpr int NSRC = SX * SY * SZ;
   constexpr int MX = MPC * BX, MY = MPC * BY, MZ = MPC * BZ;
   extern __shared__ unsigned long long acc[];  // MX*MY*MZ
-  __shared__ int pref[NSRC + 1];
+  __shared__ int pref[NSRC];
   __shared__ long long sstart[NSRC];
   __shared__ unsigned long long btot;
   const Geo& g = a.g;
@@ -121,28 +121,17 @@ __global__ void __launch_bounds__(256) k_deposit_det(DepArgs a) {
       cnt = a.rhoc[c];
       st = a.cstart[c];
     }
-    pref[t + 1] = cnt;
+    pref[t] = cnt;
     sstart[t] = st;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {  // tiny serial scan (<= 1000 entries)
-    pref[0] = 0;
-    for (int t = 1; t <= NSRC; t++) pref[t] += pref[t - 1];
-  }
-  __syncthreads();
-  int total = pref[NSRC];
-  for (int j = threadIdx.x; j < total; j += blockDim.x) {
-    int lo = 0, hi = NSRC;  // find s with pref[s] <= j < pref[s+1]
-    while (hi - lo > 1) {
-      int mid = (lo + hi) >> 1;
-      if (pref[mid] <= j) lo = mid;
-      else hi = mid;
-    }
-    int s = lo;
-    int64_t p = sstart[s] + (j - pref[s]);
-    int sl[3] = {s % SX - LO, (s / SX) % SY - LO, s / (SX * SY) - LO};
+  const int total = block_exclusive_scan(pref, NSRC);
+  const int lim[3] = {MPC * B[0], MPC * B[1], MPC * B[2]};
+  for_box_particles<SX>(pref, sstart, SX, SY * SZ, total, [&](int64_t p, int sxi, int row) {
+    const int sl[3] = {sxi - LO, row % SY - LO, row / SY - LO};
     int rel[3];
     float d1[3], d2[3];
+#pragma unroll
     for (int d = 0; d < 3; d++) {
       int gcd = wrap1(C0[d] + sl[d], nc), Tq, L;
       tile_local(g, gcd, Tq, L);
@@ -153,7 +142,6 @@ __global__ void __launch_bounds__(256) k_deposit_det(DepArgs a) {
       d2[d] = __fsub_rn(1.0f, d1[d]);
       rel[d] = MPC * sl[d] + (int)fl - MPC * (L - 1);  // mesh index relative to the brick
     }
-    int lim[3] = {MPC * B[0], MPC * B[1], MPC * B[2]};
 #pragma unroll
     for (int k = 0; k < 8; k++) {
       int ox = k & 1, oy = (k >> 1) & 1, oz = k >> 2;
@@ -167,7 +155,7 @@ __global__ void __launch_bounds__(256) k_deposit_det(DepArgs a) {
                              (unsigned int)__fmul_rn(__fsub_rn(ws, fh), 16777216.0f);
       atomicAdd(&acc[x + MX * (y + MY * z)], q);
     }
-  }
+  });
   __syncthreads();
   unsigned long long mysum = 0;
   for (int i = threadIdx.x; i < MX * MY * MZ; i += blockDim.x) {
@@ -236,6 +224,8 @@ struct KickArgs {
   const void* vp_in;
   void* vp_out;            // may equal vp_in (fine kick updates in place)
   const int32_t* pcell;
+  const int32_t* rhoc;     // staged kernels: cell counts and starts
+  const int64_t* cstart;
   const float* vfield;
   const float* f[3];
   CodecView cin, cout;     // decode with sigma_in, encode with sigma_out
@@ -536,6 +526,8 @@ int cube_fine_kick_impl(cube_ctx* c, float a_mid, float dt) {
   k.vp_in = c->vp[c->cur];
   k.vp_out = c->vp[c->cur];
   k.pcell = c->pcell[c->cur];
+  k.rhoc = c->rhoc[c->cur];
+  k.cstart = c->cstart[c->cur];
   k.vfield = c->vfield[c->cur];
   for (int d = 0; d < 3; d++) k.f[d] = c->force_f[d];
   k.a_mid = a_mid;

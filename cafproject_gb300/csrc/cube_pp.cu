@@ -136,50 +136,6 @@ __device__ __forceinline__ void pp_reduce(const PPArgs& a, unsigned long long np
   }
 }
 
-// In-place exclusive scan of n ints by a block of 256 threads; returns the
-// total to every thread.  Each thread scans a contiguous run, the run sums are
-// scanned across warps.
-__device__ int block_exclusive_scan(int* v, int n) {
-  __shared__ int wsum[8];
-  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-  const int per = (n + 255) / 256;
-  const int b0 = min(n, t * per), b1 = min(n, b0 + per);
-  int s = 0;
-  for (int i = b0; i < b1; i++) s += v[i];
-  int inc = s;
-  for (int o = 1; o < 32; o <<= 1) {
-    int y = __shfl_up_sync(0xffffffffu, inc, o);
-    if (lane >= o) inc += y;
-  }
-  if (lane == 31) wsum[w] = inc;
-  __syncthreads();
-  int wbase = 0, total = 0;
-  for (int k = 0; k < 8; k++) {
-    int x = wsum[k];
-    if (k < w) wbase += x;
-    total += x;
-  }
-  int run = wbase + inc - s;
-  for (int i = b0; i < b1; i++) {
-    int x = v[i];
-    v[i] = run;
-    run += x;
-  }
-  __syncthreads();
-  return total;
-}
-
-// largest k in [0,n) with pref[k] <= j (pref non-decreasing, pref[0]=0)
-__device__ __forceinline__ int upper_index(const int* pref, int n, int j) {
-  int lo = 0, hi = n;
-  while (hi - lo > 1) {
-    int mid = (lo + hi) >> 1;
-    if (pref[mid] <= j) lo = mid;
-    else hi = mid;
-  }
-  return lo;
-}
-
 struct PPSmem {
   int pref[PNS_MAX + 1];         // ring-and-block particles before each staged cell
   long long sstart[PNS_MAX];     // first particle of each staged cell
@@ -216,45 +172,26 @@ __device__ bool pp_block(const PPArgs& a, const int C0[3], const int B[3], PPSme
   if (threadIdx.x == 0) sm.nst = 0;
   __syncthreads();
   const int total = block_exclusive_scan(sm.pref, NS);
-  // stage the particles whose fine cell lies in the block or its fine ring;
-  // one warp per row of S0 cells along x (a contiguous range of j), the cell of
-  // each j found by comparing against the row's prefix values in registers
-  const int lane = threadIdx.x & 31;
-  for (int row = threadIdx.x >> 5; row < S1 * S2; row += blockDim.x >> 5) {
-    const int t0 = row * S0;
-    int rp[PS_MAX];
+  // stage the particles whose fine cell lies in the block or its fine ring
+  for_box_particles<PS_MAX>(sm.pref, sm.sstart, S0, S1 * S2, total, [&](int64_t p, int sx, int row) {
+    const int sl[3] = {sx - 1, row % S1 - 1, row / S1 - 1};
+    float x[3];
+    int fi[3];
+    bool in = true;
 #pragma unroll
-    for (int q = 0; q < PS_MAX; q++) rp[q] = q < S0 ? sm.pref[t0 + q] : 0x7fffffff;
-    const int jend = t0 + S0 < NS ? sm.pref[t0 + S0] : total;
-    const int sy = row % S1 - 1, sz = row / S1 - 1;
-    for (int j = rp[0] + lane; j < jend; j += 32) {
-      int cs = rp[0], sxl = 0;
-#pragma unroll
-      for (int q = 1; q < PS_MAX; q++)
-        if (rp[q] <= j) {
-          cs = rp[q];
-          sxl = q;
-        }
-      int64_t p = sm.sstart[t0 + sxl] + (j - cs);
-      const int sl[3] = {sxl - 1, sy, sz};
-      float x[3];
-      int fi[3];
-      bool in = true;
-#pragma unroll
-      for (int d = 0; d < 3; d++) {
-        x[d] = __fadd_rn((float)(4 * sl[d]), fine_off(load_code(a.xp, 3 * p + d, g.izipx), g.izipx));
-        fi[d] = (int)floorf(x[d]) + 1;  // 0 .. 4B+1 inside the staged region
-        in = in && fi[d] >= 0 && fi[d] <= 4 * B[d] + 1;
-      }
-      if (!in) continue;
-      int slot = atomicAdd(&sm.nst, 1);
-      if (slot >= PP_CAP) continue;
-      int f = fi[0] + F0 * (fi[1] + F1 * fi[2]);
-      int r = atomicAdd(&bins[f], 1);
-      pts[slot] = make_float4(x[0], x[1], x[2], __int_as_float((int)p));
-      kinfo[slot] = (unsigned)f | ((unsigned)r << 13);
+    for (int d = 0; d < 3; d++) {
+      x[d] = __fadd_rn((float)(4 * sl[d]), fine_off(load_code(a.xp, 3 * p + d, g.izipx), g.izipx));
+      fi[d] = (int)floorf(x[d]) + 1;  // 0 .. 4B+1 inside the staged region
+      in = in && fi[d] >= 0 && fi[d] <= 4 * B[d] + 1;
     }
-  }
+    if (!in) return;
+    int slot = atomicAdd(&sm.nst, 1);
+    if (slot >= PP_CAP) return;
+    int f = fi[0] + F0 * (fi[1] + F1 * fi[2]);
+    int r = atomicAdd(&bins[f], 1);
+    pts[slot] = make_float4(x[0], x[1], x[2], __int_as_float((int)p));
+    kinfo[slot] = (unsigned)f | ((unsigned)r << 13);
+  });
   __syncthreads();
   const int nst = sm.nst;
   if (nst > PP_CAP) return false;
