@@ -374,15 +374,18 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
 }
 
 // Nearest float to the real t + lo, certified when every real within margin
-// of it rounds to the same float (a quarter ulp keeps clear of binade edges).
+// of it rounds to the same float: its distance from rr stays below half an ulp
+// (a quarter ulp when rr is a power of two, where the spacing below halves).
+// diff carries one FP32 rounding, covered by the 2^-20 inflation.
 __device__ __forceinline__ bool round_certified(float t, float lo, float margin, float* r) {
   float rr = __fadd_rn(t, lo);
   float diff = __fadd_rn(__fsub_rn(t, rr), lo);
-  unsigned int e = (__float_as_uint(rr) >> 23) & 0xffu;
+  unsigned int u = __float_as_uint(rr), e = (u >> 23) & 0xffu;
   *r = rr;
   if (e <= 25u || e == 0xffu) return false;
   float quarter_ulp = __uint_as_float((e - 25u) << 23);
-  return fabsf(diff) + margin < quarter_ulp;
+  float lim = (u & 0x7fffffu) == 0u ? quarter_ulp : 2.0f * quarter_ulp;
+  return fabsf(diff) * 1.000001f + margin < lim;
 }
 
 // nint(x) of the reference (halves away from zero) for every x within E of xf

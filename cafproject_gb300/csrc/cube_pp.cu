@@ -97,6 +97,14 @@ __device__ __forceinline__ void pair_force(const PPArgs& a, float rx, float ry, 
   acc[2] += to_fix(__fmul_rn(s, rz));
 }
 
+// vreal=vreal+f_tot*a_mid*dt/6/pi in FP64 and its code, for lanes whose fast
+// path was not certified (not inlined: keeps double conversions off the
+// common path)
+__device__ __noinline__ long long pp_kick_exact(CodecView cv, int code, float F, double kick) {
+  double v = __dadd_rn(codec_decode(cv, code), __dmul_rn((double)F, kick));
+  return codec_encode(cv, v);
+}
+
 // kick + exact velocity code of one particle; returns |F|^2
 __device__ __forceinline__ float pp_kick(const PPArgs& a, int64_t p, const long long* acc) {
   const Geo& g = a.g;
@@ -113,8 +121,7 @@ __device__ __forceinline__ float pp_kick(const PPArgs& a, int64_t p, const long 
     if (!a.exact_only && certify_abs(f2d_bits(vf) & 0x7fffffffffffffffLL, E, a.cv, &n)) {
       out = vf < 0.f ? -n : n;
     } else {
-      double v = __dadd_rn(codec_decode(a.cv, code), __dmul_rn((double)F[d], a.kick));
-      out = codec_encode(a.cv, v);
+      out = pp_kick_exact(a.cv, code, F[d], a.kick);
     }
     store_code(a.vp, 3 * p + d, g.izipv, out);
     if (a.fpp) a.fpp[3 * p + d] = F[d];

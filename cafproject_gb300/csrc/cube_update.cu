@@ -65,6 +65,27 @@ __device__ __forceinline__ int frame_code(const Geo& g, int l, int s) {
   return o == 0 ? 1 : (o > 0 ? 2 : 0);
 }
 
+// The reference's FP64 expressions, taken only by lanes whose fast path could
+// not be certified.  They are separate non-inlined functions so the compiler
+// cannot hoist their double conversions into the common path (GB300 runs
+// float<->double conversions on its narrow double-precision pipe).
+
+// ig=ceiling(xq+deltax) (update_particle.f90:66-70)
+__device__ __noinline__ int dest_exact(CodecView cv, int vcode, float vfd, float dt_mid, int Ls, float offf) {
+  double v = __dadd_rn(codec_decode(cv, vcode), (double)vfd);
+  double deltax = __dmul_rn(__dmul_rn((double)dt_mid, v), 0.25);
+  double xq = __dadd_rn((double)(Ls - 1), (double)offf);
+  return (int)ceil(__dadd_rn(xq, deltax));
+}
+// vfield_new=vfield_new+vreal rounded to real(4) (update_particle.f90:72)
+__device__ __noinline__ float accumulate_exact(CodecView cv, int vcode, float vfs, float acc) {
+  double v = __dadd_rn(codec_decode(cv, vcode), (double)vfs);
+  return __double2float_rn(__dadd_rn((double)acc, v));
+}
+// vfield_new/(rhoce+weight_v) rounded to real(4) (update_particle.f90:81-83)
+__device__ __noinline__ float quotient_exact(float acc, uint32_t cnt) {
+  return __double2float_rn(__ddiv_rn((double)acc, __dadd_rn((double)cnt, kWeightV)));
+}
 // U1: destination of every particle in every frame that sees it.
 __global__ void k_dest(UpdArgs a) {
   const Geo& g = a.g;
@@ -74,10 +95,11 @@ __global__ void k_dest(UpdArgs a) {
     int64_t cell = a.pcell[p];
     int gc[3];
     cell_coords(g, cell, gc[0], gc[1], gc[2]);
-    // per dim: up to two frames (offset o of the local coordinate) that land
-    int nval[3];
-    int oval[3][2], igv[3][2];
+    // per dim: up to two frames (offset o of the local coordinate) that land;
+    // scalars per (dim, slot) so nothing is indexed dynamically (no local memory)
+    int nval[3], oa[3], ob[3], ga[3], gb[3];
     bool far = false;
+#pragma unroll
     for (int d = 0; d < 3; d++) {
       int H, L;
       tile_local(g, gc[d], H, L);
@@ -92,6 +114,8 @@ __global__ void k_dest(UpdArgs a) {
       float Edx = 0.25f * (fabsf(a.dt_mid) * (fabsf(dh) + fabsf(vfa)) * 1.2e-7f + fabsf(Pf) * 6.0e-8f);
       float offf = __fmul_rn(pos_off_f(xcode, g.izipx), g.izipx == 1 ? 1.0f / 256.0f : 1.0f / 65536.0f);
       nval[d] = 0;
+      oa[d] = ob[d] = ga[d] = gb[d] = 0;
+#pragma unroll
       for (int f = 0; f < 3; f++) {
         int o = f == 0 ? 0 : (f == 1 ? g.nt : -g.nt);
         int Ls = L + o;
@@ -104,22 +128,22 @@ __global__ void k_dest(UpdArgs a) {
         if (clo == chi && !a.exact_only) {
           ig = (int)chi;
         } else {
-          // the reference's FP64 expression (update_particle.f90:66-70)
-          double v = __dadd_rn(codec_decode(a.cv, vcode), (double)vfd);
-          double deltax = __dmul_rn(__dmul_rn((double)a.dt_mid, v), 0.25);
-          double xq = __dadd_rn((double)(Ls - 1), (double)offf);
-          ig = (int)ceil(__dadd_rn(xq, deltax));
+          ig = dest_exact(a.cv, vcode, vfd, a.dt_mid, Ls, offf);
         }
         if (ig < 1 - 2 * g.ncb || ig > g.nt + 2 * g.ncb) {
           far = true;
           continue;
         }
         if (ig >= 1 && ig <= g.nt && nval[d] < 2) {
-          oval[d][nval[d]] = o;
-          igv[d][nval[d]] = ig;
+          if (nval[d] == 0) {
+            oa[d] = o;
+            ga[d] = ig;
+          } else {
+            ob[d] = o;
+            gb[d] = ig;
+          }
           nval[d]++;
-          int disp = abs(ig - Ls);
-          local_max = max(local_max, disp);
+          local_max = max(local_max, abs(ig - Ls));
         }
       }
     }
@@ -132,17 +156,23 @@ __global__ void k_dest(UpdArgs a) {
     }
     for (int k = 0; k < ncopy; k++) {
       int sel[3] = {k % nval[0], (k / nval[0]) % nval[1], k / (nval[0] * nval[1])};
-      int dg[3];
+      int dg[3], fr = 0;
+#pragma unroll
       for (int d = 0; d < 3; d++) {
         int H = (int)fdiv((uint32_t)gc[d], g.dnt);
+        int o = sel[d] ? ob[d] : oa[d];
+        int ig = sel[d] ? gb[d] : ga[d];
         // frame tile = H - o/nt (periodic in tiles); destination global coordinate
-        int fo = oval[d][sel[d]] == 0 ? 0 : (oval[d][sel[d]] > 0 ? 1 : -1);
+        int fo = o == 0 ? 0 : (o > 0 ? 1 : -1);
         int T = wrap1(H - fo, g.nnt);
-        dg[d] = glob(g, T, igv[d][sel[d]]);
+        dg[d] = glob(g, T, ig);
+      }
+#pragma unroll
+      for (int d = 2; d >= 0; d--) {
+        int o = sel[d] ? ob[d] : oa[d];
+        fr = 3 * fr + (o == 0 ? 1 : (o > 0 ? 2 : 0));
       }
       int32_t D = (int32_t)cell_id(g, dg[0], dg[1], dg[2]);
-      int fr = 0;
-      for (int d = 2; d >= 0; d--) fr = 3 * fr + (oval[d][sel[d]] == 0 ? 1 : (oval[d][sel[d]] > 0 ? 2 : 0));
       if (k == 0) {
         a.dest[p] = D;
         a.dframe[p] = (uint8_t)fr;
@@ -173,8 +203,7 @@ __device__ __forceinline__ float accumulate_v(const UpdArgs& a, float acc, int64
                           (fabsf(acc) + fabsf(dd.x) + fabsf(vfs)) * 2.3e-16f);
   float r;
   if (!a.exact_only && round_certified(s2, lo, margin, &r)) return r;
-  double v = __dadd_rn(codec_decode(a.cv, vcode), (double)vfs);
-  return __double2float_rn(__dadd_rn((double)acc, v));
+  return accumulate_exact(a.cv, vcode, vfs, acc);
 }
 
 // vfield_new/(rhoce+weight_v) (update_particle.f90:81-83): the denominator
@@ -189,7 +218,7 @@ __device__ __forceinline__ float vfield_quotient(float acc, uint32_t cnt, int ex
   float margin = 1.25f * (fabsf(lo) * 3.6e-7f + fabsf(q1) * (fabsf(dlo / dhi) * fabsf(dlo / dhi) + 2.3e-16f));
   float r;
   if (!exact_only && cnt < (1u << 24) && round_certified(q1, lo, margin, &r)) return r;
-  return __double2float_rn(__ddiv_rn((double)acc, __dadd_rn((double)cnt, kWeightV)));
+  return quotient_exact(acc, cnt);
 }
 
 // U2: one thread per destination cell walks the sources in visit order.
