@@ -156,7 +156,9 @@ def algorithmic_bytes(p, n):
     cell = 4 + 4  # rhoc + cell start (int32 index, int32 count)
     return {
         "update_dest": n * (s + 4) + n * 5,                 # read x,v,cell; write dest+frame
-        "update_rank": n * (5 + 3 * p.izipv) + nc3 * (cell + 12 + 4 + 12),
+        # counting rank path: local ranks + 27 uint16 counts per cell, then base ranks in place
+        "update_rank": n * (4 + 1 + 2) + nc3 * (8 + 3 * 54 + 4),
+        "update_place": n * (4 + 4 + 1 + 2 + 2 + 8 + 4 + 4) + n * (4 + 4 + 3 * p.izipv + 12) + nc3 * (4 + 8 + 12 + 12),
         "update_scan": nc3 * (4 + 8),
         "update_scatter": n * (s + 4 + 4 + 4 + 5) + n * (s + 4 + 4),
         "update_sigma": n * (3 * p.izipv + 4) + nc3 * 12,

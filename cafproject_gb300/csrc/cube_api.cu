@@ -47,7 +47,7 @@ static void release(cube_ctx* c) {
   cube_timers_free(c);
   void* bufs[] = {c->xp[0], c->xp[1], c->vp[0], c->vp[1], c->pid[0], c->pid[1], c->pcell[0], c->pcell[1],
                   c->rhoc[0], c->rhoc[1],
-                  c->vfield[0], c->vfield[1], c->cstart[0], c->cstart[1], c->dest, c->dframe, c->rank, c->xtra,
+                  c->vfield[0], c->vfield[1], c->cstart[0], c->cstart[1], c->dest, c->dframe, c->doff, c->lrank, c->offc, c->perm, c->rank, c->xtra,
                   c->scan_tmp, c->red_tmp, c->tan_tab, c->codec[0].dec, c->codec[1].dec, c->codec[0].bnd, c->codec[1].bnd, c->codec[0].dech, c->codec[1].dech, c->rho_f, c->force_f[0],
                   c->force_f[1], c->force_f[2], c->kern_f, c->kern_f_raw, c->rho_c, c->force_c[0],
                   c->force_c[1], c->force_c[2], c->kern_c, c->fpp, c->pp_ovf_brick, c->pp_ovf_cell, c->pp_novf, c->dstats,
@@ -135,6 +135,10 @@ extern "C" int cube_create(const cube_params* p, const float* fine_table, const 
   }
   ALLOC(c->dest, 4 * np);
   ALLOC(c->dframe, np);
+  ALLOC(c->doff, np);
+  ALLOC(c->lrank, 2 * np);
+  ALLOC(c->offc, 2 * 27 * c->ncells);
+  ALLOC(c->perm, 4 * np);
   ALLOC(c->rank, 4 * np);
   c->xtra_cap = 1 << 20;
   ALLOC(c->xtra, sizeof(int4) * c->xtra_cap);
@@ -289,6 +293,9 @@ extern "C" int cube_set_option(cube_ctx* c, int option, int64_t value) {
   switch (option) {
     case CUBE_OPT_EXACT_KICKS:
       c->opt_exact_kicks = value ? 1 : 0;
+      return CUBE_OK;
+    case CUBE_OPT_RANK_WALK:
+      c->opt_rank_walk = value ? 1 : 0;
       return CUBE_OK;
     case CUBE_OPT_PP_LEVEL:
       if (value < 0 || value > 2) return cube_fail(c, CUBE_ERR_ARG, "PP level must be 0, 1 or 2");

@@ -66,6 +66,10 @@ struct cube_ctx {
   // update_x scratch
   int32_t* dest = nullptr;      // primary destination cell per particle (-1: none)
   uint8_t* dframe = nullptr;    // frame of the primary copy: (ox+1)+3(oy+1)+9(oz+1), o in tiles
+  uint8_t* doff = nullptr;      // cell offset source-destination of the primary copy, (dx+1)+3(dy+1)+9(dz+1); 255 if |d|>1
+  uint16_t* lrank = nullptr;    // rank among the particles of one source cell bound for one destination
+  uint16_t* offc = nullptr;     // 27 per source cell: counts bound for each neighbour, then their base ranks
+  int32_t* perm = nullptr;      // new position -> old particle index
   uint32_t* rank = nullptr;     // rank of the primary copy in its destination
   int4* xtra = nullptr;         // extra copies: (particle, dest cell, rank, -)
   int64_t xtra_cap = 0;
@@ -86,6 +90,8 @@ struct cube_ctx {
   float vmax_prev[3] = {0.f, 0.f, 0.f};  // last coarse-kick vmax (0: unknown)
   unsigned long long kick_exact_lanes = 0;
   int opt_exact_kicks = 0;
+  int opt_rank_walk = 0;   // force the general visit-order rank walker
+  int rank_walked = 0;     // the last update used the walker
   int opt_pp_level = 0;  // first PP level (0 bricks, 1 single cells, 2 global memory)
   // fine PM
   cufftHandle plan_f_r2c = 0, plan_f_c2r = 0;
@@ -527,7 +533,7 @@ int cube_stats_fetch(cube_ctx* c);
 enum {
   PH_UPD_DEST = 0, PH_UPD_RANK, PH_UPD_SCAN, PH_UPD_SCATTER, PH_UPD_SIGMA, PH_PP,
   PH_F_DEPOSIT, PH_F_R2C, PH_F_GREEN, PH_F_C2R, PH_F_F2MAX, PH_F_KICK,
-  PH_C_DEPOSIT, PH_C_FFT, PH_C_KICK
+  PH_C_DEPOSIT, PH_C_FFT, PH_C_KICK, PH_UPD_PLACE
 };
 void cube_phase_begin(cube_ctx* c, int phase);
 void cube_phase_end(cube_ctx* c, int phase);

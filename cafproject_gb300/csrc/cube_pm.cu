@@ -199,18 +199,26 @@ __global__ void k_green3(const float2* __restrict__ rk, const float* __restrict_
   }
 }
 
-// maxval(sum(force**2,1)) over the mesh (pm.f90:126, 315)
+// maxval(sum(force**2,1)) over the mesh (pm.f90:126, 315): one block per row
+// (y, z) at a time, float2 loads along x (rows start 8-byte aligned: stride n+2)
+__device__ __forceinline__ float f2sum(float a, float b, float c) {
+  return __fadd_rn(__fadd_rn(__fmul_rn(a, a), __fmul_rn(b, b)), __fmul_rn(c, c));
+}
 __global__ void k_f2max(const float* __restrict__ f0, const float* __restrict__ f1, const float* __restrict__ f2,
                         int n, unsigned int* __restrict__ out) {
-  int64_t rows = (int64_t)n * n;
+  const int64_t rows = (int64_t)n * n;
+  const int h = n >> 1;
   float m = 0.f;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rows * n; i += (int64_t)gridDim.x * blockDim.x) {
-    int64_t r = i / n;
-    int x = (int)(i - r * n);
-    int64_t j = r * (n + 2) + x;
-    float a = f0[j], b = f1[j], c = f2[j];
-    float s = __fadd_rn(__fadd_rn(__fmul_rn(a, a), __fmul_rn(b, b)), __fmul_rn(c, c));
-    m = fmaxf(m, s);
+  for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
+    const int64_t o = r * (n + 2);
+    const float2* a = reinterpret_cast<const float2*>(f0 + o);
+    const float2* b = reinterpret_cast<const float2*>(f1 + o);
+    const float2* c = reinterpret_cast<const float2*>(f2 + o);
+    for (int x = threadIdx.x; x < h; x += blockDim.x) {
+      float2 u = __ldg(a + x), v = __ldg(b + x), w = __ldg(c + x);
+      m = fmaxf(m, fmaxf(f2sum(u.x, v.x, w.x), f2sum(u.y, v.y, w.y)));
+    }
+    if ((n & 1) && threadIdx.x == 0) m = fmaxf(m, f2sum(f0[o + n - 1], f1[o + n - 1], f2[o + n - 1]));
   }
   for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) atomic_max_pos(out, m);
@@ -503,7 +511,7 @@ int cube_fine_forces_impl(cube_ctx* c, cube_stats* st) {
     CUBE_FFT(c, cufftExecC2R(c->plan_f_c2r, (cufftComplex*)c->force_f[d], c->force_f[d]));
   cube_phase_end(c, PH_F_C2R);
   cube_phase_begin(c, PH_F_F2MAX);
-  k_f2max<<<cube_grid(c->nfine, 256), 256, 0, s>>>(c->force_f[0], c->force_f[1], c->force_f[2], c->nf,
+  k_f2max<<<cube_grid((int64_t)c->nf * c->nf, 1, 8), 256, 0, s>>>(c->force_f[0], c->force_f[1], c->force_f[2], c->nf,
                                                    &c->dstats->f2_fine_bits);
   cube_phase_end(c, PH_F_F2MAX);
   CUBE_CUDA(c, cudaGetLastError());
@@ -573,7 +581,7 @@ int cube_coarse_forces_impl(cube_ctx* c, cube_stats* st) {
                                                   (float2*)c->force_c[1], (float2*)c->force_c[2]);
   for (int d = 0; d < 3; d++)
     CUBE_FFT(c, cufftExecC2R(c->plan_c_c2r, (cufftComplex*)c->force_c[d], c->force_c[d]));
-  k_f2max<<<cube_grid((int64_t)nc * nc * nc, 256), 256, 0, s>>>(c->force_c[0], c->force_c[1], c->force_c[2], nc,
+  k_f2max<<<cube_grid((int64_t)nc * nc, 1, 8), 256, 0, s>>>(c->force_c[0], c->force_c[1], c->force_c[2], nc,
                                                                  &c->dstats->f2_coarse_bits);
   cube_phase_end(c, PH_C_FFT);
   CUBE_CUDA(c, cudaGetLastError());

@@ -12,7 +12,7 @@
 static const char* kPhaseNames[CUBE_NPHASE] = {
     "update_dest", "update_rank", "update_scan", "update_scatter", "update_sigma", "pp_force",
     "fine_deposit", "fine_r2c", "fine_green", "fine_c2r", "fine_f2max", "fine_kick",
-    "coarse_deposit", "coarse_fft", "coarse_kick"};
+    "coarse_deposit", "coarse_fft", "coarse_kick", "update_place"};
 
 struct TimerPair {
   cudaEvent_t a, b;

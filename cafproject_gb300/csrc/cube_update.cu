@@ -38,6 +38,10 @@ struct UpdArgs {
   int exact_only;     // skip every certified fast path (FP64 expressions only)
   int32_t* dest;
   uint8_t* dframe;
+  uint8_t* doff;
+  uint16_t* lrank;
+  uint16_t* offc;
+  int32_t* perm;
   uint32_t* rank;
   int4* xtra;
   int64_t xtra_cap;
@@ -176,6 +180,19 @@ __global__ void k_dest(UpdArgs a) {
       if (k == 0) {
         a.dest[p] = D;
         a.dframe[p] = (uint8_t)fr;
+        // offset of the source from the destination in the destination's frame
+        int oc = 0;
+        bool near = true;
+#pragma unroll
+        for (int d = 2; d >= 0; d--) {
+          int H, L;
+          tile_local(g, gc[d], H, L);
+          int o = sel[d] ? ob[d] : oa[d], ig = sel[d] ? gb[d] : ga[d];
+          int off = L + o - ig;
+          near = near && off >= -1 && off <= 1;
+          oc = 3 * oc + (off + 1);
+        }
+        a.doff[p] = near ? (uint8_t)oc : (uint8_t)255;
       } else {
         unsigned long long slot = atomicAdd(&a.st->ndup_list, 1ull);
         if ((int64_t)slot < a.xtra_cap) a.xtra[slot] = make_int4((int)p, D, -1, fr);
@@ -219,6 +236,159 @@ __device__ __forceinline__ float vfield_quotient(float acc, uint32_t cnt, int ex
   float r;
   if (!exact_only && cnt < (1u << 24) && round_certified(q1, lo, margin, &r)) return r;
   return quotient_exact(acc, cnt);
+}
+
+// U2 fast path, valid when every particle moved at most one cell and none
+// landed in two frames (the usual step).  The rank of particle p in its
+// destination D is the number of particles reaching D from the source cells
+// D visits before p's cell, plus p's rank among the particles of its own cell
+// bound for D.  Steps: per source cell, local ranks and 27 counts (one per
+// neighbour it feeds); per destination, the counts in visit order turned into
+// base ranks in place; after the scan, rank = base + local rank and the
+// inverse permutation; per destination, vfield_new summed in rank order, i.e.
+// the reference's visit order.
+constexpr int NOFF = 27;
+constexpr int RL_T = 256;
+
+// one warp per source cell: its particles in chunks of 32 lanes; lanes bound
+// for the same neighbour are grouped with a match, their order inside the
+// group is their lane order (= storage order), and the group leader advances
+// that neighbour's running count (held by lane o of the warp's counters)
+__global__ void __launch_bounds__(RL_T) k_rank_local(UpdArgs a) {
+  __shared__ uint32_t cnt[RL_T / 32][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (a.st->max_disp > 1 || a.st->ndup_list != 0) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&a.st->flags, 8);  // not eligible
+    return;
+  }
+  const unsigned lt = (1u << lane) - 1u;
+  const int64_t nw = (int64_t)gridDim.x * (RL_T / 32);
+  for (int64_t S = (int64_t)blockIdx.x * (RL_T / 32) + w; S < a.ncells; S += nw) {
+    cnt[w][lane] = 0u;
+    __syncwarp();
+    const int64_t p0 = a.cstart[S], p1 = a.cstart[S + 1];
+    for (int64_t q = p0; q < p1; q += 32) {
+      const int64_t p = q + lane;
+      int o = 255;
+      if (p < p1 && a.dest[p] >= 0) {
+        o = a.doff[p];
+        if (o >= NOFF) atomicOr(&a.st->flags, 4);  // moved farther than one cell
+      }
+      const unsigned m = __match_any_sync(0xffffffffu, o);
+      const bool mine = o < NOFF;
+      uint32_t c = mine ? cnt[w][o] + (uint32_t)__popc(m & lt) : 0u;
+      if (mine) {
+        if (c > 0xffffu) atomicOr(&a.st->flags, 4);
+        a.lrank[p] = (uint16_t)c;
+      }
+      __syncwarp();
+      if (mine && (m & lt) == 0u) cnt[w][o] += (uint32_t)__popc(m);
+      __syncwarp();
+    }
+    if (lane < NOFF) {
+      uint32_t c = cnt[w][lane];
+      if (c > 0xffffu) atomicOr(&a.st->flags, 4);
+      a.offc[S * NOFF + lane] = (uint16_t)c;
+    }
+    __syncwarp();
+  }
+}
+
+// one thread per destination: the 27 counts it owns, read together, turned
+// into base ranks in the destination's visit order, written back in place
+__global__ void k_rank_base(UpdArgs a) {
+  const Geo& g = a.g;
+  if (a.st->flags & 12) return;
+  for (int64_t D = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; D < a.ncells;
+       D += (int64_t)gridDim.x * blockDim.x) {
+    int dgc[3], T[3], Dl[3];
+    cell_coords(g, D, dgc[0], dgc[1], dgc[2]);
+#pragma unroll
+    for (int d = 0; d < 3; d++) tile_local(g, dgc[d], T[d], Dl[d]);
+    // source cells and their count of particles bound for D, in (dz, dy, dx) order
+    uint32_t sid[NOFF];
+    uint16_t c[NOFF];
+#pragma unroll
+    for (int dz = -1; dz <= 1; dz++) {
+      int sz = glob(g, T[2], Dl[2] + dz);
+#pragma unroll
+      for (int dy = -1; dy <= 1; dy++) {
+        int sy = glob(g, T[1], Dl[1] + dy);
+#pragma unroll
+        for (int dx = -1; dx <= 1; dx++) {
+          const int o = (dx + 1) + 3 * (dy + 1) + 9 * (dz + 1);
+          sid[o] = (uint32_t)cell_id(g, glob(g, T[0], Dl[0] + dx), sy, sz);
+          c[o] = a.offc[(int64_t)sid[o] * NOFF + o];
+        }
+      }
+    }
+    // the three source z-slabs in visit order: by (layer, k), layer=(k+ncb-1) mod nlayer
+    int key[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      int kl = Dl[2] + i - 1;
+      key[i] = ((kl + g.ncb - 1) % a.nlayer) * 4096 + kl + 8;
+    }
+    int zo[3] = {0, 1, 2};  // slab index dz+1
+    if (key[1] < key[0]) { int t = key[0]; key[0] = key[1]; key[1] = t; t = zo[0]; zo[0] = zo[1]; zo[1] = t; }
+    if (key[2] < key[1]) { int t = key[1]; key[1] = key[2]; key[2] = t; t = zo[1]; zo[1] = zo[2]; zo[2] = t; }
+    if (key[1] < key[0]) { int t = key[0]; key[0] = key[1]; key[1] = t; t = zo[0]; zo[0] = zo[1]; zo[1] = t; }
+    uint32_t base = 0, bz[3];
+    uint32_t sum[3];
+#pragma unroll
+    for (int z = 0; z < 3; z++) {
+      uint32_t s = 0;
+#pragma unroll
+      for (int k = 0; k < 9; k++) s += c[9 * z + k];
+      sum[z] = s;
+    }
+    for (int i = 0; i < 3; i++) {
+      bz[zo[i]] = base;
+      base += sum[zo[i]];
+    }
+    if (base > 0xffffu) atomicOr(&a.st->flags, 4);
+#pragma unroll
+    for (int z = 0; z < 3; z++) {
+      uint32_t b = bz[z];
+#pragma unroll
+      for (int k = 0; k < 9; k++) {
+        const int o = 9 * z + k;
+        a.offc[(int64_t)sid[o] * NOFF + o] = (uint16_t)b;
+        b += c[o];
+      }
+    }
+    a.cnt_new[D] = (int32_t)base;
+  }
+}
+
+__global__ void k_rank_place(UpdArgs a) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.np; p += (int64_t)gridDim.x * blockDim.x) {
+    int32_t D = a.dest[p];
+    if (D < 0) continue;
+    uint32_t r = (uint32_t)a.offc[(int64_t)a.pcell[p] * NOFF + a.doff[p]] + a.lrank[p];
+    a.rank[p] = r;
+    if (r < (uint32_t)a.cnt_new[D]) a.perm[a.cstart_new[D] + r] = (int32_t)p;
+    else atomicOr(&a.st->flags, 2);
+  }
+}
+
+__global__ void k_vfield_new(UpdArgs a) {
+  for (int64_t D = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; D < a.ncells;
+       D += (int64_t)gridDim.x * blockDim.x) {
+    float acc[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) acc[d] = __fmul_rn(a.vfield[3 * D + d], 0.1f);  // vfield*weight_v
+    const uint32_t cnt = (uint32_t)a.cnt_new[D];
+    const int64_t i0 = a.cstart_new[D];
+    for (uint32_t i = 0; i < cnt; i++) {
+      int64_t p = a.perm[i0 + i];
+      int64_t S = a.pcell[p];
+#pragma unroll
+      for (int d = 0; d < 3; d++) acc[d] = accumulate_v(a, acc[d], p, d, S);
+    }
+#pragma unroll
+    for (int d = 0; d < 3; d++) a.vfield_new[3 * D + d] = vfield_quotient(acc[d], cnt, a.exact_only);
+  }
 }
 
 // U2: one thread per destination cell walks the sources in visit order.
@@ -448,6 +618,10 @@ int cube_update_x_impl(cube_ctx* c, float dt_old, float dt, float vz_max, cube_s
   a.exact_only = c->opt_exact_kicks;
   a.dest = c->dest;
   a.dframe = c->dframe;
+  a.doff = c->doff;
+  a.lrank = c->lrank;
+  a.offc = c->offc;
+  a.perm = c->perm;
   a.rank = c->rank;
   a.xtra = c->xtra;
   a.xtra_cap = c->xtra_cap;
@@ -464,8 +638,16 @@ int cube_update_x_impl(cube_ctx* c, float dt_old, float dt, float vz_max, cube_s
   cube_phase_begin(c, PH_UPD_DEST);
   k_dest<<<cube_grid(c->np, B), B, 0, c->stream>>>(a);
   cube_phase_end(c, PH_UPD_DEST);
+  // ranks: the counting path (kernels check their own eligibility on the
+  // device and flag it), else the general visit-order walker
+  bool walker = c->opt_rank_walk != 0;
   cube_phase_begin(c, PH_UPD_RANK);
-  k_rank<<<cube_grid(c->ncells, 128, 32), 128, 0, c->stream>>>(a);
+  if (walker) {
+    k_rank<<<cube_grid(c->ncells, 128, 32), 128, 0, c->stream>>>(a);
+  } else {
+    k_rank_local<<<cube_grid(c->ncells, RL_T / 32, 8), RL_T, 0, c->stream>>>(a);
+    k_rank_base<<<cube_grid(c->ncells, 256), 256, 0, c->stream>>>(a);
+  }
   cube_phase_end(c, PH_UPD_RANK);
   CUBE_CUDA(c, cudaGetLastError());
   cube_phase_begin(c, PH_UPD_SCAN);
@@ -476,11 +658,32 @@ int cube_update_x_impl(cube_ctx* c, float dt_old, float dt, float vz_max, cube_s
   CUBE_CUDA(c, cudaMemcpyAsync(&np_new, c->cstart[kn] + c->ncells, 8, cudaMemcpyDeviceToHost, c->stream));
   r = cube_stats_fetch(c);
   if (r) return r;
+  if (c->hstats->flags & 1) return cube_fail(c, CUBE_ERR_DISPLACEMENT, "a particle left the double-buffer tile");
+  if (!walker && (c->hstats->flags & 12)) {  // counting path not applicable: walk
+    walker = true;
+    CUBE_CUDA(c, cudaMemsetAsync(&c->dstats->flags, 0, sizeof(int), c->stream));
+    cube_phase_begin(c, PH_UPD_RANK);
+    k_rank<<<cube_grid(c->ncells, 128, 32), 128, 0, c->stream>>>(a);
+    cube_phase_end(c, PH_UPD_RANK);
+    CUBE_CUDA(c, cudaGetLastError());
+    r = cube_scan_counts(c, c->rhoc[kn], c->cstart[kn], c->ncells);
+    if (r) return r;
+    CUBE_CUDA(c, cudaMemcpyAsync(&np_new, c->cstart[kn] + c->ncells, 8, cudaMemcpyDeviceToHost, c->stream));
+    r = cube_stats_fetch(c);
+    if (r) return r;
+  }
+  c->rank_walked = walker ? 1 : 0;
   DevStats hs = *c->hstats;
-  if (hs.flags & 1) return cube_fail(c, CUBE_ERR_DISPLACEMENT, "a particle left the double-buffer tile");
   if ((int64_t)hs.ndup_list > c->xtra_cap) return cube_fail(c, CUBE_ERR_TILE_OVERFLOW, "extra-copy list overflow");
   if (np_new > c->p.np_max)
     return cube_fail(c, CUBE_ERR_IMAGE_OVERFLOW, "new particle count exceeds np_max");
+  if (!walker) {
+    cube_phase_begin(c, PH_UPD_PLACE);
+    k_rank_place<<<cube_grid(c->np, B), B, 0, c->stream>>>(a);
+    k_vfield_new<<<cube_grid(c->ncells, 128, 32), 128, 0, c->stream>>>(a);
+    cube_phase_end(c, PH_UPD_PLACE);
+    CUBE_CUDA(c, cudaGetLastError());
+  }
   cube_phase_begin(c, PH_UPD_SCATTER);
   k_scatter<<<cube_grid(c->np, B), B, 0, c->stream>>>(a);
   if (hs.ndup_list) k_scatter_xtra<<<cube_grid((int64_t)hs.ndup_list, B), B, 0, c->stream>>>(a);
@@ -519,6 +722,7 @@ int cube_update_x_impl(cube_ctx* c, float dt_old, float dt, float vz_max, cube_s
     st->sigma_vi_new = c->sigma_vi_new;
     st->nlayer = nlayer;
     st->max_disp = hs.max_disp;
+    st->rank_walked = c->rank_walked;
   }
   return CUBE_OK;
 }

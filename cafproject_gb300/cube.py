@@ -35,7 +35,8 @@ EXPORTS = ["cube_create", "cube_destroy", "cube_last_error", "cube_upload_state"
 CODEC_STATIC_MAX = 16384
 OPT_EXACT_KICKS = 1
 OPT_PP_LEVEL = 2
-NPHASE = 15
+OPT_RANK_WALK = 3
+NPHASE = 16
 
 
 class CubeError(RuntimeError):
@@ -50,7 +51,7 @@ class CubeStats(ctypes.Structure):
     _fields_ = [("nplocal", ctypes.c_int64), ("max_tile_np", ctypes.c_int64), ("nlost", ctypes.c_int64),
                 ("ndup", ctypes.c_int64), ("sum_c", ctypes.c_double), ("sum_r", ctypes.c_double),
                 ("sum_s", ctypes.c_double), ("sigma_vi_new", ctypes.c_float), ("nlayer", ctypes.c_int32),
-                ("max_disp", ctypes.c_int32), ("pad0", ctypes.c_int32), ("f2_max_pp", ctypes.c_float),
+                ("max_disp", ctypes.c_int32), ("rank_walked", ctypes.c_int32), ("f2_max_pp", ctypes.c_float),
                 ("pp_dense_bricks", ctypes.c_int32), ("npairs", ctypes.c_int64), ("itest1", ctypes.c_int64),
                 ("f2_max_fine", ctypes.c_float), ("f2_max_coarse", ctypes.c_float),
                 ("vmax", ctypes.c_float * 3), ("pad2", ctypes.c_int32), ("testrhof", ctypes.c_double),

@@ -75,7 +75,7 @@ typedef struct cube_stats {
   float sigma_vi_new;     /* std_vsim_res/sqrt(3.) */
   int32_t nlayer;         /* layer count used for the visit order */
   int32_t max_disp;       /* largest cell displacement seen */
-  int32_t pad0;
+  int32_t rank_walked;    /* 1: ranks came from the general walker, 0: counting path */
   /* cube_pp_force (ext_pp_force.f90:10-162) */
   float f2_max_pp;
   int32_t pp_dense_bricks; /* bricks redone cell by cell (too dense to stage) */
@@ -169,7 +169,7 @@ int cube_synchronize(cube_ctx* ctx);
    e.g. pm.f90:35-411): enable=1 resets and starts event pairs around every
    phase on the context's stream, enable=0 stops; cube_timing_read harvests
    the accumulated milliseconds and launch counts per phase. */
-#define CUBE_NPHASE 15
+#define CUBE_NPHASE 16
 int cube_timing(cube_ctx* ctx, int enable);
 int cube_timing_read(cube_ctx* ctx, double* ms, int64_t* count, int nphase);
 const char* cube_phase_name(int phase);
@@ -184,8 +184,10 @@ void* cube_stream(cube_ctx* ctx);
    1: single cells staged; 2: global memory, one CTA per cell), which
    otherwise serve only regions too dense for the level before.  The pair sums
    are order-independent, so every level gives bitwise the same result; used
-   to test the dense-region paths. */
-enum cube_option { CUBE_OPT_EXACT_KICKS = 1, CUBE_OPT_PP_LEVEL = 2 };
+   to test the dense-region paths.  CUBE_OPT_RANK_WALK=3 makes cube_update_x
+   use its general visit-order walker for the ranks instead of the counting
+   path it takes when every particle moved at most one cell (same result). */
+enum cube_option { CUBE_OPT_EXACT_KICKS = 1, CUBE_OPT_PP_LEVEL = 2, CUBE_OPT_RANK_WALK = 3 };
 int cube_set_option(cube_ctx* ctx, int option, int64_t value);
 
 /* Velocity-code self check: encodes n host doubles with sigma both by the

@@ -78,6 +78,32 @@ def test_update_x_bitexact(name, pk, sk, dt):
     g.close()
 
 
+@pytest.mark.parametrize("name,pk,sk", CASES, ids=[c[0] for c in CASES])
+@pytest.mark.parametrize("dt", [20.0, 40.0])
+def test_update_rank_paths_agree_bitwise(name, pk, sk, dt):
+    # counting path (every particle moved at most one cell) against the
+    # general visit-order walker: identical state and statistics
+    p = _params(pk)
+    st = synth.random_state(p, **sk)
+    outs = []
+    for walk in (0, 1):
+        g = C.CubeGPU(p)
+        g.upload(st["xp"], st["vp"], st["pid"], st["rhoc"], st["vfield"])
+        g.set_sigma(st["sigma_vi"], st["sigma_vi"])
+        g.set_option(C.OPT_RANK_WALK, walk)
+        s = g.update_x(np.float32(dt * 0.7), np.float32(dt), st["vz_max"])
+        outs.append((s, g.download()))
+        g.close()
+    (sa, da), (sb, db) = outs
+    assert sb["rank_walked"] == 1
+    if sa["max_disp"] <= 1 and sa["ndup"] == 0:
+        assert sa["rank_walked"] == 0
+    for k in ("xp", "vp", "pid", "rhoc"):
+        np.testing.assert_array_equal(da[k], db[k])
+    np.testing.assert_array_equal(da["vfield"].view(np.uint32), db["vfield"].view(np.uint32))
+    assert sa["sum_r"] == sb["sum_r"] and sa["nplocal"] == sb["nplocal"]
+
+
 def test_upload_download_roundtrip():
     p = _params(dict(nc=24, nnt=2))
     st = synth.random_state(p, seed=7)
