@@ -146,6 +146,21 @@ class ClockSampler:
 # ------------------------------------------------------------------ gb300 arm
 
 
+# DRAM bytes (read + write) per particle of one launch, from the full ncu
+# capture of the 256^3 workload (profiles/step_kernels_cdm256.md); meshes and
+# particle counts scale together between 256^3 and 512^3, so per-particle
+# traffic carries over
+TRAFFIC_PER_PARTICLE = {
+    "pp_force": (178.7e6 + 53.3e6) / 16778347,
+    "fine_kick": (2033.7e6 + 100.3e6) / 16778347,
+    "fine_deposit": (84.1e6 + 480.1e6) / 16778347,
+    "update_dest": (243.8e6 + 65.9e6) / 16778347,
+    "update_scatter": (503.1e6 + 255.5e6) / 16778347,
+    "fine_green": (1347.6e6 + 1568.0e6) / 16778347,
+    "fine_f2max": (1617.4e6 + 4.0e6) / 16778347,
+}
+
+
 def algorithmic_bytes(p, n):
     """Algorithmic bytes per launch of each phase (each array element read or
     written once; s = 3*izipx+3*izipv bytes of particle code)."""
@@ -267,7 +282,9 @@ def run_gb300(args, ws, rank, lrank):
         d = phases[dom]
         roof = {"kernel": dom, "bound": "hbm", "achieved": d["achieved_gbs"], "peak": hbm, "unit": "GB/s",
                 "frac": round(d["achieved_gbs"] / hbm, 4), "peak_source": peak_src,
-                "traffic": None, "algo_bytes_per_launch": d["algo_bytes"]}
+                "traffic": (round(TRAFFIC_PER_PARTICLE[dom] * n0) if dom in TRAFFIC_PER_PARTICLE else None),
+                "traffic_source": "ncu capture at 256^3 scaled per particle" if dom in TRAFFIC_PER_PARTICLE else None,
+                "algo_bytes_per_launch": d["algo_bytes"]}
 
     # e2e: host arrays in, host arrays out, every step
     ke = args.e2e_steps or max(1, min(args.steps, 3))
