@@ -90,11 +90,14 @@ struct DepArgs {
   float mass;
   float* rho;                 // padded periodic mesh, row stride n+2
   unsigned long long* total;  // sum of all owned cells in fixed point (exact)
+  int ng;                     // power-spectrum mesh (kPk only)
 };
 
 constexpr double kFixScale = 4294967296.0;  // 2^32
 
-template <int MPC, int BX, int BY, int BZ, int LO, int HI>
+// kPk: the power-spectrum deposit of cicpower.f90:100-133 (position
+// (cell + frac)*ng/nc - 0.5 in real(4), global frame) instead of the PM ones
+template <int MPC, int BX, int BY, int BZ, int LO, int HI, bool kPk = false>
 __global__ void __launch_bounds__(256) k_deposit_det(DepArgs a) {
   constexpr int SX = BX + LO + HI, SY = BY + LO + HI, SZ = BZ + LO + HI;
   constexpr int NSRC = SX * SY * SZ;
@@ -104,7 +107,7 @@ __global__ void __launch_bounds__(256) k_deposit_det(DepArgs a) {
   __shared__ long long sstart[NSRC];
   __shared__ unsigned long long btot;
   const Geo& g = a.g;
-  const int nc = g.nc, n = MPC == 1 ? g.nc : g.nf;
+  const int nc = g.nc, n = kPk ? a.ng : (MPC == 1 ? g.nc : g.nf);
   int nbx = (nc + BX - 1) / BX, nby = (nc + BY - 1) / BY;
   int b = blockIdx.x;
   int C0[3] = {(b % nbx) * BX, ((b / nbx) % nby) * BY, (b / (nbx * nby)) * BZ};
@@ -136,11 +139,21 @@ __global__ void __launch_bounds__(256) k_deposit_det(DepArgs a) {
       int gcd = wrap1(C0[d] + sl[d], nc), Tq, L;
       tile_local(g, gcd, Tq, L);
       int code = load_code(a.xp, 3 * p + d, g.izipx);
-      float tx = MPC == 1 ? coarse_tempx(L, code, g.izipx) : fine_tempx(MPC, L, code, g.izipx);
+      float tx;
+      if (kPk) {
+        float frac = __fmul_rn(pos_off_f(code, g.izipx), g.izipx == 1 ? 1.0f / 256.0f : 1.0f / 65536.0f);
+        // the particle's own global frame, as the reference rounds it
+        float pos = __fadd_rn((float)gcd, frac);
+        tx = __fsub_rn(__fdiv_rn(__fmul_rn(pos, (float)a.ng), (float)nc), 0.5f);
+      } else {
+        tx = MPC == 1 ? coarse_tempx(L, code, g.izipx) : fine_tempx(MPC, L, code, g.izipx);
+      }
       float fl = floorf(tx);
       d1[d] = __fsub_rn(__fadd_rn(fl, 1.0f), tx);
       d2[d] = __fsub_rn(1.0f, d1[d]);
-      rel[d] = MPC * sl[d] + (int)fl - MPC * (L - 1);  // mesh index relative to the brick
+      // mesh index relative to the brick
+      // (kPk: unwrap the ring cell's periodic image, then relative to the brick)
+      rel[d] = kPk ? (int)fl + MPC * (sl[d] - gcd) : MPC * sl[d] + (int)fl - MPC * (L - 1);
     }
 #pragma unroll
     for (int k = 0; k < 8; k++) {
@@ -174,12 +187,12 @@ __global__ void __launch_bounds__(256) k_deposit_det(DepArgs a) {
   if (threadIdx.x == 0 && a.total) atomicAdd(a.total, btot);
 }
 
-template <int MPC, int BX, int BY, int BZ, int LO, int HI>
+template <int MPC, int BX, int BY, int BZ, int LO, int HI, bool kPk = false>
 int launch_deposit(cube_ctx* c, const DepArgs& a) {
   int nc = c->p.nc;
   int nb = ((nc + BX - 1) / BX) * ((nc + BY - 1) / BY) * ((nc + BZ - 1) / BZ);
   size_t smem = sizeof(unsigned long long) * (MPC * BX) * (MPC * BY) * (MPC * BZ);
-  auto kern = k_deposit_det<MPC, BX, BY, BZ, LO, HI>;
+  auto kern = k_deposit_det<MPC, BX, BY, BZ, LO, HI, kPk>;
   CUBE_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   kern<<<nb, 256, smem, c->stream>>>(a);
   CUBE_CUDA(c, cudaGetLastError());
@@ -480,7 +493,7 @@ int cube_fine_density_impl(cube_ctx* c, cube_stats* st) {
   cudaStream_t s = c->stream;
   Geo g = make_geo(c);
   CUBE_CUDA(c, cudaMemsetAsync(c->dstats, 0, sizeof(DevStats), s));
-  DepArgs a{g, c->xp[c->cur], c->rhoc[c->cur], c->cstart[c->cur], c->p.mass_p, c->rho_f, &c->dstats->rhof_fix};
+  DepArgs a{g, c->xp[c->cur], c->rhoc[c->cur], c->cstart[c->cur], c->p.mass_p, c->rho_f, &c->dstats->rhof_fix, 0};
   cube_phase_begin(c, PH_F_DEPOSIT);
   int r = launch_deposit<4, 8, 4, 4, 1, 0>(c, a);
   cube_phase_end(c, PH_F_DEPOSIT);
@@ -550,12 +563,24 @@ int cube_fine_kick_impl(cube_ctx* c, float a_mid, float dt) {
   return CUBE_OK;
 }
 
+// CIC density of the particles on an ng^3 mesh (ng = nc, 2 nc or 4 nc) for the
+// power spectrum, mass 1 per particle (cicpower.f90:79,100-133), into the
+// padded mesh rho; *total receives the exact fixed-point sum.
+int cube_pk_deposit(cube_ctx* c, int ng, float* rho, unsigned long long* total) {
+  DepArgs a{make_geo(c), c->xp[c->cur], c->rhoc[c->cur], c->cstart[c->cur], 1.0f, rho, total, ng};
+  int nc = c->p.nc;
+  if (ng == nc) return launch_deposit<1, 8, 8, 8, 1, 1, true>(c, a);
+  if (ng == 2 * nc) return launch_deposit<2, 8, 8, 4, 1, 1, true>(c, a);
+  if (ng == 4 * nc) return launch_deposit<4, 8, 4, 4, 1, 1, true>(c, a);
+  return cube_fail(c, CUBE_ERR_ARG, "power-spectrum mesh must be nc, 2nc or 4nc per dimension");
+}
+
 // --------------------------------------------------------------- coarse
 int cube_coarse_density_impl(cube_ctx* c, cube_stats* st) {
   Geo g = make_geo(c);
   CUBE_CUDA(c, cudaMemsetAsync(&c->dstats->f2_coarse_bits, 0, 4, c->stream));
   CUBE_CUDA(c, cudaMemsetAsync(&c->dstats->rhoc_fix, 0, 8, c->stream));
-  DepArgs a{g, c->xp[c->cur], c->rhoc[c->cur], c->cstart[c->cur], c->p.mass_p, c->rho_c, &c->dstats->rhoc_fix};
+  DepArgs a{g, c->xp[c->cur], c->rhoc[c->cur], c->cstart[c->cur], c->p.mass_p, c->rho_c, &c->dstats->rhoc_fix, 0};
   cube_phase_begin(c, PH_C_DEPOSIT);
   int r = launch_deposit<1, 8, 8, 8, 1, 1>(c, a);
   cube_phase_end(c, PH_C_DEPOSIT);

@@ -31,7 +31,8 @@ EXPORTS = ["cube_create", "cube_destroy", "cube_last_error", "cube_upload_state"
            "cube_pm_fine_forces", "cube_pm_fine_kick",
            "cube_pm_coarse_forces", "cube_pm_coarse_kick", "cube_get_field", "cube_set_field", "cube_nplocal",
            "cube_synchronize", "cube_timing", "cube_timing_read", "cube_phase_name", "cube_stream",
-           "cube_codec_check", "cube_codec_check_static", "cube_arith_check", "cube_set_option"]
+           "cube_codec_check", "cube_codec_check_static", "cube_arith_check", "cube_pk_nbin",
+           "cube_power_spectrum", "cube_set_option"]
 CODEC_STATIC_MAX = 16384
 OPT_EXACT_KICKS = 1
 OPT_PP_LEVEL = 2
@@ -112,6 +113,8 @@ def load_library(path=None):
     L.cube_codec_check.argtypes = [P, F, P, I64, P, P]
     L.cube_codec_check_static.argtypes = [P, F, P, I64, P, P]
     L.cube_arith_check.argtypes = [P, P]
+    L.cube_pk_nbin.argtypes = [ctypes.c_int]
+    L.cube_power_spectrum.argtypes = [P, ctypes.c_int, F, P, P, ctypes.c_int]
     L.cube_set_option.argtypes = [P, ctypes.c_int, I64]
     _lib = L
     return L
@@ -274,6 +277,19 @@ class CubeGPU:
         b = np.empty(v.size, np.int32)
         self._check(self.L.cube_codec_check(self.h, float(sigma), _ptr(v), v.size, _ptr(a), _ptr(b)))
         return a, b
+
+    def power_spectrum(self, ng, box, delta2=None):
+        """xi(10, nbin) of cross_power (powerspectrum.f90) for the particles'
+        CIC density on an ng^3 mesh, as an (nbin, 10) array; delta2 (ng^3,
+        Fortran order) gives the cross power, None the auto power."""
+        nbin = int(self.L.cube_pk_nbin(int(ng)))
+        xi = np.zeros((nbin, 10), np.float64)
+        d2 = None
+        if delta2 is not None:
+            d2 = np.ascontiguousarray(np.asarray(delta2, np.float32).reshape(ng, ng, ng))
+        self._check(self.L.cube_power_spectrum(self.h, int(ng), float(box), _ptr(d2) if d2 is not None else None,
+                                               _ptr(xi), nbin))
+        return xi
 
     def arith_check(self):
         """Mismatches of the fast division by 6 and by pi_f against the IEEE

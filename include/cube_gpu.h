@@ -158,6 +158,18 @@ int cube_pm_fine_kick(cube_ctx* ctx, float a_mid, float dt);
 int cube_pm_coarse_forces(cube_ctx* ctx, cube_stats* st);
 int cube_pm_coarse_kick(cube_ctx* ctx, float a_mid, float dt, cube_stats* st);
 
+/* Power spectrum of the resident particles (cicpower.f90 + powerspectrum.f90
+   cross_power): CIC density on an ng^3 mesh (ng = nc, 2 nc or 4 nc; mass 1,
+   position (cell+frac)*ng/nc - 0.5), density contrast, R2C, linear bins
+   ibin = nint(|k|) for ibin = 1..nbin with nbin >= cube_pk_nbin(ng) =
+   nint(ng/2*sqrt(3)).  delta2: optional second density contrast (host,
+   ng^3 float, Fortran order) for the cross power; NULL gives the auto power.
+   xi receives xi(10, nbin) in the reference's meaning: modes, k (h/Mpc, box
+   in Mpc/h), Delta^2_11, Delta^2_22, Delta^2_12, <1/sinc^2>, <1/sinc^4>, r,
+   b, reconstructed power.  Uses the fine-mesh buffers as scratch. */
+int cube_pk_nbin(int ng);
+int cube_power_spectrum(cube_ctx* ctx, int ng, float box, const float* delta2, double* xi, int nbin);
+
 int cube_get_field(cube_ctx* ctx, int field, void* host);
 int cube_set_field(cube_ctx* ctx, int field, const void* host);
 

@@ -232,6 +232,14 @@ class OracleImage:
         L.orc_unbuffer(ctypes.byref(self.op), _p(self.brhoc), _p(self.bstart), _p(self.bxp), _p(self.bvp),
                        _p(self.bpid), _p(self.xp), _p(self.vp), _p(self.pid))
 
+    def buffer_v(self):
+        """buffer_v (buffer_particle.f90:5-25; main.f90:118): refresh the buffer
+        copies from the kicked physical particles.  PP and PM kick only the
+        physical particles of each tile; the next update_x reads the buffer
+        regions too."""
+        self._unbuffer()
+        self._buffer()
+
     def state(self):
         """Disjoint state (checkpoint layout) after the last call."""
         self._unbuffer()
@@ -412,6 +420,7 @@ class OracleImage:
             fields["rho_c"] = r3
             fields["force_c"] = fc
         self.fields = fields
+        self.buffer_v()
         return dict(f2_max_fine=f2f, f2_max_coarse=f2c, vmax=vmax, testrhof=testrhof, testrhoc=testrhoc)
 
 
@@ -472,3 +481,97 @@ def time_sample(params, state, sigma, a_mid, dt, dt_old, vz_max, tile=0, nthread
     est = nt3 * (t_upd + t_pp + t_fine) + t_buf + t_coarse
     return dict(t_update_tile=t_upd, t_pp_tile=t_pp, t_fine_tile=t_fine, t_buffer=t_buf, t_coarse=t_coarse,
                 step_estimate=est, sampled=t_upd + t_pp + t_fine + t_buf + t_coarse)
+
+
+def particle_cells(params, rhoc):
+    """Global coarse-cell coordinates (x, y, z) of every particle in storage
+    order: tile (x fastest), cell inside the tile (x fastest), rank
+    (update_particle.f90:132-142)."""
+    nt, nnt = params.nt, params.nnt
+    t = np.arange(nnt)
+    c = np.arange(nt)
+    # index order of rhoc(nt,nt,nt,nnt,nnt,nnt): i, j, k, itx, ity, itz (i fastest)
+    tz, ty, tx, k, j, i = np.meshgrid(t, t, t, c, c, c, indexing="ij")
+    gx = (tx * nt + i).ravel()
+    gy = (ty * nt + j).ravel()
+    gz = (tz * nt + k).ravel()
+    cnt = np.asarray(rhoc).ravel().astype(np.int64)
+    return np.stack([np.repeat(gx, cnt), np.repeat(gy, cnt), np.repeat(gz, cnt)], axis=1)
+
+
+def cic_density(params, xp, rhoc, ng):
+    """Density contrast of mass-1 particles deposited by CIC at
+    (cell + frac)*ng/nc - 0.5 in real(4) (cicpower.f90:100-133, 171-176);
+    an (ng, ng, ng) float32 array indexed [z, y, x], summed in float64."""
+    nc = params.nc
+    xres = np.float32(1.0 / 256.0) if params.izipx == 1 else np.float32(1.0 / 65536.0)
+    mask = (1 << (8 * params.izipx)) - 1
+    gc = particle_cells(params, rhoc)
+    frac = ((np.asarray(xp).reshape(-1, 3).astype(np.int64) & mask).astype(np.float32) + np.float32(0.5)) * xres
+    pos = gc.astype(np.float32) + frac
+    pos = (pos * np.float32(ng)) / np.float32(nc) - np.float32(0.5)
+    fl = np.floor(pos)
+    d1 = (fl + np.float32(1.0)) - pos
+    d2 = np.float32(1.0) - d1
+    i1 = fl.astype(np.int64) % ng
+    i2 = (i1 + 1) % ng
+    rho = np.zeros((ng, ng, ng), np.float64)  # [z, y, x]
+    for oz in (0, 1):
+        for oy in (0, 1):
+            for ox in (0, 1):
+                w = ((d2[:, 0] if ox else d1[:, 0]) * (d2[:, 1] if oy else d1[:, 1])) * (d2[:, 2] if oz else d1[:, 2])
+                np.add.at(rho, ((i2 if oz else i1)[:, 2], (i2 if oy else i1)[:, 1], (i2 if ox else i1)[:, 0]),
+                          w.astype(np.float64))
+    mean = rho.sum() / float(ng) ** 3
+    return (rho / mean - 1.0).astype(np.float32)
+
+
+def binned_power(delta1, delta2, ng, box):
+    """cross_power of powerspectrum.f90:21-135 for two density contrasts
+    ([z, y, x] arrays; delta2 None for the auto power): forward FFT / ng^3,
+    linear bins nint(|k|) with the reference's skipped modes, 1/sinc^4 and
+    4 pi k^3 weights; returns xi as an (nbin, 10) array (float64 sums)."""
+    c1 = np.fft.rfftn(np.asarray(delta1, np.float64).reshape(ng, ng, ng)) / float(ng) ** 3
+    if delta2 is None:
+        c2 = c1
+    else:
+        c2 = np.fft.rfftn(np.asarray(delta2, np.float64).reshape(ng, ng, ng)) / float(ng) ** 3
+    nyq = ng // 2
+    kk = (np.arange(ng) + nyq) % ng - nyq
+    kz, ky, kx = np.meshgrid(kk, kk, kk[: nyq + 1], indexing="ij")
+    k_i, j_i, i_i = np.meshgrid(np.arange(ng), np.arange(ng), np.arange(nyq + 1), indexing="ij")
+    keep = ~((i_i == 0) & (j_i == 0) & (k_i == 0))
+    edge = (i_i == 0) | (i_i == nyq)
+    keep &= ~(edge & (j_i > nyq))
+    keep &= ~(edge & ((j_i == 0) | (j_i == nyq)) & (k_i > nyq))
+    kr = np.sqrt((kx * kx + ky * ky + kz * kz).astype(np.float32))
+
+    def sinc(q):
+        a = PI_F * q.astype(np.float32) / np.float32(ng)
+        with np.errstate(invalid="ignore", divide="ignore"):
+            return np.where(q == 0, np.float32(1.0), np.sin(a) / a).astype(np.float32)
+
+    s = sinc(kx) * sinc(ky) * sinc(kz)
+    ibin = np.floor(kr.astype(np.float64) + 0.5).astype(np.int64)  # nint, kr >= 0
+    nbin = int(np.floor(np.float32(nyq) * np.sqrt(np.float32(3.0)) + np.float32(0.5)))
+    w = 4.0 * np.pi * kr.astype(np.float64) ** 3 / s.astype(np.float64) ** 4
+    q = [np.ones_like(kr, np.float64), kr.astype(np.float64), (np.abs(c1) ** 2) * w, (np.abs(c2) ** 2) * w,
+         (c1 * np.conj(c2)).real * w, 1.0 / s.astype(np.float64) ** 2, 1.0 / s.astype(np.float64) ** 4]
+    b = ibin[keep]
+    sums = np.stack([np.bincount(b, weights=v[keep], minlength=nbin + 1)[1: nbin + 1] for v in q], axis=1)
+    xi = np.zeros((nbin, 10))
+    with np.errstate(invalid="ignore", divide="ignore"):
+        xi[:, 0] = sums[:, 0]
+        xi[:, 1] = sums[:, 1] / sums[:, 0] * (2 * float(PI_F)) / box
+        for t in range(2, 7):
+            xi[:, t] = sums[:, t] / sums[:, 0]
+        xi[:, 7] = xi[:, 4] / np.sqrt(xi[:, 2] * xi[:, 3])
+        xi[:, 8] = np.sqrt(xi[:, 3] / xi[:, 2])
+        xi[:, 9] = xi[:, 7] ** 4 / xi[:, 8] ** 2 * xi[:, 3]
+    return xi
+
+
+def power_spectrum(params, xp, rhoc, ng, box, delta2=None):
+    """cicpower.f90 + powerspectrum.f90: xi of the particles' CIC density
+    (crossed with delta2 when given)."""
+    return binned_power(cic_density(params, xp, rhoc, ng), delta2, ng, box)

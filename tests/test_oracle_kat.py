@@ -239,3 +239,29 @@ def test_coarse_kernel_lrck_modes():
     assert np.all(np.isfinite(k))
     # the x kernel vanishes on kx=0 and kx=-nc/2 planes only through oddness
     assert np.abs(k[0][:, :, 0]).max() < 1e-3 * np.abs(k[0]).max()
+
+
+@pytest.mark.parametrize("ng", [8, 16, 24])
+def test_power_spectrum_counts_every_independent_mode_once(ng):
+    # powerspectrum.f90:60-62 skip the zero mode and the conjugate duplicates on
+    # the i=1 and i=nyquist+1 planes: (ng^3 - 8)/2 pairs plus 7 self-conjugate modes
+    rng = np.random.default_rng(ng)
+    xi = O.binned_power(rng.normal(size=(ng, ng, ng)).astype(np.float32), None, ng, 100.0)
+    assert xi[:, 0].sum() == (ng ** 3 - 8) // 2 + 7
+    assert len(xi) == int(np.floor(np.float32(ng // 2) * np.sqrt(np.float32(3)) + np.float32(0.5)))
+
+
+def test_power_spectrum_single_mode_known_answer():
+    # delta = A cos(2 pi k0 x / ng): one mode of amplitude A/2 at k = (k0,0,0),
+    # so Delta^2(k0) = (A/2)^2 / sinc(pi k0/ng)^4 * 4 pi k0^3 / N(k0)
+    ng, k0, A, box = 32, 5, 0.3, 64.0
+    x = np.arange(ng)
+    d = np.broadcast_to(A * np.cos(2 * np.pi * k0 * x / ng), (ng, ng, ng)).astype(np.float64)
+    xi = O.binned_power(d, None, ng, box)
+    a = float(O.PI_F) * k0 / ng
+    sinc = np.sin(a) / a
+    expect = (A / 2) ** 2 / sinc ** 4 * 4 * np.pi * k0 ** 3 / xi[k0 - 1, 0]
+    assert abs(xi[k0 - 1, 2] - expect) < 1e-6 * expect
+    other = np.delete(xi[:, 2], k0 - 1)
+    assert np.all(np.abs(other) < 1e-12)
+    assert abs(xi[k0 - 1, 1] * box / (2 * float(O.PI_F)) - k0) < 0.5
