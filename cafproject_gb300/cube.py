@@ -32,7 +32,7 @@ EXPORTS = ["cube_create", "cube_destroy", "cube_last_error", "cube_upload_state"
            "cube_pm_coarse_forces", "cube_pm_coarse_kick", "cube_get_field", "cube_set_field", "cube_nplocal",
            "cube_synchronize", "cube_timing", "cube_timing_read", "cube_phase_name", "cube_stream",
            "cube_codec_check", "cube_codec_check_static", "cube_arith_check", "cube_pk_nbin",
-           "cube_power_spectrum", "cube_set_option"]
+           "cube_power_spectrum", "cube_checkpoint_write", "cube_checkpoint_read", "cube_set_option"]
 CODEC_STATIC_MAX = 16384
 OPT_EXACT_KICKS = 1
 OPT_PP_LEVEL = 2
@@ -44,6 +44,22 @@ class CubeError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__("%s: %s" % (STATUS.get(code, code), msg))
         self.code = code
+
+
+class SimHeader(ctypes.Structure):
+    """ctypes image of ``cube_sim_header``: the reference's sim_header
+    (parameters.f90:136-160), 224 bytes."""
+
+    _fields_ = ([(n, ctypes.c_int64) for n in (
+        "nplocal", "npglobal", "nplocal_nu", "npglobal_nu", "izipx", "izipv", "izipx_nu", "izipv_nu", "image",
+        "nn", "nnt", "nt", "ncell", "ncb", "timestep", "cur_checkpoint", "cur_halofind")] +
+        [(n, ctypes.c_float) for n in (
+            "a", "t", "tau", "dt_pp", "dt_fine", "dt_coarse", "dt_vmax", "dt_vmax_nu", "mass_p_cdm", "mass_p_nu",
+            "box", "h0", "omega_m", "omega_l", "s8", "vsim2phys", "sigma_vres", "sigma_vi", "sigma_vi_nu", "z_i",
+            "z_i_nu", "vz_max")])
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
 
 
 class CubeStats(ctypes.Structure):
@@ -115,6 +131,8 @@ def load_library(path=None):
     L.cube_arith_check.argtypes = [P, P]
     L.cube_pk_nbin.argtypes = [ctypes.c_int]
     L.cube_power_spectrum.argtypes = [P, ctypes.c_int, F, P, P, ctypes.c_int]
+    L.cube_checkpoint_write.argtypes = [P, ctypes.c_char_p, F, ctypes.c_int, P]
+    L.cube_checkpoint_read.argtypes = [P, ctypes.c_char_p, F, ctypes.c_int, P]
     L.cube_set_option.argtypes = [P, ctypes.c_int, I64]
     _lib = L
     return L
@@ -277,6 +295,22 @@ class CubeGPU:
         b = np.empty(v.size, np.int32)
         self._check(self.L.cube_codec_check(self.h, float(sigma), _ptr(v), v.size, _ptr(a), _ptr(b)))
         return a, b
+
+    def checkpoint_write(self, directory, z, image=1, **header):
+        """checkpoint (checkpoint.f90): the reference's files for this image;
+        header fields (a, t, tau, box, omega_m, ...) as keyword arguments."""
+        h = SimHeader()
+        for k, v in header.items():
+            setattr(h, k, v)
+        self._check(self.L.cube_checkpoint_write(self.h, os.fsencode(directory), float(z), int(image),
+                                                 ctypes.byref(h)))
+
+    def checkpoint_read(self, directory, z, image=1):
+        """particle_initialization's restart read; returns the header dict."""
+        h = SimHeader()
+        self._check(self.L.cube_checkpoint_read(self.h, os.fsencode(directory), float(z), int(image),
+                                                ctypes.byref(h)))
+        return h.as_dict()
 
     def power_spectrum(self, ng, box, delta2=None):
         """xi(10, nbin) of cross_power (powerspectrum.f90) for the particles'

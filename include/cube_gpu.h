@@ -91,6 +91,26 @@ typedef struct cube_stats {
   int32_t pad3;
 } cube_stats;
 
+/* The reference's checkpoint header, type sim_header (parameters.f90:136-160),
+   byte for byte as Fortran stream I/O writes it: 17 int64 then 22 real(4). */
+typedef struct cube_sim_header {
+  int64_t nplocal, npglobal, nplocal_nu, npglobal_nu;
+  int64_t izipx, izipv, izipx_nu, izipv_nu;
+  int64_t image;
+  int64_t nn, nnt, nt, ncell, ncb;
+  int64_t timestep;
+  int64_t cur_checkpoint;
+  int64_t cur_halofind;
+  float a, t, tau;
+  float dt_pp, dt_fine, dt_coarse, dt_vmax, dt_vmax_nu;
+  float mass_p_cdm, mass_p_nu;
+  float box;
+  float h0, omega_m, omega_l, s8;
+  float vsim2phys, sigma_vres, sigma_vi, sigma_vi_nu;
+  float z_i, z_i_nu;
+  float vz_max;
+} cube_sim_header;
+
 typedef struct cube_ctx cube_ctx;
 
 /* Fields for inspection / injection in parity tests. */
@@ -120,6 +140,16 @@ int cube_upload_state(cube_ctx* ctx, int64_t nplocal, const void* xp, const void
                       const int32_t* rhoc, const float* vfield);
 int cube_download_state(cube_ctx* ctx, int64_t* nplocal, void* xp, void* vp, int32_t* pid, int32_t* rhoc,
                         float* vfield);
+
+/* Checkpoint files in the reference's format (checkpoint.f90:10-50; read back
+   as particle_initialization.f90:34-64 does): in dir, <z>_info_<image>.bin,
+   _xp_, _vp_, _np_, _vc_ and (with particle ids) _id_, <z> = z printed as
+   Fortran f7.3 without blanks.  Write fills nplocal, izipx/v, nnt, nt, ncell,
+   ncb, image and sigma_vi from the context and takes the other header fields
+   from hdr; read checks the zip format and tile geometry, uploads the state,
+   sets sigma_vi and returns the header in hdr (may be NULL). */
+int cube_checkpoint_write(cube_ctx* ctx, const char* dir, float z, int image, const cube_sim_header* hdr);
+int cube_checkpoint_read(cube_ctx* ctx, const char* dir, float z, int image, cube_sim_header* hdr);
 
 /* sigma_vi / sigma_vi_new module variables (variables.f90:36). */
 int cube_set_sigma(cube_ctx* ctx, float sigma_vi, float sigma_vi_new);

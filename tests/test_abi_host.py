@@ -116,3 +116,11 @@ def test_fast_division_is_exact():
         for n in ns:
             n = int(n)
             assert fdiv(n, d, m, l) == n // d, (n, d)
+
+
+def test_sim_header_matches_reference_layout():
+    # sim_header (parameters.f90:136-160) in Fortran stream I/O: 17 int64 then 22 real(4)
+    from cafproject_gb300.cube import SimHeader
+    assert ctypes.sizeof(SimHeader) == 17 * 8 + 22 * 4 == 224
+    assert SimHeader.a.offset == 136 and SimHeader.vz_max.offset == 220
+    assert SimHeader.sigma_vi.offset == 136 + 4 * 17
