@@ -1,0 +1,70 @@
+"""Golden fixtures (tests/golden/oracle_step_nc20.npz, made by
+tests/golden/make_golden.py): the oracle must reproduce them exactly on the
+CPU, and the CUDA path is checked against them on the GPU with the bars of
+the parity tests."""
+import os
+
+import numpy as np
+import pytest
+
+from cafproject_gb300 import params as P
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLD = os.path.join(HERE, "golden", "oracle_step_nc20.npz")
+
+
+def _gold():
+    return dict(np.load(GOLD))
+
+
+def _mk():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(HERE, "golden", "make_golden.py"))
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    return m
+
+
+def test_oracle_reproduces_golden_fixtures():
+    pytest.importorskip("oracle.cube_oracle")
+    g = _gold()
+    new = _mk().make()
+    assert set(new) == set(g)
+    for k, v in g.items():
+        if k == "pk_xi":
+            np.testing.assert_allclose(new[k], v, rtol=1e-12, equal_nan=True)
+        else:
+            np.testing.assert_array_equal(np.asarray(new[k]), v, err_msg=k)
+
+
+@pytest.mark.gpu
+def test_gpu_step_matches_golden_fixtures():
+    from cafproject_gb300 import cube as C
+    m = _mk()
+    g = _gold()
+    p = m.golden_params()
+    c = C.CubeGPU(p)
+    try:
+        c.upload(g["in_xp"], g["in_vp"], g["in_pid"], g["in_rhoc"], g["in_vfield"])
+        c.set_sigma(g["sigma_vi"], g["sigma_vi"])
+        u = c.update_x(np.float32(m.DT_OLD), np.float32(m.DT_STEP), g["vz_max"])
+        s = c.download()
+        for k in ("xp", "vp", "pid", "rhoc"):
+            np.testing.assert_array_equal(s[k].reshape(g["upd_" + k].shape), g["upd_" + k], err_msg=k)
+        np.testing.assert_array_equal(s["vfield"].reshape(-1, 3).view(np.uint32), g["upd_vfield"].view(np.uint32))
+        assert abs(u["sum_r"] - g["upd_sum_r"]) <= 1e-12 * abs(g["upd_sum_r"])
+        xi = c.power_spectrum(2 * p.nc, p.box)
+        full = g["pk_xi"][:, 0] > 0
+        np.testing.assert_array_equal(xi[:, 0], g["pk_xi"][:, 0])
+        np.testing.assert_allclose(xi[full, 2], g["pk_xi"][full, 2], rtol=1e-4)
+        pp = c.ext_pp_force(m.A_MID, m.DT)
+        assert pp["npairs"] == g["pp_npairs"]
+        d = np.abs(c.download()["vp"].reshape(-1, 3).astype(np.int64) - g["pp_vp"].astype(np.int64))
+        assert d.max() <= 1 and (d > 0).mean() < 1e-3
+        pm = c.particle_mesh(m.A_MID, m.DT)
+        d = np.abs(c.download()["vp"].reshape(-1, 3).astype(np.int64) - g["pm_vp"].astype(np.int64))
+        assert d.max() <= 2 and (d > 0).mean() < 5e-3
+        assert abs(pm["f2_max_fine"] - g["pm_f2_max_fine"]) <= 1e-5 * g["pm_f2_max_fine"]
+        assert abs(pm["f2_max_coarse"] - g["pm_f2_max_coarse"]) <= 1e-5 * g["pm_f2_max_coarse"]
+    finally:
+        c.close()
