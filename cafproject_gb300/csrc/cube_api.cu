@@ -279,11 +279,12 @@ extern "C" int cube_pm_coarse_kick(cube_ctx* c, float a_mid, float dt, cube_stat
 extern "C" int cube_particle_mesh(cube_ctx* c, float a_mid, float dt, cube_stats* st) {
   int r = check_ready(c);
   if (r) return r;
-  if ((r = cube_fine_forces_impl(c, st))) return r;
-  if ((r = cube_fine_kick_impl(c, a_mid, dt))) return r;
+  const float pre[2] = {a_mid, dt};
+  if ((r = cube_fine_forces_impl(c, st, pre))) return r;
+  if ((r = cube_fine_kick_impl(c, a_mid, dt, true))) return r;
   c->sigma_vi = c->sigma_vi_new;  // pm.f90:193
-  if ((r = cube_coarse_forces_impl(c, st))) return r;
-  return cube_coarse_kick_impl(c, a_mid, dt, st);
+  if ((r = cube_coarse_forces_impl(c, st, pre))) return r;
+  return cube_coarse_kick_impl(c, a_mid, dt, st, true);
 }
 
 extern "C" int64_t cube_nplocal(const cube_ctx* c) { return c ? c->np : -1; }

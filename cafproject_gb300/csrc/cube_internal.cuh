@@ -421,15 +421,20 @@ __device__ __forceinline__ float div_const(float x, float c, float rc) {
   return __fmaf_rn(r, rc, q);
 }
 
-// one CIC kick term force*a_mid*dt/6/pi*wa*wb*wc in real(4), left to right (pm.f90:146)
-__device__ __forceinline__ float kick_term(float f, float a_mid, float dt, float wa, float wb, float wc) {
+// one CIC kick term force*a_mid*dt/6/pi*wa*wb*wc in real(4), left to right
+// (pm.f90:146), split at the weights: kick_pre depends on the mesh point only,
+// kick_w applies the particle's three CIC weights to it
+__device__ __forceinline__ float kick_pre(float f, float a_mid, float dt) {
   float r = __fmul_rn(f, a_mid);
   r = __fmul_rn(r, dt);
   r = div_const(r, 6.0f, 0.16666667163372040f);         // RN(1/6)
-  r = div_const(r, CUBE_PI_F, 0.31830987334251404f);    // RN(1/pi_f)
-  r = __fmul_rn(r, wa);
-  r = __fmul_rn(r, wb);
-  return __fmul_rn(r, wc);
+  return div_const(r, CUBE_PI_F, 0.31830987334251404f);  // RN(1/pi_f)
+}
+__device__ __forceinline__ float kick_w(float g, float wa, float wb, float wc) {
+  return __fmul_rn(__fmul_rn(__fmul_rn(g, wa), wb), wc);
+}
+__device__ __forceinline__ float kick_term(float f, float a_mid, float dt, float wa, float wb, float wc) {
+  return kick_w(kick_pre(f, a_mid, dt), wa, wb, wc);
 }
 
 // host view of a float stored as its bit pattern
@@ -520,10 +525,13 @@ int cube_update_x_impl(cube_ctx* c, float dt_old, float dt, float vz_max, cube_s
 int cube_pp_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st);
 int cube_fine_density_impl(cube_ctx* c, cube_stats* st);
 int cube_coarse_density_impl(cube_ctx* c, cube_stats* st);
-int cube_fine_forces_impl(cube_ctx* c, cube_stats* st);
-int cube_fine_kick_impl(cube_ctx* c, float a_mid, float dt);
-int cube_coarse_forces_impl(cube_ctx* c, cube_stats* st);
-int cube_coarse_kick_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st);
+// pre (a_mid, dt) non-null: after the maxima, the force meshes are rewritten
+// as the mesh part of the kick term, force*a_mid*dt/6/pi, and the kick that
+// follows is given pre=true (fused step only; the stage calls keep forces)
+int cube_fine_forces_impl(cube_ctx* c, cube_stats* st, const float* pre = nullptr);
+int cube_fine_kick_impl(cube_ctx* c, float a_mid, float dt, bool pre = false);
+int cube_coarse_forces_impl(cube_ctx* c, cube_stats* st, const float* pre = nullptr);
+int cube_coarse_kick_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st, bool pre = false);
 int cube_pk_deposit(cube_ctx* c, int ng, float* rho, unsigned long long* total);
 int cube_state_in(cube_ctx* c, int64_t np, const void* xp, const void* vp, const int32_t* pid,
                   const int32_t* rhoc, const float* vfield);

@@ -217,21 +217,36 @@ __global__ void k_green3(const float2* __restrict__ rk, const float* __restrict_
 __device__ __forceinline__ float f2sum(float a, float b, float c) {
   return __fadd_rn(__fadd_rn(__fmul_rn(a, a), __fmul_rn(b, b)), __fmul_rn(c, c));
 }
-__global__ void k_f2max(const float* __restrict__ f0, const float* __restrict__ f1, const float* __restrict__ f2,
-                        int n, unsigned int* __restrict__ out) {
+// kPre: then rewrite each force value as its kick factor force*a_mid*dt/6/pi
+template <bool kPre>
+__global__ void k_f2max(float* __restrict__ f0, float* __restrict__ f1, float* __restrict__ f2, int n,
+                        unsigned int* __restrict__ out, float a_mid, float dt) {
   const int64_t rows = (int64_t)n * n;
   const int h = n >> 1;
   float m = 0.f;
   for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
     const int64_t o = r * (n + 2);
-    const float2* a = reinterpret_cast<const float2*>(f0 + o);
-    const float2* b = reinterpret_cast<const float2*>(f1 + o);
-    const float2* c = reinterpret_cast<const float2*>(f2 + o);
+    float2* a = reinterpret_cast<float2*>(f0 + o);
+    float2* b = reinterpret_cast<float2*>(f1 + o);
+    float2* c = reinterpret_cast<float2*>(f2 + o);
     for (int x = threadIdx.x; x < h; x += blockDim.x) {
-      float2 u = __ldg(a + x), v = __ldg(b + x), w = __ldg(c + x);
+      float2 u = a[x], v = b[x], w = c[x];
       m = fmaxf(m, fmaxf(f2sum(u.x, v.x, w.x), f2sum(u.y, v.y, w.y)));
+      if (kPre) {
+        a[x] = make_float2(kick_pre(u.x, a_mid, dt), kick_pre(u.y, a_mid, dt));
+        b[x] = make_float2(kick_pre(v.x, a_mid, dt), kick_pre(v.y, a_mid, dt));
+        c[x] = make_float2(kick_pre(w.x, a_mid, dt), kick_pre(w.y, a_mid, dt));
+      }
     }
-    if ((n & 1) && threadIdx.x == 0) m = fmaxf(m, f2sum(f0[o + n - 1], f1[o + n - 1], f2[o + n - 1]));
+    if ((n & 1) && threadIdx.x == 0) {
+      const int64_t e = o + n - 1;
+      m = fmaxf(m, f2sum(f0[e], f1[e], f2[e]));
+      if (kPre) {
+        f0[e] = kick_pre(f0[e], a_mid, dt);
+        f1[e] = kick_pre(f1[e], a_mid, dt);
+        f2[e] = kick_pre(f2[e], a_mid, dt);
+      }
+    }
   }
   for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) atomic_max_pos(out, m);
@@ -268,7 +283,8 @@ struct KickArgs {
 // float hi is within half an ulp).  certify_abs keeps the code only when every
 // double inside that bound encodes to it; otherwise the lane runs the exact
 // chain, so the stored code is always the reference's.
-template <bool kFine>
+// kPre: the meshes hold force*a_mid*dt/6/pi already (k_f2max<true>)
+template <bool kFine, bool kPre>
 __global__ void k_kick(KickArgs a) {
   const Geo& g = a.g;
   float vm[3] = {0.f, 0.f, 0.f};
@@ -306,14 +322,16 @@ __global__ void k_kick(KickArgs a) {
     for (int d = 0; d < 3; d++) {
       const float* F = a.f[d];
       float t[8];
-      t[0] = kick_term(__ldg(F + c111), a.a_mid, a.dt, d1[0], d1[1], d1[2]);
-      t[1] = kick_term(__ldg(F + c211), a.a_mid, a.dt, d2[0], d1[1], d1[2]);
-      t[2] = kick_term(__ldg(F + c121), a.a_mid, a.dt, d1[0], d2[1], d1[2]);
-      t[3] = kick_term(__ldg(F + c112), a.a_mid, a.dt, d1[0], d1[1], d2[2]);
-      t[4] = kick_term(__ldg(F + c122), a.a_mid, a.dt, d1[0], d2[1], d2[2]);
-      t[5] = kick_term(__ldg(F + c212), a.a_mid, a.dt, d2[0], d1[1], d2[2]);
-      t[6] = kick_term(__ldg(F + c221), a.a_mid, a.dt, d2[0], d2[1], d1[2]);
-      t[7] = kick_term(__ldg(F + c222), a.a_mid, a.dt, d2[0], d2[1], d2[2]);
+#define KT(c, wa, wb, wc) (kPre ? kick_w(__ldg(F + (c)), wa, wb, wc) : kick_term(__ldg(F + (c)), a.a_mid, a.dt, wa, wb, wc))
+      t[0] = KT(c111, d1[0], d1[1], d1[2]);
+      t[1] = KT(c211, d2[0], d1[1], d1[2]);
+      t[2] = KT(c121, d1[0], d2[1], d1[2]);
+      t[3] = KT(c112, d1[0], d1[1], d2[2]);
+      t[4] = KT(c122, d1[0], d2[1], d2[2]);
+      t[5] = KT(c212, d2[0], d1[1], d2[2]);
+      t[6] = KT(c221, d2[0], d2[1], d1[2]);
+      t[7] = KT(c222, d2[0], d2[1], d2[2]);
+#undef KT
       int code = load_code(a.vp_in, 3 * p + d, g.izipv);
       float dh = codec_decode_ff(a.cin, code).x;
       float S = t[0], T = fabsf(t[0]);
@@ -506,7 +524,7 @@ int cube_fine_density_impl(cube_ctx* c, cube_stats* st) {
   return CUBE_OK;
 }
 
-int cube_fine_forces_impl(cube_ctx* c, cube_stats* st) {
+int cube_fine_forces_impl(cube_ctx* c, cube_stats* st, const float* pre) {
   cudaStream_t s = c->stream;
   int64_t nfh = c->nf / 2 + 1;
   int64_t nspec = nfh * c->nf * (int64_t)c->nf;
@@ -524,8 +542,12 @@ int cube_fine_forces_impl(cube_ctx* c, cube_stats* st) {
     CUBE_FFT(c, cufftExecC2R(c->plan_f_c2r, (cufftComplex*)c->force_f[d], c->force_f[d]));
   cube_phase_end(c, PH_F_C2R);
   cube_phase_begin(c, PH_F_F2MAX);
-  k_f2max<<<cube_grid((int64_t)c->nf * c->nf, 1, 8), 256, 0, s>>>(c->force_f[0], c->force_f[1], c->force_f[2], c->nf,
-                                                   &c->dstats->f2_fine_bits);
+  if (pre)
+    k_f2max<true><<<cube_grid((int64_t)c->nf * c->nf, 1, 8), 256, 0, s>>>(
+        c->force_f[0], c->force_f[1], c->force_f[2], c->nf, &c->dstats->f2_fine_bits, pre[0], pre[1]);
+  else
+    k_f2max<false><<<cube_grid((int64_t)c->nf * c->nf, 1, 8), 256, 0, s>>>(
+        c->force_f[0], c->force_f[1], c->force_f[2], c->nf, &c->dstats->f2_fine_bits, 0.f, 0.f);
   cube_phase_end(c, PH_F_F2MAX);
   CUBE_CUDA(c, cudaGetLastError());
   if (st) {
@@ -537,7 +559,7 @@ int cube_fine_forces_impl(cube_ctx* c, cube_stats* st) {
   return CUBE_OK;
 }
 
-int cube_fine_kick_impl(cube_ctx* c, float a_mid, float dt) {
+int cube_fine_kick_impl(cube_ctx* c, float a_mid, float dt, bool pre) {
   KickArgs k{};
   int r = cube_codec_pair(c, c->sigma_vi, c->sigma_vi_new, &k.cin, &k.cout);
   if (r) return r;
@@ -557,7 +579,10 @@ int cube_fine_kick_impl(cube_ctx* c, float a_mid, float dt) {
   k.nexact = &c->dstats->nexact;
   k.exact_only = c->opt_exact_kicks;
   cube_phase_begin(c, PH_F_KICK);
-  k_kick<true><<<cube_grid(c->np, 256), 256, 0, c->stream>>>(k);
+  if (pre)
+    k_kick<true, true><<<cube_grid(c->np, 256), 256, 0, c->stream>>>(k);
+  else
+    k_kick<true, false><<<cube_grid(c->np, 256), 256, 0, c->stream>>>(k);
   cube_phase_end(c, PH_F_KICK);
   CUBE_CUDA(c, cudaGetLastError());
   return CUBE_OK;
@@ -593,7 +618,7 @@ int cube_coarse_density_impl(cube_ctx* c, cube_stats* st) {
   return CUBE_OK;
 }
 
-int cube_coarse_forces_impl(cube_ctx* c, cube_stats* st) {
+int cube_coarse_forces_impl(cube_ctx* c, cube_stats* st, const float* pre) {
   cudaStream_t s = c->stream;
   int nc = c->p.nc;
   int64_t nch = nc / 2 + 1;
@@ -606,8 +631,12 @@ int cube_coarse_forces_impl(cube_ctx* c, cube_stats* st) {
                                                   (float2*)c->force_c[1], (float2*)c->force_c[2]);
   for (int d = 0; d < 3; d++)
     CUBE_FFT(c, cufftExecC2R(c->plan_c_c2r, (cufftComplex*)c->force_c[d], c->force_c[d]));
-  k_f2max<<<cube_grid((int64_t)nc * nc, 1, 8), 256, 0, s>>>(c->force_c[0], c->force_c[1], c->force_c[2], nc,
-                                                                 &c->dstats->f2_coarse_bits);
+  if (pre)
+    k_f2max<true><<<cube_grid((int64_t)nc * nc, 1, 8), 256, 0, s>>>(c->force_c[0], c->force_c[1], c->force_c[2], nc,
+                                                                    &c->dstats->f2_coarse_bits, pre[0], pre[1]);
+  else
+    k_f2max<false><<<cube_grid((int64_t)nc * nc, 1, 8), 256, 0, s>>>(c->force_c[0], c->force_c[1], c->force_c[2], nc,
+                                                                     &c->dstats->f2_coarse_bits, 0.f, 0.f);
   cube_phase_end(c, PH_C_FFT);
   CUBE_CUDA(c, cudaGetLastError());
   if (st) {
@@ -619,7 +648,7 @@ int cube_coarse_forces_impl(cube_ctx* c, cube_stats* st) {
   return CUBE_OK;
 }
 
-int cube_coarse_kick_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st) {
+int cube_coarse_kick_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st, bool pre) {
   KickArgs k{};
   int r = cube_codec_pair(c, c->sigma_vi, c->sigma_vi, &k.cin, &k.cout);
   if (r) return r;
@@ -646,7 +675,10 @@ int cube_coarse_kick_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st) {
   k.vmax_only = 0;
   k.exact_only = c->opt_exact_kicks;
   cube_phase_begin(c, PH_C_KICK);
-  k_kick<false><<<cube_grid(c->np, 256), 256, 0, c->stream>>>(k);
+  if (pre)
+    k_kick<false, true><<<cube_grid(c->np, 256), 256, 0, c->stream>>>(k);
+  else
+    k_kick<false, false><<<cube_grid(c->np, 256), 256, 0, c->stream>>>(k);
   cube_phase_end(c, PH_C_KICK);
   CUBE_CUDA(c, cudaGetLastError());
   r = cube_stats_fetch(c);
@@ -661,7 +693,10 @@ int cube_coarse_kick_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st) {
   if (rerun) {
     CUBE_CUDA(c, cudaMemsetAsync(c->dstats->vmax_bits, 0, 12, c->stream));
     k.vmax_only = 1;
-    k_kick<false><<<cube_grid(c->np, 256), 256, 0, c->stream>>>(k);
+    if (pre)
+      k_kick<false, true><<<cube_grid(c->np, 256), 256, 0, c->stream>>>(k);
+    else
+      k_kick<false, false><<<cube_grid(c->np, 256), 256, 0, c->stream>>>(k);
     CUBE_CUDA(c, cudaGetLastError());
     r = cube_stats_fetch(c);
     if (r) return r;
