@@ -486,6 +486,37 @@ __device__ __forceinline__ int block_exclusive_scan(int* v, int n) {
   return total;
 }
 
+// The same for n 16-bit counts whose total stays below 65536.
+__device__ __forceinline__ int block_exclusive_scan_u16(unsigned short* v, int n) {
+  __shared__ int wsum16[32];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5, nw = blockDim.x >> 5;
+  const int per = (n + blockDim.x - 1) / blockDim.x;
+  const int b0 = min(n, t * per), b1 = min(n, b0 + per);
+  int s = 0;
+  for (int i = b0; i < b1; i++) s += v[i];
+  int inc = s;
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += y;
+  }
+  if (lane == 31) wsum16[w] = inc;
+  __syncthreads();
+  int wbase = 0, total = 0;
+  for (int k = 0; k < nw; k++) {
+    int x = wsum16[k];
+    if (k < w) wbase += x;
+    total += x;
+  }
+  int run = wbase + inc - s;
+  for (int i = b0; i < b1; i++) {
+    int x = v[i];
+    v[i] = (unsigned short)run;
+    run += x;
+  }
+  __syncthreads();
+  return total;
+}
+
 // Visit every particle of a box of source cells: cell t = sx + S0*row has
 // pref[t] particles before it (exclusive scan over the box, pref[ns] not
 // needed) and its first particle at sstart[t].  One warp per row of S0 <= S0MAX

@@ -39,7 +39,8 @@ constexpr int PNF_MAX = (4 * PB + 2) * (4 * PB + 2) * (4 * PB + 2);
 constexpr int PP_CAP = 1536;                   // staged particles per block
 constexpr int PP_THREADS = 256;
 constexpr size_t PP_SMEM = (sizeof(float4) + sizeof(unsigned) + sizeof(unsigned short)) * PP_CAP +
-                           sizeof(int) * (PNF_MAX + 1);
+                           sizeof(unsigned short) * (PNF_MAX + 2);
+static_assert(PP_CAP < 65536, "bin offsets are 16-bit");
 
 struct PPArgs {
   Geo g;
@@ -168,14 +169,16 @@ __device__ bool pp_block(const PPArgs& a, const int C0[3], const int B[3], PPSme
   float4* pts = dyn;                                              // x, y, z, particle index
   unsigned* kinfo = reinterpret_cast<unsigned*>(pts + PP_CAP);    // bin | rank in bin << 13
   unsigned short* order = reinterpret_cast<unsigned short*>(kinfo + PP_CAP);  // slots by bin
-  int* bins = reinterpret_cast<int*>(order + PP_CAP);             // NF+1 bin offsets
+  // NF+1 16-bit bin offsets, counted two to a 32-bit word
+  unsigned short* bins = order + PP_CAP;
+  unsigned* bins32 = reinterpret_cast<unsigned*>(bins);
   for (int t = threadIdx.x; t < NS; t += blockDim.x) {
     int sx = t % S0, sy = (t / S0) % S1, sz = t / (S0 * S1);
     int64_t c = cell_id(g, wrap1(C0[0] + sx - 1, nc), wrap1(C0[1] + sy - 1, nc), wrap1(C0[2] + sz - 1, nc));
     sm.pref[t] = a.rhoc[c];
     sm.sstart[t] = a.cstart[c];
   }
-  for (int t = threadIdx.x; t < NF; t += blockDim.x) bins[t] = 0;
+  for (int t = threadIdx.x; t < (NF + 2) / 2; t += blockDim.x) bins32[t] = 0u;
   if (threadIdx.x == 0) sm.nst = 0;
   __syncthreads();
   const int total = block_exclusive_scan(sm.pref, NS);
@@ -195,15 +198,16 @@ __device__ bool pp_block(const PPArgs& a, const int C0[3], const int B[3], PPSme
     int slot = atomicAdd(&sm.nst, 1);
     if (slot >= PP_CAP) return;
     int f = fi[0] + F0 * (fi[1] + F1 * fi[2]);
-    int r = atomicAdd(&bins[f], 1);
+    const unsigned sh = 16u * (unsigned)(f & 1);
+    int r = (int)((atomicAdd(&bins32[f >> 1], 1u << sh) >> sh) & 0xffffu);
     pts[slot] = make_float4(x[0], x[1], x[2], __int_as_float((int)p));
     kinfo[slot] = (unsigned)f | ((unsigned)r << 13);
   });
   __syncthreads();
   const int nst = sm.nst;
   if (nst > PP_CAP) return false;
-  block_exclusive_scan(bins, NF);
-  if (threadIdx.x == 0) bins[NF] = nst;
+  block_exclusive_scan_u16(bins, NF);
+  if (threadIdx.x == 0) bins[NF] = (unsigned short)nst;
   for (int t = threadIdx.x; t < nst; t += blockDim.x) {
     unsigned k = kinfo[t];
     order[bins[k & 8191u] + (int)(k >> 13)] = (unsigned short)t;
@@ -215,17 +219,17 @@ __device__ bool pp_block(const PPArgs& a, const int C0[3], const int B[3], PPSme
     if (fx < 1 || fy < 1 || fz < 1 || fx > 4 * B[0] || fy > 4 * B[1] || fz > 4 * B[2]) continue;  // ring
     int f = (int)(kinfo[t] & 8191u);
     long long F[3] = {0, 0, 0};
+    // the three bins dx = -1..1 of one (dy, dz) row are consecutive: one range
     for (int dz = -1; dz <= 1; dz++)
-      for (int dy = -1; dy <= 1; dy++)
-        for (int dx = -1; dx <= 1; dx++) {
-          int f2 = f + dx + F0 * (dy + F1 * dz);
-          int k1 = bins[f2 + 1];
-          for (int k = bins[f2]; k < k1; k++) {
-            float4 o = pts[order[k]];
-            acc.npairs++;
-            pair_force(a, o.x - q.x, o.y - q.y, o.z - q.z, F);
-          }
+      for (int dy = -1; dy <= 1; dy++) {
+        const int f2 = f + F0 * (dy + F1 * dz);
+        const int k1 = bins[f2 + 2];
+        for (int k = bins[f2 - 1]; k < k1; k++) {
+          float4 o = pts[order[k]];
+          acc.npairs++;
+          pair_force(a, o.x - q.x, o.y - q.y, o.z - q.z, F);
         }
+      }
     acc.nwork++;
     acc.f2max = fmaxf(acc.f2max, pp_kick(a, (int64_t)__float_as_int(q.w), F));
   }
