@@ -564,6 +564,7 @@ int cube_fine_kick_impl(cube_ctx* c, float a_mid, float dt, bool pre = false);
 int cube_coarse_forces_impl(cube_ctx* c, cube_stats* st, const float* pre = nullptr);
 int cube_coarse_kick_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st, bool pre = false);
 int cube_pk_deposit(cube_ctx* c, int ng, float* rho, unsigned long long* total);
+int dep_shift(float mass);  // deposits' fixed point: total = integer * 2^-dep_shift(mass)
 int cube_state_in(cube_ctx* c, int64_t np, const void* xp, const void* vp, const int32_t* pid,
                   const int32_t* rhoc, const float* vfield);
 int cube_state_out(cube_ctx* c, int64_t* np, void* xp, void* vp, int32_t* pid, int32_t* rhoc, float* vfield);

@@ -119,7 +119,7 @@ extern "C" int cube_power_spectrum(cube_ctx* c, int ng, float box, const float* 
   if (r) return r;
   r = cube_stats_fetch(c);
   if (r) return r;
-  const double total = (double)c->hstats->rhof_fix / 4294967296.0;
+  const double total = std::ldexp((double)c->hstats->rhof_fix, -dep_shift(1.0f));
   if (!(total > 0.0)) return cube_fail(c, CUBE_ERR_STATE, "no mass on the mesh");
   const double mean = total / ((double)ng * ng * ng);
   k_pk_delta<<<cube_grid((int64_t)ng * ng, 1, 8), 256, 0, s>>>(m1, ng, (float)(1.0 / mean));

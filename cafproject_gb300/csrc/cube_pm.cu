@@ -91,9 +91,10 @@ struct DepArgs {
   float* rho;                 // padded periodic mesh, row stride n+2
   unsigned long long* total;  // sum of all owned cells in fixed point (exact)
   int ng;                     // power-spectrum mesh (kPk only)
+  float qscale, qinv;         // fixed-point scale 2^s and 2^-s (dep_shift)
 };
 
-constexpr double kFixScale = 4294967296.0;  // 2^32
+
 
 // kPk: the power-spectrum deposit of cicpower.f90:100-133 (position
 // (cell + frac)*ng/nc - 0.5 in real(4), global frame) instead of the PM ones
@@ -102,7 +103,8 @@ __global__ void __launch_bounds__(256) k_deposit_det(DepArgs a) {
   constexpr int SX = BX + LO + HI, SY = BY + LO + HI, SZ = BZ + LO + HI;
   constexpr int NSRC = SX * SY * SZ;
   constexpr int MX = MPC * BX, MY = MPC * BY, MZ = MPC * BZ;
-  extern __shared__ unsigned long long acc[];  // MX*MY*MZ
+  extern __shared__ unsigned acc[];  // low words [0, MX*MY*MZ), carry words after them
+  unsigned* carry = acc + MX * MY * MZ;
   __shared__ int pref[NSRC];
   __shared__ long long sstart[NSRC];
   __shared__ unsigned long long btot;
@@ -112,7 +114,7 @@ __global__ void __launch_bounds__(256) k_deposit_det(DepArgs a) {
   int b = blockIdx.x;
   int C0[3] = {(b % nbx) * BX, ((b / nbx) % nby) * BY, (b / (nbx * nby)) * BZ};
   int B[3] = {min(BX, nc - C0[0]), min(BY, nc - C0[1]), min(BZ, nc - C0[2])};
-  for (int i = threadIdx.x; i < MX * MY * MZ; i += blockDim.x) acc[i] = 0ull;
+  for (int i = threadIdx.x; i < 2 * MX * MY * MZ; i += blockDim.x) acc[i] = 0u;
   if (threadIdx.x == 0) btot = 0ull;
   // source cells and their particle counts
   for (int t = threadIdx.x; t < NSRC; t += blockDim.x) {
@@ -161,12 +163,11 @@ __global__ void __launch_bounds__(256) k_deposit_det(DepArgs a) {
       int x = rel[0] + ox, y = rel[1] + oy, z = rel[2] + oz;
       if (x < 0 || y < 0 || z < 0 || x >= lim[0] || y >= lim[1] || z >= lim[2]) continue;
       float w = __fmul_rn(__fmul_rn(__fmul_rn(ox ? d2[0] : d1[0], oy ? d2[1] : d1[1]), oz ? d2[2] : d1[2]), a.mass);
-      // w * 2^32 as an integer from two 32-bit conversions (a 64-bit conversion
-      // would run on the double-precision unit)
-      float ws = __fmul_rn(w, 256.0f), fh = floorf(ws);
-      unsigned long long q = ((unsigned long long)(unsigned int)fh << 24) +
-                             (unsigned int)__fmul_rn(__fsub_rn(ws, fh), 16777216.0f);
-      atomicAdd(&acc[x + MX * (y + MY * z)], q);
+      // w * 2^s (exact scaling, truncated) < 2^31; carry out of the low word
+      const unsigned q = __float2uint_rz(__fmul_rn(w, a.qscale));
+      const int e = x + MX * (y + MY * z);
+      const unsigned old = atomicAdd(&acc[e], q);
+      if (old + q < old) atomicAdd(&carry[e], 1u);
     }
   });
   __syncthreads();
@@ -174,11 +175,10 @@ __global__ void __launch_bounds__(256) k_deposit_det(DepArgs a) {
   for (int i = threadIdx.x; i < MX * MY * MZ; i += blockDim.x) {
     int x = i % MX, y = (i / MX) % MY, z = i / (MX * MY);
     if (x >= MPC * B[0] || y >= MPC * B[1] || z >= MPC * B[2]) continue;
-    unsigned long long v = acc[i];
-    mysum += v;
-    // v * 2^-32 as float: split so each part converts exactly-ish in FP32
-    float hi = (float)(unsigned int)(v >> 32), lo = (float)(unsigned int)(v & 0xffffffffull);
-    float r = __fmaf_rn(lo, 2.3283064365386963e-10f, hi);
+    const unsigned lo = acc[i], hi = carry[i];
+    mysum += ((unsigned long long)hi << 32) | lo;
+    // (hi*2^32 + lo) * 2^-s as float
+    float r = __fmaf_rn((float)lo, a.qinv, __fmul_rn((float)hi, __fmul_rn(a.qinv, 4294967296.0f)));
     a.rho[mesh_idx(n, MPC * C0[0] + x, MPC * C0[1] + y, MPC * C0[2] + z)] = r;
   }
   for (int o = 16; o > 0; o >>= 1) mysum += __shfl_xor_sync(0xffffffffu, mysum, o);
@@ -191,7 +191,7 @@ template <int MPC, int BX, int BY, int BZ, int LO, int HI, bool kPk = false>
 int launch_deposit(cube_ctx* c, const DepArgs& a) {
   int nc = c->p.nc;
   int nb = ((nc + BX - 1) / BX) * ((nc + BY - 1) / BY) * ((nc + BZ - 1) / BZ);
-  size_t smem = sizeof(unsigned long long) * (MPC * BX) * (MPC * BY) * (MPC * BZ);
+  size_t smem = 2 * sizeof(unsigned) * (MPC * BX) * (MPC * BY) * (MPC * BZ);
   auto kern = k_deposit_det<MPC, BX, BY, BZ, LO, HI, kPk>;
   CUBE_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   kern<<<nb, 256, smem, c->stream>>>(a);
@@ -382,6 +382,20 @@ __global__ void k_kick(KickArgs a) {
 
 }  // namespace
 
+// Fixed-point scale of the deposits: each weight w <= mass becomes the integer
+// w*2^s < 2^31 with the largest such s, so a 32-bit atomic adds it (64-bit
+// shared-memory atomics are several times slower); a second 32-bit counter per
+// mesh point takes the carries out of the first.
+int dep_shift(float mass) {
+  int s = 31;
+  float lim = 1.0f;
+  while (lim < mass && s > 1) {
+    lim *= 2.0f;
+    s--;
+  }
+  return s;
+}
+
 // -------------------------------------------------------------- init
 int cube_kernels_init(cube_ctx* c, const float* fine_table, const float* coarse_table) {
   int nf = c->nf, nc = c->p.nc, nfc = c->p.nf_cutoff;
@@ -511,7 +525,9 @@ int cube_fine_density_impl(cube_ctx* c, cube_stats* st) {
   cudaStream_t s = c->stream;
   Geo g = make_geo(c);
   CUBE_CUDA(c, cudaMemsetAsync(c->dstats, 0, sizeof(DevStats), s));
-  DepArgs a{g, c->xp[c->cur], c->rhoc[c->cur], c->cstart[c->cur], c->p.mass_p, c->rho_f, &c->dstats->rhof_fix, 0};
+  const int sh = dep_shift(c->p.mass_p);
+  DepArgs a{g, c->xp[c->cur], c->rhoc[c->cur], c->cstart[c->cur], c->p.mass_p, c->rho_f, &c->dstats->rhof_fix, 0,
+            std::ldexp(1.0f, sh), std::ldexp(1.0f, -sh)};
   cube_phase_begin(c, PH_F_DEPOSIT);
   int r = launch_deposit<4, 8, 4, 4, 1, 0>(c, a);
   cube_phase_end(c, PH_F_DEPOSIT);
@@ -519,7 +535,7 @@ int cube_fine_density_impl(cube_ctx* c, cube_stats* st) {
   if (st) {
     r = cube_stats_fetch(c);
     if (r) return r;
-    st->testrhof = (double)c->hstats->rhof_fix / kFixScale;
+    st->testrhof = std::ldexp((double)c->hstats->rhof_fix, -dep_shift(c->p.mass_p));
   }
   return CUBE_OK;
 }
@@ -554,7 +570,7 @@ int cube_fine_forces_impl(cube_ctx* c, cube_stats* st, const float* pre) {
     int r = cube_stats_fetch(c);
     if (r) return r;
     st->f2_max_fine = bits_float(c->hstats->f2_fine_bits);
-    st->testrhof = (double)c->hstats->rhof_fix / kFixScale;
+    st->testrhof = std::ldexp((double)c->hstats->rhof_fix, -dep_shift(c->p.mass_p));
   }
   return CUBE_OK;
 }
@@ -592,7 +608,9 @@ int cube_fine_kick_impl(cube_ctx* c, float a_mid, float dt, bool pre) {
 // power spectrum, mass 1 per particle (cicpower.f90:79,100-133), into the
 // padded mesh rho; *total receives the exact fixed-point sum.
 int cube_pk_deposit(cube_ctx* c, int ng, float* rho, unsigned long long* total) {
-  DepArgs a{make_geo(c), c->xp[c->cur], c->rhoc[c->cur], c->cstart[c->cur], 1.0f, rho, total, ng};
+  const int sh = dep_shift(1.0f);
+  DepArgs a{make_geo(c), c->xp[c->cur], c->rhoc[c->cur], c->cstart[c->cur], 1.0f, rho, total, ng,
+            std::ldexp(1.0f, sh), std::ldexp(1.0f, -sh)};
   int nc = c->p.nc;
   if (ng == nc) return launch_deposit<1, 8, 8, 8, 1, 1, true>(c, a);
   if (ng == 2 * nc) return launch_deposit<2, 8, 8, 4, 1, 1, true>(c, a);
@@ -605,7 +623,9 @@ int cube_coarse_density_impl(cube_ctx* c, cube_stats* st) {
   Geo g = make_geo(c);
   CUBE_CUDA(c, cudaMemsetAsync(&c->dstats->f2_coarse_bits, 0, 4, c->stream));
   CUBE_CUDA(c, cudaMemsetAsync(&c->dstats->rhoc_fix, 0, 8, c->stream));
-  DepArgs a{g, c->xp[c->cur], c->rhoc[c->cur], c->cstart[c->cur], c->p.mass_p, c->rho_c, &c->dstats->rhoc_fix, 0};
+  const int sh = dep_shift(c->p.mass_p);
+  DepArgs a{g, c->xp[c->cur], c->rhoc[c->cur], c->cstart[c->cur], c->p.mass_p, c->rho_c, &c->dstats->rhoc_fix, 0,
+            std::ldexp(1.0f, sh), std::ldexp(1.0f, -sh)};
   cube_phase_begin(c, PH_C_DEPOSIT);
   int r = launch_deposit<1, 8, 8, 8, 1, 1>(c, a);
   cube_phase_end(c, PH_C_DEPOSIT);
@@ -613,7 +633,7 @@ int cube_coarse_density_impl(cube_ctx* c, cube_stats* st) {
   if (st) {
     r = cube_stats_fetch(c);
     if (r) return r;
-    st->testrhoc = (double)c->hstats->rhoc_fix / kFixScale;
+    st->testrhoc = std::ldexp((double)c->hstats->rhoc_fix, -dep_shift(c->p.mass_p));
   }
   return CUBE_OK;
 }
@@ -643,7 +663,7 @@ int cube_coarse_forces_impl(cube_ctx* c, cube_stats* st, const float* pre) {
     int r = cube_stats_fetch(c);
     if (r) return r;
     st->f2_max_coarse = bits_float(c->hstats->f2_coarse_bits);
-    st->testrhoc = (double)c->hstats->rhoc_fix / kFixScale;
+    st->testrhoc = std::ldexp((double)c->hstats->rhoc_fix, -dep_shift(c->p.mass_p));
   }
   return CUBE_OK;
 }
@@ -710,7 +730,7 @@ int cube_coarse_kick_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st, bo
   if (st) {
     for (int d = 0; d < 3; d++) st->vmax[d] = vm[d];
     st->f2_max_coarse = bits_float(c->hstats->f2_coarse_bits);
-    st->testrhoc = (double)c->hstats->rhoc_fix / kFixScale;
+    st->testrhoc = std::ldexp((double)c->hstats->rhoc_fix, -dep_shift(c->p.mass_p));
   }
   return CUBE_OK;
 }
