@@ -68,7 +68,7 @@ struct cube_ctx {
   uint8_t* dframe = nullptr;    // frame of the primary copy: (ox+1)+3(oy+1)+9(oz+1), o in tiles
   uint8_t* doff = nullptr;      // cell offset source-destination of the primary copy, (dx+1)+3(dy+1)+9(dz+1); 255 if |d|>1
   uint16_t* lrank = nullptr;    // rank among the particles of one source cell bound for one destination
-  uint16_t* offc = nullptr;     // 27 per source cell: counts bound for each neighbour, then their base ranks
+  uint16_t* offc = nullptr;     // 27 planes over the source cells: counts bound for each neighbour, then base ranks
   int32_t* perm = nullptr;      // new position -> old particle index
   uint32_t* rank = nullptr;     // rank of the primary copy in its destination
   int4* xtra = nullptr;         // extra copies: (particle, dest cell, rank, -)

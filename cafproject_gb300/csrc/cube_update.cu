@@ -40,7 +40,7 @@ struct UpdArgs {
   uint8_t* dframe;
   uint8_t* doff;
   uint16_t* lrank;
-  uint16_t* offc;
+  uint16_t* offc;    // [o * ncells + S]: per neighbour o, one plane over the source cells
   int32_t* perm;
   uint32_t* rank;
   int4* xtra;
@@ -155,6 +155,7 @@ __global__ void k_dest(UpdArgs a) {
     int ncopy = nval[0] * nval[1] * nval[2];
     if (ncopy == 0) {
       a.dest[p] = -1;
+      a.doff[p] = 255;
       atomicAdd(&a.st->nlost, 1ull);
       continue;
     }
@@ -248,49 +249,39 @@ __device__ __forceinline__ float vfield_quotient(float acc, uint32_t cnt, int ex
 // inverse permutation; per destination, vfield_new summed in rank order, i.e.
 // the reference's visit order.
 constexpr int NOFF = 27;
-constexpr int RL_T = 256;
 
-// one warp per source cell: its particles in chunks of 32 lanes; lanes bound
-// for the same neighbour are grouped with a match, their order inside the
-// group is their lane order (= storage order), and the group leader advances
-// that neighbour's running count (held by lane o of the warp's counters)
-__global__ void __launch_bounds__(RL_T) k_rank_local(UpdArgs a) {
-  __shared__ uint32_t cnt[RL_T / 32][32];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+// one thread per particle: its rank among the earlier particles of its cell
+// bound for the same neighbour (storage order); the last of them also writes
+// that neighbour's count (the counts start at zero).  Cells denser than
+// RL_MAX particles are left to the walker.
+constexpr int RL_MAX = 2048;
+
+__global__ void k_rank_local(UpdArgs a) {
   if (a.st->max_disp > 1 || a.st->ndup_list != 0) {
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&a.st->flags, 8);  // not eligible
     return;
   }
-  const unsigned lt = (1u << lane) - 1u;
-  const int64_t nw = (int64_t)gridDim.x * (RL_T / 32);
-  for (int64_t S = (int64_t)blockIdx.x * (RL_T / 32) + w; S < a.ncells; S += nw) {
-    cnt[w][lane] = 0u;
-    __syncwarp();
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.np; p += (int64_t)gridDim.x * blockDim.x) {
+    const int o = a.doff[p];
+    if (o == 255) {
+      if (a.dest[p] >= 0) atomicOr(&a.st->flags, 4);  // moved farther than one cell
+      continue;
+    }
+    const int64_t S = a.pcell[p];
     const int64_t p0 = a.cstart[S], p1 = a.cstart[S + 1];
-    for (int64_t q = p0; q < p1; q += 32) {
-      const int64_t p = q + lane;
-      int o = 255;
-      if (p < p1 && a.dest[p] >= 0) {
-        o = a.doff[p];
-        if (o >= NOFF) atomicOr(&a.st->flags, 4);  // moved farther than one cell
-      }
-      const unsigned m = __match_any_sync(0xffffffffu, o);
-      const bool mine = o < NOFF;
-      uint32_t c = mine ? cnt[w][o] + (uint32_t)__popc(m & lt) : 0u;
-      if (mine) {
-        if (c > 0xffffu) atomicOr(&a.st->flags, 4);
-        a.lrank[p] = (uint16_t)c;
-      }
-      __syncwarp();
-      if (mine && (m & lt) == 0u) cnt[w][o] += (uint32_t)__popc(m);
-      __syncwarp();
+    if (p1 - p0 > RL_MAX) {
+      atomicOr(&a.st->flags, 4);
+      continue;
     }
-    if (lane < NOFF) {
-      uint32_t c = cnt[w][lane];
-      if (c > 0xffffu) atomicOr(&a.st->flags, 4);
-      a.offc[S * NOFF + lane] = (uint16_t)c;
+    int r = 0;
+    bool last = true;
+    for (int64_t q = p0; q < p1; q++) {
+      if (a.doff[q] != o || q == p) continue;
+      if (q < p) r++;
+      else last = false;
     }
-    __syncwarp();
+    a.lrank[p] = (uint16_t)r;
+    if (last) a.offc[o * a.ncells + S] = (uint16_t)(r + 1);
   }
 }
 
@@ -318,7 +309,7 @@ __global__ void k_rank_base(UpdArgs a) {
         for (int dx = -1; dx <= 1; dx++) {
           const int o = (dx + 1) + 3 * (dy + 1) + 9 * (dz + 1);
           sid[o] = (uint32_t)cell_id(g, glob(g, T[0], Dl[0] + dx), sy, sz);
-          c[o] = a.offc[(int64_t)sid[o] * NOFF + o];
+          c[o] = a.offc[o * a.ncells + sid[o]];
         }
       }
     }
@@ -353,7 +344,7 @@ __global__ void k_rank_base(UpdArgs a) {
 #pragma unroll
       for (int k = 0; k < 9; k++) {
         const int o = 9 * z + k;
-        a.offc[(int64_t)sid[o] * NOFF + o] = (uint16_t)b;
+        a.offc[o * a.ncells + sid[o]] = (uint16_t)b;
         b += c[o];
       }
     }
@@ -365,7 +356,7 @@ __global__ void k_rank_place(UpdArgs a) {
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.np; p += (int64_t)gridDim.x * blockDim.x) {
     int32_t D = a.dest[p];
     if (D < 0) continue;
-    uint32_t r = (uint32_t)a.offc[(int64_t)a.pcell[p] * NOFF + a.doff[p]] + a.lrank[p];
+    uint32_t r = (uint32_t)a.offc[a.doff[p] * a.ncells + a.pcell[p]] + a.lrank[p];
     a.rank[p] = r;
     if (r < (uint32_t)a.cnt_new[D]) a.perm[a.cstart_new[D] + r] = (int32_t)p;
     else atomicOr(&a.st->flags, 2);
@@ -645,7 +636,8 @@ int cube_update_x_impl(cube_ctx* c, float dt_old, float dt, float vz_max, cube_s
   if (walker) {
     k_rank<<<cube_grid(c->ncells, 128, 32), 128, 0, c->stream>>>(a);
   } else {
-    k_rank_local<<<cube_grid(c->ncells, RL_T / 32, 8), RL_T, 0, c->stream>>>(a);
+    CUBE_CUDA(c, cudaMemsetAsync(c->offc, 0, sizeof(uint16_t) * NOFF * (size_t)c->ncells, c->stream));
+    k_rank_local<<<cube_grid(c->np, 256), 256, 0, c->stream>>>(a);
     k_rank_base<<<cube_grid(c->ncells, 256), 256, 0, c->stream>>>(a);
   }
   cube_phase_end(c, PH_UPD_RANK);
