@@ -151,13 +151,13 @@ class ClockSampler:
 # particle counts scale together between 256^3 and 512^3, so per-particle
 # traffic carries over
 TRAFFIC_PER_PARTICLE = {
-    "pp_force": (178.7e6 + 53.3e6) / 16778347,
-    "fine_kick": (2033.7e6 + 100.3e6) / 16778347,
+    "pp_force": (178.5e6 + 55.0e6) / 16778347,
+    "fine_kick": (2034.4e6 + 100.0e6) / 16778347,
+    "coarse_kick": (289.6e6 + 81.0e6) / 16778347,
     "fine_deposit": (84.1e6 + 480.1e6) / 16778347,
-    "update_dest": (243.8e6 + 65.9e6) / 16778347,
-    "update_scatter": (503.1e6 + 255.5e6) / 16778347,
+    "update_dest": (244.1e6 + 78.6e6) / 16778347,
+    "update_scatter": (502.9e6 + 255.8e6) / 16778347,
     "fine_green": (1347.6e6 + 1568.0e6) / 16778347,
-    "fine_f2max": (1617.4e6 + 4.0e6) / 16778347,
 }
 
 
@@ -182,10 +182,10 @@ def algorithmic_bytes(p, n):
         "fine_r2c": 4 * nf3 + 8 * hf,
         "fine_green": 8 * hf + 12 * hf + 3 * 8 * hf,
         "fine_c2r": 3 * (8 * hf + 4 * nf3),
-        "fine_f2max": 12 * nf3,
+        "fine_f2max": 12 * nf3 + 12 * nf3,                 # maxima, then the kick factors written back
         "fine_kick": n * (3 * p.izipx + 2 * 3 * p.izipv + 4) + 12 * nf3,
         "coarse_deposit": n * (3 * p.izipx + 4) + 4 * nc3,
-        "coarse_fft": (4 * nc3 + 8 * hc) + (8 * hc + 12 * hc + 24 * hc) + 3 * (8 * hc + 4 * nc3) + 12 * nc3,
+        "coarse_fft": (4 * nc3 + 8 * hc) + (8 * hc + 12 * hc + 24 * hc) + 3 * (8 * hc + 4 * nc3) + 24 * nc3,
         "coarse_kick": n * (3 * p.izipx + 2 * 3 * p.izipv + 4 + 12) + 12 * nc3,
     }
 
