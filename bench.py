@@ -316,12 +316,12 @@ def run_gb300(args, ws, rank, lrank):
 
 def gpu_launches(p, steps):
     """Launches of this library's kernels per step (cuFFT kernels not counted)."""
-    upd = 2 + 3 + 1 + 1        # dest, rank, scan x3, scatter, sigma
-    pp = 3 if p.pp_on else 0   # staged bricks, staged cells, dense cells
-    fine = 1 + 1 + 1 + 1       # deposit, green, f2max, kick
-    coarse = 1 + 1 + 1 + 1
-    dec = 1                    # decode table when sigma changes
-    return steps * (upd + pp + fine + coarse + dec)
+    upd = 1 + 2 + 3 + 2 + 1 + 1  # dest, counting ranks (2), scan (3), place + vfield, scatter, sigma
+    pp = 3 if p.pp_on else 0     # staged bricks, staged cells, dense cells
+    fine = 4                     # deposit, green, maxima + kick factors, kick
+    coarse = 4
+    codec = 2                    # decode table and encode boundaries for the new sigma
+    return steps * (upd + pp + fine + coarse + codec)
 
 
 def cpu_baseline(p, state, sigma, ts):
