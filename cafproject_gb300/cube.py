@@ -32,7 +32,7 @@ EXPORTS = ["cube_create", "cube_destroy", "cube_last_error", "cube_upload_state"
            "cube_pm_coarse_forces", "cube_pm_coarse_kick", "cube_get_field", "cube_set_field", "cube_nplocal",
            "cube_synchronize", "cube_timing", "cube_timing_read", "cube_phase_name", "cube_stream",
            "cube_codec_check", "cube_codec_check_static", "cube_arith_check", "cube_pk_nbin",
-           "cube_power_spectrum", "cube_checkpoint_write", "cube_checkpoint_read", "cube_set_option"]
+           "cube_power_spectrum", "cube_checkpoint_write", "cube_checkpoint_read", "cube_ic_zeldovich", "cube_set_option"]
 CODEC_STATIC_MAX = 16384
 OPT_EXACT_KICKS = 1
 OPT_PP_LEVEL = 2
@@ -44,6 +44,14 @@ class CubeError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__("%s: %s" % (STATUS.get(code, code), msg))
         self.code = code
+
+
+class Cosmology(ctypes.Structure):
+    """ctypes image of ``cube_cosmology``."""
+
+    _fields_ = [("box", ctypes.c_float), ("omega_m", ctypes.c_float), ("omega_l", ctypes.c_float),
+                ("h0", ctypes.c_float), ("s8", ctypes.c_float), ("n_s", ctypes.c_float), ("omega_b", ctypes.c_float),
+                ("np_nc", ctypes.c_int32)]
 
 
 class SimHeader(ctypes.Structure):
@@ -133,6 +141,7 @@ def load_library(path=None):
     L.cube_power_spectrum.argtypes = [P, ctypes.c_int, F, P, P, ctypes.c_int]
     L.cube_checkpoint_write.argtypes = [P, ctypes.c_char_p, F, ctypes.c_int, P]
     L.cube_checkpoint_read.argtypes = [P, ctypes.c_char_p, F, ctypes.c_int, P]
+    L.cube_ic_zeldovich.argtypes = [P, P, F, ctypes.c_uint32, P, P]
     L.cube_set_option.argtypes = [P, ctypes.c_int, I64]
     _lib = L
     return L
@@ -295,6 +304,19 @@ class CubeGPU:
         b = np.empty(v.size, np.int32)
         self._check(self.L.cube_codec_check(self.h, float(sigma), _ptr(v), v.size, _ptr(a), _ptr(b)))
         return a, b
+
+    def ic_zeldovich(self, z_init, seed, omega_b=0.045):
+        """Zel'dovich initial conditions generated on the device into this
+        context (cosmology and particle grid from the context's parameters);
+        returns (sigma_vi, vmax[3])."""
+        p = self.p
+        cs = Cosmology(box=p.box, omega_m=p.omega_m, omega_l=p.omega_l, h0=p.h0, s8=p.s8, n_s=p.n_s,
+                       omega_b=omega_b, np_nc=p.np_nc)
+        sig = ctypes.c_float()
+        vm = (ctypes.c_float * 3)()
+        self._check(self.L.cube_ic_zeldovich(self.h, ctypes.byref(cs), float(z_init), int(seed) & 0xFFFFFFFF,
+                                             ctypes.byref(sig), vm))
+        return np.float32(sig.value), [float(v) for v in vm]
 
     def checkpoint_write(self, directory, z, image=1, **header):
         """checkpoint (checkpoint.f90): the reference's files for this image;

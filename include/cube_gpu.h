@@ -111,6 +111,14 @@ typedef struct cube_sim_header {
   float vz_max;
 } cube_sim_header;
 
+/* Cosmology and particle grid of the initial conditions. */
+typedef struct cube_cosmology {
+  float box;       /* Mpc/h */
+  float omega_m, omega_l, h0, s8, n_s;
+  float omega_b;   /* baryon fraction of the Eisenstein-Hu no-wiggle shape */
+  int32_t np_nc;   /* particles per coarse cell per dimension */
+} cube_cosmology;
+
 typedef struct cube_ctx cube_ctx;
 
 /* Fields for inspection / injection in parity tests. */
@@ -150,6 +158,15 @@ int cube_download_state(cube_ctx* ctx, int64_t* nplocal, void* xp, void* vp, int
    sets sigma_vi and returns the header in hdr (may be NULL). */
 int cube_checkpoint_write(cube_ctx* ctx, const char* dir, float z, int image, const cube_sim_header* hdr);
 int cube_checkpoint_read(cube_ctx* ctx, const char* dir, float z, int image, cube_sim_header* hdr);
+
+/* Zel'dovich initial conditions generated on the device into the context's
+   state (initial_conditions.f90:250-825, with an Eisenstein-Hu no-wiggle
+   transfer function and a counter-hash white noise): (nc*np_nc)^3 particles
+   at z_init in the compressed layout, particles of a cell in Lagrangian order.
+   Returns sigma_vi (also set in the context) and the largest |v| per
+   dimension.  Uses the fine-mesh buffers as scratch. */
+int cube_ic_zeldovich(cube_ctx* ctx, const cube_cosmology* cosmo, float z_init, uint32_t seed, float* sigma_vi,
+                      float* vmax);
 
 /* sigma_vi / sigma_vi_new module variables (variables.f90:36). */
 int cube_set_sigma(cube_ctx* ctx, float sigma_vi, float sigma_vi_new);
