@@ -50,7 +50,7 @@ static void release(cube_ctx* c) {
                   c->vfield[0], c->vfield[1], c->cstart[0], c->cstart[1], c->dest, c->dframe, c->doff, c->lrank, c->offc, c->perm, c->rank, c->xtra,
                   c->scan_tmp, c->red_tmp, c->tan_tab, c->codec[0].dec, c->codec[1].dec, c->codec[0].bnd, c->codec[1].bnd, c->codec[0].dech, c->codec[1].dech, c->rho_f, c->force_f[0],
                   c->force_f[1], c->force_f[2], c->kern_f, c->kern_f_raw, c->rho_c, c->force_c[0],
-                  c->force_c[1], c->force_c[2], c->kern_c, c->fpp, c->pp_ovf_brick, c->pp_ovf_cell, c->pp_novf, c->dstats,
+                  c->force_c[1], c->force_c[2], c->kern_c, c->fpp, c->pp_ovf_brick, c->pp_ovf_cell, c->pp_ovf_cell2, c->pp_novf, c->dstats,
                   c->cufft_work};
   for (void* b : bufs)
     if (b) cudaFree(b);
@@ -167,9 +167,10 @@ extern "C" int cube_create(const cube_params* p, const float* fine_table, const 
     c->pp_brick_cap = nb * nb * nb;
     ALLOC(c->pp_ovf_brick, 4 * (size_t)c->pp_brick_cap);
     ALLOC(c->pp_ovf_cell, 4 * (size_t)c->ncells);
-    ALLOC(c->pp_novf, 8);
-    CUBE_CUDA(c, cudaMallocHost((void**)&c->pp_novf_host, 8));
-    c->pp_novf_host[0] = c->pp_novf_host[1] = 0;
+    ALLOC(c->pp_ovf_cell2, 4 * (size_t)c->ncells);
+    ALLOC(c->pp_novf, 16);
+    CUBE_CUDA(c, cudaMallocHost((void**)&c->pp_novf_host, 16));
+    c->pp_novf_host[0] = c->pp_novf_host[1] = c->pp_novf_host[2] = 0;
   }
   ALLOC(c->dstats, sizeof(DevStats));
   CUBE_CUDA(c, cudaMallocHost((void**)&c->hstats, sizeof(DevStats)));
@@ -299,7 +300,7 @@ extern "C" int cube_set_option(cube_ctx* c, int option, int64_t value) {
       c->opt_rank_walk = value ? 1 : 0;
       return CUBE_OK;
     case CUBE_OPT_PP_LEVEL:
-      if (value < 0 || value > 2) return cube_fail(c, CUBE_ERR_ARG, "PP level must be 0, 1 or 2");
+      if (value < 0 || value > 3) return cube_fail(c, CUBE_ERR_ARG, "PP level must be 0, 1, 2 or 3");
       c->opt_pp_level = (int)value;
       return CUBE_OK;
     default:

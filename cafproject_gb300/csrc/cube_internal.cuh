@@ -92,7 +92,7 @@ struct cube_ctx {
   int opt_exact_kicks = 0;
   int opt_rank_walk = 0;   // force the general visit-order rank walker
   int rank_walked = 0;     // the last update used the walker
-  int opt_pp_level = 0;  // first PP level (0 bricks, 1 single cells, 2 global memory)
+  int opt_pp_level = 0;  // first PP level (0 bricks, 1 single cells, 2 large cell blocks, 3 global memory)
   // fine PM
   cufftHandle plan_f_r2c = 0, plan_f_c2r = 0;
   float* rho_f = nullptr;       // padded real / complex in place
@@ -107,8 +107,9 @@ struct cube_ctx {
   // PP
   float* fpp = nullptr;         // optional per-particle PP force (3*np), debug only
   int* pp_ovf_brick = nullptr;      // bricks too dense to stage (ceil(nc/4)^3 entries)
-  int* pp_ovf_cell = nullptr;       // cells too dense to stage (nc^3 entries)
-  int* pp_novf = nullptr;           // [0] listed bricks, [1] listed cells
+  int* pp_ovf_cell = nullptr;       // cells too dense for a small staging block (nc^3 entries)
+  int* pp_ovf_cell2 = nullptr;      // cells too dense to stage at all (nc^3 entries)
+  int* pp_novf = nullptr;           // [0] listed bricks, [1] listed cells, [2] cells for global memory
   int* pp_novf_host = nullptr;      // pinned copy of the last call's counts
   int pp_brick_cap = 0;             // ceil(nc/4)^3
   // per-phase timers (null when disabled)

@@ -16,11 +16,13 @@
 // kernel handles a particle).
 //
 // Three levels keep dense regions correct without a host round trip:
-//   0. one CTA per brick of 4^3 coarse cells;
-//   1. bricks whose staged set exceeds PP_CAP are listed and redone one coarse
-//      cell at a time (persistent CTAs walking the list);
-//   2. cells still too dense are listed and done from global memory, one CTA
-//      per cell.
+//   0. one CTA per brick of 4^3 coarse cells, 1536 staged particles at most
+//      (several CTAs per SM);
+//   1. bricks over that are listed and redone one coarse cell at a time, the
+//      same capacity per cell;
+//   2. cells over that are redone by one 1024-thread CTA per SM with 8960
+//      staged particles of room;
+//   3. cells still too dense are done from global memory, one CTA per cell.
 // The kick adds F*a_mid*dt/(6 pi) in FP64 as one product with the precomputed
 // factor -- the FP32 pair sum already sets this kick's tolerance against the
 // reference's FP64 sum -- and the velocity code is the exact code of
@@ -36,11 +38,20 @@ constexpr int PS_MAX = PB + 2;                 // staged coarse cells per edge
 constexpr int PNS_MAX = PS_MAX * PS_MAX * PS_MAX;
 constexpr int PNCORE_MAX = PB * PB * PB;
 constexpr int PNF_MAX = (4 * PB + 2) * (4 * PB + 2) * (4 * PB + 2);
-constexpr int PP_CAP = 1536;                   // staged particles per block
+constexpr int PP_CAP = 1536;      // staged particles per brick (several blocks per SM)
+constexpr int PP_CAP1 = 8960;     // staged particles per single cell (one block per SM)
 constexpr int PP_THREADS = 256;
-constexpr size_t PP_SMEM = (sizeof(float4) + sizeof(unsigned) + sizeof(unsigned short)) * PP_CAP +
-                           sizeof(unsigned short) * (PNF_MAX + 2);
-static_assert(PP_CAP < 65536, "bin offsets are 16-bit");
+constexpr int PP_THREADS1 = 1024;
+constexpr int PNF1 = 6 * 6 * 6;   // staged fine cells of one coarse cell and its ring
+// shared memory of one block: staged points, bin/rank words, slots by bin, 16-bit bin offsets
+constexpr size_t pp_smem(int cap, int nf) {
+  return (sizeof(float4) + sizeof(unsigned) + sizeof(unsigned short)) * (size_t)cap +
+         sizeof(unsigned short) * (size_t)(nf + 2);
+}
+constexpr size_t PP_SMEM = pp_smem(PP_CAP, PNF_MAX);
+constexpr size_t PP_SMEM1 = pp_smem(PP_CAP1, PNF1);
+static_assert(PP_CAP1 < 65536 && PP_CAP1 < (1 << 19), "slots are 16-bit, ranks fit 19 bits");
+static_assert(PP_SMEM1 + 4096 < 227 * 1024, "the single-cell block fits the shared memory of an SM");
 
 struct PPArgs {
   Geo g;
@@ -57,8 +68,9 @@ struct PPArgs {
   float* fpp;    // optional per-particle force output
   int nb;        // bricks per dimension
   int* ovf_brick;  // level-1 list: bricks too dense to stage
-  int* ovf_cell;   // level-2 list: cells too dense to stage
-  int* novf;       // [0] listed bricks, [1] listed cells
+  int* ovf_cell;   // level-2 list: cells too dense for a small block
+  int* ovf_cell2;  // level-3 list: cells too dense to stage at all
+  int* novf;       // [0] listed bricks, [1] listed cells, [2] cells for global memory
   DevStats* st;
 };
 
@@ -161,16 +173,17 @@ struct PPAcc {
 // particle of the block then walks its 27 neighbouring fine-cell bins.
 // Returns false (nothing kicked) when more than PP_CAP particles would be
 // staged.  Block-uniform control flow; ends with a barrier.
+template <int CAP>
 __device__ bool pp_block(const PPArgs& a, const int C0[3], const int B[3], PPSmem& sm, float4* dyn, PPAcc& acc) {
   const Geo& g = a.g;
   const int nc = g.nc;
   const int S0 = B[0] + 2, S1 = B[1] + 2, S2 = B[2] + 2, NS = S0 * S1 * S2;
   const int F0 = 4 * B[0] + 2, F1 = 4 * B[1] + 2, F2 = 4 * B[2] + 2, NF = F0 * F1 * F2;
   float4* pts = dyn;                                              // x, y, z, particle index
-  unsigned* kinfo = reinterpret_cast<unsigned*>(pts + PP_CAP);    // bin | rank in bin << 13
-  unsigned short* order = reinterpret_cast<unsigned short*>(kinfo + PP_CAP);  // slots by bin
+  unsigned* kinfo = reinterpret_cast<unsigned*>(pts + CAP);    // bin | rank in bin << 13
+  unsigned short* order = reinterpret_cast<unsigned short*>(kinfo + CAP);  // slots by bin
   // NF+1 16-bit bin offsets, counted two to a 32-bit word
-  unsigned short* bins = order + PP_CAP;
+  unsigned short* bins = order + CAP;
   unsigned* bins32 = reinterpret_cast<unsigned*>(bins);
   for (int t = threadIdx.x; t < NS; t += blockDim.x) {
     int sx = t % S0, sy = (t / S0) % S1, sz = t / (S0 * S1);
@@ -196,7 +209,7 @@ __device__ bool pp_block(const PPArgs& a, const int C0[3], const int B[3], PPSme
     }
     if (!in) return;
     int slot = atomicAdd(&sm.nst, 1);
-    if (slot >= PP_CAP) return;
+    if (slot >= CAP) return;
     int f = fi[0] + F0 * (fi[1] + F1 * fi[2]);
     const unsigned sh = 16u * (unsigned)(f & 1);
     int r = (int)((atomicAdd(&bins32[f >> 1], 1u << sh) >> sh) & 0xffffu);
@@ -205,7 +218,7 @@ __device__ bool pp_block(const PPArgs& a, const int C0[3], const int B[3], PPSme
   });
   __syncthreads();
   const int nst = sm.nst;
-  if (nst > PP_CAP) return false;
+  if (nst > CAP) return false;
   block_exclusive_scan_u16(bins, NF);
   if (threadIdx.x == 0) bins[NF] = (unsigned short)nst;
   for (int t = threadIdx.x; t < nst; t += blockDim.x) {
@@ -246,7 +259,7 @@ __global__ void __launch_bounds__(PP_THREADS) k_pp_bricks(PPArgs a) {
   int C0[3] = {(b % a.nb) * PB, ((b / a.nb) % a.nb) * PB, (b / (a.nb * a.nb)) * PB};
   int B[3] = {min(PB, nc - C0[0]), min(PB, nc - C0[1]), min(PB, nc - C0[2])};
   PPAcc acc;
-  if (!pp_block(a, C0, B, sm, pts, acc) && threadIdx.x == 0) a.ovf_brick[atomicAdd(&a.novf[0], 1)] = b;
+  if (!pp_block<PP_CAP>(a, C0, B, sm, pts, acc) && threadIdx.x == 0) a.ovf_brick[atomicAdd(&a.novf[0], 1)] = b;
   pp_reduce(a, acc.npairs, acc.nwork, acc.f2max);
 }
 
@@ -264,7 +277,7 @@ __global__ void __launch_bounds__(PP_THREADS) k_pp_cells(PPArgs a) {
                  (b / (a.nb * a.nb)) * PB + l / (PB * PB)};
     if (C0[0] >= nc || C0[1] >= nc || C0[2] >= nc) continue;
     const int B[3] = {1, 1, 1};
-    if (!pp_block(a, C0, B, sm, pts, acc)) {
+    if (!pp_block<PP_CAP>(a, C0, B, sm, pts, acc)) {
       if (threadIdx.x == 0) a.ovf_cell[atomicAdd(&a.novf[1], 1)] = (int)cell_id(g, C0[0], C0[1], C0[2]);
       __syncthreads();
     }
@@ -272,13 +285,32 @@ __global__ void __launch_bounds__(PP_THREADS) k_pp_cells(PPArgs a) {
   pp_reduce(a, acc.npairs, acc.nwork, acc.f2max);
 }
 
-// level 2: listed cells from global memory, one CTA per cell (persistent)
-__global__ void __launch_bounds__(PP_THREADS) k_pp_dense(PPArgs a) {
+// level 2: listed cells with a large staging area, one 1024-thread block per SM
+__global__ void __launch_bounds__(PP_THREADS1) k_pp_bigcells(PPArgs a) {
+  __shared__ PPSmem sm;
+  extern __shared__ float4 pts[];
   const Geo& g = a.g;
   const int n = a.novf[1];
   PPAcc acc;
   for (int it = blockIdx.x; it < n; it += gridDim.x) {
-    int64_t c = a.ovf_cell[it];
+    int gc[3];
+    cell_coords(g, a.ovf_cell[it], gc[0], gc[1], gc[2]);
+    const int B[3] = {1, 1, 1};
+    if (!pp_block<PP_CAP1>(a, gc, B, sm, pts, acc)) {
+      if (threadIdx.x == 0) a.ovf_cell2[atomicAdd(&a.novf[2], 1)] = a.ovf_cell[it];
+      __syncthreads();
+    }
+  }
+  pp_reduce(a, acc.npairs, acc.nwork, acc.f2max);
+}
+
+// level 3: listed cells from global memory, one CTA per cell (persistent)
+__global__ void __launch_bounds__(PP_THREADS) k_pp_dense(PPArgs a) {
+  const Geo& g = a.g;
+  const int n = a.novf[2];
+  PPAcc acc;
+  for (int it = blockIdx.x; it < n; it += gridDim.x) {
+    int64_t c = a.ovf_cell2[it];
     int gc[3];
     cell_coords(g, c, gc[0], gc[1], gc[2]);
     int64_t p1 = a.cstart[c + 1];
@@ -350,26 +382,32 @@ int cube_pp_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st) {
   if (nbrick > c->pp_brick_cap) return cube_fail(c, CUBE_ERR_ARG, "PP brick list too small");
   a.ovf_brick = c->pp_ovf_brick;
   a.ovf_cell = c->pp_ovf_cell;
+  a.ovf_cell2 = c->pp_ovf_cell2;
   a.novf = c->pp_novf;
-  CUBE_CUDA(c, cudaMemsetAsync(c->pp_novf, 0, 2 * sizeof(int), c->stream));
-  for (auto k : {k_pp_bricks, k_pp_cells})
-    CUBE_CUDA(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PP_SMEM));
+  CUBE_CUDA(c, cudaMemsetAsync(c->pp_novf, 0, 3 * sizeof(int), c->stream));
+  CUBE_CUDA(c, cudaFuncSetAttribute(k_pp_bricks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PP_SMEM));
+  CUBE_CUDA(c, cudaFuncSetAttribute(k_pp_cells, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PP_SMEM));
+  CUBE_CUDA(c, cudaFuncSetAttribute(k_pp_bigcells, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PP_SMEM1));
   int persist = cube_grid((int64_t)1 << 40, 1, 4);
   cube_phase_begin(c, PH_PP);
   if (c->opt_pp_level == 1) {
     k_pp_list_all<<<cube_grid(nbrick, 256), 256, 0, c->stream>>>(c->pp_ovf_brick, (int)nbrick, c->pp_novf);
   } else if (c->opt_pp_level == 2) {
     k_pp_list_all<<<cube_grid(c->ncells, 256), 256, 0, c->stream>>>(c->pp_ovf_cell, (int)c->ncells, c->pp_novf + 1);
+  } else if (c->opt_pp_level == 3) {
+    k_pp_list_all<<<cube_grid(c->ncells, 256), 256, 0, c->stream>>>(c->pp_ovf_cell2, (int)c->ncells, c->pp_novf + 2);
   } else {
     k_pp_bricks<<<(unsigned)nbrick, PP_THREADS, PP_SMEM, c->stream>>>(a);
   }
   CUBE_CUDA(c, cudaGetLastError());
   k_pp_cells<<<persist, PP_THREADS, PP_SMEM, c->stream>>>(a);
   CUBE_CUDA(c, cudaGetLastError());
+  k_pp_bigcells<<<cube_grid((int64_t)1 << 40, 1, 1), PP_THREADS1, PP_SMEM1, c->stream>>>(a);
+  CUBE_CUDA(c, cudaGetLastError());
   k_pp_dense<<<persist, PP_THREADS, 0, c->stream>>>(a);
   CUBE_CUDA(c, cudaGetLastError());
   cube_phase_end(c, PH_PP);
-  CUBE_CUDA(c, cudaMemcpyAsync(c->pp_novf_host, c->pp_novf, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CUBE_CUDA(c, cudaMemcpyAsync(c->pp_novf_host, c->pp_novf, 3 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   r = cube_stats_fetch(c);
   if (r) return r;
   if ((int64_t)c->hstats->itest1 != c->np)
