@@ -50,12 +50,12 @@ static void release(cube_ctx* c) {
                   c->vfield[0], c->vfield[1], c->cstart[0], c->cstart[1], c->dest, c->dframe, c->doff, c->lrank, c->offc, c->perm, c->rank, c->xtra,
                   c->scan_tmp, c->red_tmp, c->tan_tab, c->codec[0].dec, c->codec[1].dec, c->codec[0].bnd, c->codec[1].bnd, c->codec[0].dech, c->codec[1].dech, c->rho_f, c->force_f[0],
                   c->force_f[1], c->force_f[2], c->kern_f, c->kern_f_raw, c->rho_c, c->force_c[0],
-                  c->force_c[1], c->force_c[2], c->kern_c, c->fpp, c->pp_ovf_brick, c->pp_ovf_cell, c->pp_ovf_cell2, c->pp_novf, c->dstats,
+                  c->force_c[1], c->force_c[2], c->kern_c, c->fpp, c->pp_list[0], c->pp_list[1], c->pp_list[2], c->pp_list[3], c->pp_nlist, c->dstats,
                   c->cufft_work};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (c->hstats) cudaFreeHost(c->hstats);
-  if (c->pp_novf_host) cudaFreeHost(c->pp_novf_host);
+  if (c->pp_nlist_host) cudaFreeHost(c->pp_nlist_host);
   if (c->plan_f_r2c) cufftDestroy(c->plan_f_r2c);
   if (c->plan_f_c2r) cufftDestroy(c->plan_f_c2r);
   if (c->plan_c_r2c) cufftDestroy(c->plan_c_r2c);
@@ -165,12 +165,13 @@ extern "C" int cube_create(const cube_params* p, const float* fine_table, const 
   {
     int nb = (p->nc + 3) / 4;
     c->pp_brick_cap = nb * nb * nb;
-    ALLOC(c->pp_ovf_brick, 4 * (size_t)c->pp_brick_cap);
-    ALLOC(c->pp_ovf_cell, 4 * (size_t)c->ncells);
-    ALLOC(c->pp_ovf_cell2, 4 * (size_t)c->ncells);
-    ALLOC(c->pp_novf, 16);
-    CUBE_CUDA(c, cudaMallocHost((void**)&c->pp_novf_host, 16));
-    c->pp_novf_host[0] = c->pp_novf_host[1] = c->pp_novf_host[2] = 0;
+    ALLOC(c->pp_list[0], 4 * (size_t)c->pp_brick_cap);
+    ALLOC(c->pp_list[1], 4 * (size_t)c->pp_brick_cap);
+    ALLOC(c->pp_list[2], 4 * (size_t)c->ncells);
+    ALLOC(c->pp_list[3], 4 * (size_t)c->ncells);
+    ALLOC(c->pp_nlist, 16);
+    CUBE_CUDA(c, cudaMallocHost((void**)&c->pp_nlist_host, 16));
+    for (int l = 0; l < 4; l++) c->pp_nlist_host[l] = 0;
   }
   ALLOC(c->dstats, sizeof(DevStats));
   CUBE_CUDA(c, cudaMallocHost((void**)&c->hstats, sizeof(DevStats)));
@@ -300,7 +301,7 @@ extern "C" int cube_set_option(cube_ctx* c, int option, int64_t value) {
       c->opt_rank_walk = value ? 1 : 0;
       return CUBE_OK;
     case CUBE_OPT_PP_LEVEL:
-      if (value < 0 || value > 3) return cube_fail(c, CUBE_ERR_ARG, "PP level must be 0, 1, 2 or 3");
+      if (value < 0 || value > 4) return cube_fail(c, CUBE_ERR_ARG, "PP level must be 0 to 4");
       c->opt_pp_level = (int)value;
       return CUBE_OK;
     default:

@@ -92,7 +92,7 @@ struct cube_ctx {
   int opt_exact_kicks = 0;
   int opt_rank_walk = 0;   // force the general visit-order rank walker
   int rank_walked = 0;     // the last update used the walker
-  int opt_pp_level = 0;  // first PP level (0 bricks, 1 single cells, 2 large cell blocks, 3 global memory)
+  int opt_pp_level = 0;  // first PP level (0-4)
   // fine PM
   cufftHandle plan_f_r2c = 0, plan_f_c2r = 0;
   float* rho_f = nullptr;       // padded real / complex in place
@@ -106,11 +106,9 @@ struct cube_ctx {
   float* kern_c = nullptr;      // scaled by 1/nc^3 (exact: power of two)
   // PP
   float* fpp = nullptr;         // optional per-particle PP force (3*np), debug only
-  int* pp_ovf_brick = nullptr;      // bricks too dense to stage (ceil(nc/4)^3 entries)
-  int* pp_ovf_cell = nullptr;       // cells too dense for a small staging block (nc^3 entries)
-  int* pp_ovf_cell2 = nullptr;      // cells too dense to stage at all (nc^3 entries)
-  int* pp_novf = nullptr;           // [0] listed bricks, [1] listed cells, [2] cells for global memory
-  int* pp_novf_host = nullptr;      // pinned copy of the last call's counts
+  int* pp_list[4] = {nullptr, nullptr, nullptr, nullptr};  // work of PP levels 1-4 (bricks, bricks, cells, cells)
+  int* pp_nlist = nullptr;          // their lengths
+  int* pp_nlist_host = nullptr;     // pinned copy of the last call's lengths
   int pp_brick_cap = 0;             // ceil(nc/4)^3
   // per-phase timers (null when disabled)
   struct CubeTimers* timers = nullptr;
@@ -409,13 +407,14 @@ __device__ __forceinline__ bool nint_certified(float xf, float E, long long* out
 // x/c correctly rounded, for a constant c with rc = RN(1/c): q = RN(x*rc), the
 // residual x - q*c is exact in one FMA, and q + residual*rc rounds to RN(x/c)
 // (Markstein's correction step, IBM J. Res. Dev. 34(1), 1990).  For c = 6 and
-// c = pi_f the identity with __fdiv_rn is checked for every float in the
-// window below by cube_arith_check; zeros, tiny, huge and non-finite x take
-// the IEEE division.
+// c = pi_f the identity with __fdiv_rn is checked for every float by
+// cube_arith_check; zeros keep their sign through the product, tiny, huge and
+// non-finite x take the IEEE division.
 constexpr float kDivLo = 7.888609052210118e-31f;  // 2^-100
 constexpr float kDivHi = 1.2676506002282294e30f;  // 2^100
 __device__ __forceinline__ float div_const(float x, float c, float rc) {
   float ax = fabsf(x);
+  if (ax == 0.f) return __fmul_rn(x, rc);
   if (!(ax >= kDivLo && ax <= kDivHi)) return __fdiv_rn(x, c);
   float q = __fmul_rn(x, rc);
   float r = __fmaf_rn(-q, c, x);

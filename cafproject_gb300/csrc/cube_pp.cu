@@ -15,14 +15,14 @@
 // sum does not depend on the visit order (bitwise reproducible whichever
 // kernel handles a particle).
 //
-// Three levels keep dense regions correct without a host round trip:
-//   0. one CTA per brick of 4^3 coarse cells, 1536 staged particles at most
-//      (several CTAs per SM);
-//   1. bricks over that are listed and redone one coarse cell at a time, the
-//      same capacity per cell;
-//   2. cells over that are redone by one 1024-thread CTA per SM with 8960
-//      staged particles of room;
-//   3. cells still too dense are done from global memory, one CTA per cell.
+// Five levels keep dense regions correct without a host round trip; each
+// level lists what did not fit for the next one:
+//   0. one block per brick of 4^3 coarse cells, 1536 staged particles at most
+//      (several blocks per SM);
+//   1. listed bricks again, one 1024-thread block per SM with 8960 of room;
+//   2. the cells of bricks listed by level 1, one at a time, 1536 of room;
+//   3. listed cells with 8960 of room;
+//   4. cells still too dense, from global memory, one block per cell.
 // The kick adds F*a_mid*dt/(6 pi) in FP64 as one product with the precomputed
 // factor -- the FP32 pair sum already sets this kick's tolerance against the
 // reference's FP64 sum -- and the velocity code is the exact code of
@@ -50,8 +50,9 @@ constexpr size_t pp_smem(int cap, int nf) {
 }
 constexpr size_t PP_SMEM = pp_smem(PP_CAP, PNF_MAX);
 constexpr size_t PP_SMEM1 = pp_smem(PP_CAP1, PNF1);
+constexpr size_t PP_SMEM1B = pp_smem(PP_CAP1, PNF_MAX);
 static_assert(PP_CAP1 < 65536 && PP_CAP1 < (1 << 19), "slots are 16-bit, ranks fit 19 bits");
-static_assert(PP_SMEM1 + 4096 < 227 * 1024, "the single-cell block fits the shared memory of an SM");
+static_assert(PP_SMEM1B + 4096 < 227 * 1024, "the large brick block fits the shared memory of an SM");
 
 struct PPArgs {
   Geo g;
@@ -67,10 +68,8 @@ struct PPArgs {
   int exact_only;
   float* fpp;    // optional per-particle force output
   int nb;        // bricks per dimension
-  int* ovf_brick;  // level-1 list: bricks too dense to stage
-  int* ovf_cell;   // level-2 list: cells too dense for a small block
-  int* ovf_cell2;  // level-3 list: cells too dense to stage at all
-  int* novf;       // [0] listed bricks, [1] listed cells, [2] cells for global memory
+  int* list[4];    // work of levels 1..4: bricks, bricks, cells, cells
+  int* nlist;      // their lengths
   DevStats* st;
 };
 
@@ -250,67 +249,57 @@ __device__ bool pp_block(const PPArgs& a, const int C0[3], const int B[3], PPSme
   return true;
 }
 
-// level 0: one CTA per 4^3 brick
-__global__ void __launch_bounds__(PP_THREADS) k_pp_bricks(PPArgs a) {
-  __shared__ PPSmem sm;
-  extern __shared__ float4 pts[];
-  const int nc = a.g.nc;
-  int b = blockIdx.x;
-  int C0[3] = {(b % a.nb) * PB, ((b / a.nb) % a.nb) * PB, (b / (a.nb * a.nb)) * PB};
-  int B[3] = {min(PB, nc - C0[0]), min(PB, nc - C0[1]), min(PB, nc - C0[2])};
-  PPAcc acc;
-  if (!pp_block<PP_CAP>(a, C0, B, sm, pts, acc) && threadIdx.x == 0) a.ovf_brick[atomicAdd(&a.novf[0], 1)] = b;
-  pp_reduce(a, acc.npairs, acc.nwork, acc.f2max);
-}
-
-// level 1: the cells of listed bricks, one at a time (persistent CTAs)
-__global__ void __launch_bounds__(PP_THREADS) k_pp_cells(PPArgs a) {
+// Levels 0-3: kLevel selects the work item of iteration it (a brick: its
+// index, or listed; a cell: of a listed brick, or listed) and where an item
+// that did not fit is listed.
+template <int kLevel, int CAP, int NT>
+__global__ void __launch_bounds__(NT) k_pp_level(PPArgs a) {
   __shared__ PPSmem sm;
   extern __shared__ float4 pts[];
   const Geo& g = a.g;
-  const int nc = g.nc;
-  const int n = a.novf[0] * PNCORE_MAX;
+  const int nc = g.nc, nb = a.nb;
+  const int n = kLevel == 0 ? nb * nb * nb
+                            : (kLevel == 2 ? a.nlist[1] * PNCORE_MAX : a.nlist[kLevel - 1]);
   PPAcc acc;
   for (int it = blockIdx.x; it < n; it += gridDim.x) {
-    int b = a.ovf_brick[it / PNCORE_MAX], l = it % PNCORE_MAX;
-    int C0[3] = {(b % a.nb) * PB + l % PB, ((b / a.nb) % a.nb) * PB + (l / PB) % PB,
-                 (b / (a.nb * a.nb)) * PB + l / (PB * PB)};
-    if (C0[0] >= nc || C0[1] >= nc || C0[2] >= nc) continue;
-    const int B[3] = {1, 1, 1};
-    if (!pp_block<PP_CAP>(a, C0, B, sm, pts, acc)) {
-      if (threadIdx.x == 0) a.ovf_cell[atomicAdd(&a.novf[1], 1)] = (int)cell_id(g, C0[0], C0[1], C0[2]);
+    int C0[3], B[3];
+    int item;  // what is listed for the next level if this one does not fit
+    if (kLevel <= 1) {
+      const int b = kLevel == 0 ? it : a.list[0][it];
+      C0[0] = (b % nb) * PB;
+      C0[1] = ((b / nb) % nb) * PB;
+      C0[2] = (b / (nb * nb)) * PB;
+      for (int d = 0; d < 3; d++) B[d] = min(PB, nc - C0[d]);
+      item = b;
+    } else {
+      if (kLevel == 2) {
+        const int b = a.list[1][it / PNCORE_MAX], l = it % PNCORE_MAX;
+        C0[0] = (b % nb) * PB + l % PB;
+        C0[1] = ((b / nb) % nb) * PB + (l / PB) % PB;
+        C0[2] = (b / (nb * nb)) * PB + l / (PB * PB);
+        if (C0[0] >= nc || C0[1] >= nc || C0[2] >= nc) continue;
+        item = (int)cell_id(g, C0[0], C0[1], C0[2]);
+      } else {
+        item = a.list[2][it];
+        cell_coords(g, item, C0[0], C0[1], C0[2]);
+      }
+      B[0] = B[1] = B[2] = 1;
+    }
+    if (!pp_block<CAP>(a, C0, B, sm, pts, acc)) {
+      if (threadIdx.x == 0) a.list[kLevel][atomicAdd(&a.nlist[kLevel], 1)] = item;
       __syncthreads();
     }
   }
   pp_reduce(a, acc.npairs, acc.nwork, acc.f2max);
 }
 
-// level 2: listed cells with a large staging area, one 1024-thread block per SM
-__global__ void __launch_bounds__(PP_THREADS1) k_pp_bigcells(PPArgs a) {
-  __shared__ PPSmem sm;
-  extern __shared__ float4 pts[];
-  const Geo& g = a.g;
-  const int n = a.novf[1];
-  PPAcc acc;
-  for (int it = blockIdx.x; it < n; it += gridDim.x) {
-    int gc[3];
-    cell_coords(g, a.ovf_cell[it], gc[0], gc[1], gc[2]);
-    const int B[3] = {1, 1, 1};
-    if (!pp_block<PP_CAP1>(a, gc, B, sm, pts, acc)) {
-      if (threadIdx.x == 0) a.ovf_cell2[atomicAdd(&a.novf[2], 1)] = a.ovf_cell[it];
-      __syncthreads();
-    }
-  }
-  pp_reduce(a, acc.npairs, acc.nwork, acc.f2max);
-}
-
-// level 3: listed cells from global memory, one CTA per cell (persistent)
+// level 4: listed cells from global memory, one CTA per cell (persistent)
 __global__ void __launch_bounds__(PP_THREADS) k_pp_dense(PPArgs a) {
   const Geo& g = a.g;
-  const int n = a.novf[2];
+  const int n = a.nlist[3];
   PPAcc acc;
   for (int it = blockIdx.x; it < n; it += gridDim.x) {
-    int64_t c = a.ovf_cell2[it];
+    int64_t c = a.list[3][it];
     int gc[3];
     cell_coords(g, c, gc[0], gc[1], gc[2]);
     int64_t p1 = a.cstart[c + 1];
@@ -380,34 +369,35 @@ int cube_pp_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st) {
   a.nb = (c->p.nc + PB - 1) / PB;
   int64_t nbrick = (int64_t)a.nb * a.nb * a.nb;
   if (nbrick > c->pp_brick_cap) return cube_fail(c, CUBE_ERR_ARG, "PP brick list too small");
-  a.ovf_brick = c->pp_ovf_brick;
-  a.ovf_cell = c->pp_ovf_cell;
-  a.ovf_cell2 = c->pp_ovf_cell2;
-  a.novf = c->pp_novf;
-  CUBE_CUDA(c, cudaMemsetAsync(c->pp_novf, 0, 3 * sizeof(int), c->stream));
-  CUBE_CUDA(c, cudaFuncSetAttribute(k_pp_bricks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PP_SMEM));
-  CUBE_CUDA(c, cudaFuncSetAttribute(k_pp_cells, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PP_SMEM));
-  CUBE_CUDA(c, cudaFuncSetAttribute(k_pp_bigcells, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PP_SMEM1));
-  int persist = cube_grid((int64_t)1 << 40, 1, 4);
+  for (int l = 0; l < 4; l++) a.list[l] = c->pp_list[l];
+  a.nlist = c->pp_nlist;
+  CUBE_CUDA(c, cudaMemsetAsync(c->pp_nlist, 0, 4 * sizeof(int), c->stream));
+  auto k0 = k_pp_level<0, PP_CAP, PP_THREADS>;
+  auto k1 = k_pp_level<1, PP_CAP1, PP_THREADS1>;
+  auto k2 = k_pp_level<2, PP_CAP, PP_THREADS>;
+  auto k3 = k_pp_level<3, PP_CAP1, PP_THREADS1>;
+  CUBE_CUDA(c, cudaFuncSetAttribute(k0, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PP_SMEM));
+  CUBE_CUDA(c, cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PP_SMEM1B));
+  CUBE_CUDA(c, cudaFuncSetAttribute(k2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PP_SMEM));
+  CUBE_CUDA(c, cudaFuncSetAttribute(k3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PP_SMEM1));
+  const int persist = cube_grid((int64_t)1 << 40, 1, 4), one_per_sm = cube_grid((int64_t)1 << 40, 1, 1);
   cube_phase_begin(c, PH_PP);
-  if (c->opt_pp_level == 1) {
-    k_pp_list_all<<<cube_grid(nbrick, 256), 256, 0, c->stream>>>(c->pp_ovf_brick, (int)nbrick, c->pp_novf);
-  } else if (c->opt_pp_level == 2) {
-    k_pp_list_all<<<cube_grid(c->ncells, 256), 256, 0, c->stream>>>(c->pp_ovf_cell, (int)c->ncells, c->pp_novf + 1);
-  } else if (c->opt_pp_level == 3) {
-    k_pp_list_all<<<cube_grid(c->ncells, 256), 256, 0, c->stream>>>(c->pp_ovf_cell2, (int)c->ncells, c->pp_novf + 2);
-  } else {
-    k_pp_bricks<<<(unsigned)nbrick, PP_THREADS, PP_SMEM, c->stream>>>(a);
-  }
-  CUBE_CUDA(c, cudaGetLastError());
-  k_pp_cells<<<persist, PP_THREADS, PP_SMEM, c->stream>>>(a);
-  CUBE_CUDA(c, cudaGetLastError());
-  k_pp_bigcells<<<cube_grid((int64_t)1 << 40, 1, 1), PP_THREADS1, PP_SMEM1, c->stream>>>(a);
-  CUBE_CUDA(c, cudaGetLastError());
+  // a forced first level lists everything for it (tests of the dense paths)
+  const int start = c->opt_pp_level;
+  if (start == 1 || start == 2)
+    k_pp_list_all<<<cube_grid(nbrick, 256), 256, 0, c->stream>>>(c->pp_list[start - 1], (int)nbrick,
+                                                                 c->pp_nlist + start - 1);
+  else if (start >= 3)
+    k_pp_list_all<<<cube_grid(c->ncells, 256), 256, 0, c->stream>>>(c->pp_list[start - 1], (int)c->ncells,
+                                                                     c->pp_nlist + start - 1);
+  if (start <= 0) k0<<<(unsigned)nbrick, PP_THREADS, PP_SMEM, c->stream>>>(a);
+  if (start <= 1) k1<<<one_per_sm, PP_THREADS1, PP_SMEM1B, c->stream>>>(a);
+  if (start <= 2) k2<<<persist, PP_THREADS, PP_SMEM, c->stream>>>(a);
+  if (start <= 3) k3<<<one_per_sm, PP_THREADS1, PP_SMEM1, c->stream>>>(a);
   k_pp_dense<<<persist, PP_THREADS, 0, c->stream>>>(a);
   CUBE_CUDA(c, cudaGetLastError());
   cube_phase_end(c, PH_PP);
-  CUBE_CUDA(c, cudaMemcpyAsync(c->pp_novf_host, c->pp_novf, 3 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CUBE_CUDA(c, cudaMemcpyAsync(c->pp_nlist_host, c->pp_nlist, 4 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   r = cube_stats_fetch(c);
   if (r) return r;
   if ((int64_t)c->hstats->itest1 != c->np)
@@ -416,7 +406,7 @@ int cube_pp_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st) {
     st->f2_max_pp = bits_float(c->hstats->f2_pp_bits);
     st->npairs = (int64_t)c->hstats->npairs;
     st->itest1 = (int64_t)c->hstats->itest1;
-    st->pp_dense_bricks = c->pp_novf_host[0];
+    st->pp_dense_bricks = c->pp_nlist_host[0];
   }
   return CUBE_OK;
 }

@@ -239,10 +239,10 @@ void* cube_stream(cube_ctx* ctx);
    reference's FP64 expressions directly instead of the certified FP32 /
    float-float fast paths (results are identical by construction; used to test
    that claim and to time it).  CUBE_OPT_PP_LEVEL=2 sets the first of the
-   four PP levels (0: 4^3-cell bricks staged in shared memory, the default;
-   1: single cells staged; 2: single cells staged in a large block; 3: global
-   memory, one CTA per cell), which otherwise serve only regions too dense for
-   the level before.  The pair sums
+   five PP levels (0: 4^3-cell bricks staged in shared memory, the default;
+   1: bricks in a large block; 2: single cells; 3: single cells in a large
+   block; 4: global memory, one block per cell), which otherwise serve only
+   regions too dense for the level before.  The pair sums
    are order-independent, so every level gives bitwise the same result; used
    to test the dense-region paths.  CUBE_OPT_RANK_WALK=3 makes cube_update_x
    use its general visit-order walker for the ranks instead of the counting

@@ -229,7 +229,7 @@ def test_pp_levels_agree_bitwise(clump):
     p = _params(dict(nc=24, nnt=2))
     st = synth.random_state(p, mean_per_cell=6, seed=22, clump=clump, clump_mult=600)
     outs = []
-    for level in (0, 1, 2, 3):
+    for level in (0, 1, 2, 3, 4):
         g = C.CubeGPU(p)
         g.upload(st["xp"], st["vp"], st["pid"], st["rhoc"], st["vfield"])
         s = np.float32(st["sigma_vi"])
