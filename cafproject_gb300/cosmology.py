@@ -124,3 +124,28 @@ class TimeState:
         if pp_stats is not None and f32(pp_stats["f2_max_pp"]) > 0:
             self.dt_pp = f32(f32(1.0) * f32(np.sqrt(f32(1.0))) /
                              f32(f32(np.sqrt(f32(pp_stats["f2_max_pp"]))) * am * GG))
+
+
+def neutrino_checkpoints(z_checkpoint, z_i, z_i_nu):
+    """When the second species (neutrinos) switches on (initialize.f90:90-136).
+
+    Returns (checkpoint redshifts, index of the switch-on checkpoint (1-based,
+    0 when the species starts with the run), neutrino_flag at the start).
+    z_i_nu above z_i is an error; equal means both species start together;
+    otherwise z_i_nu becomes a checkpoint (inserted in decreasing order, or
+    appended after the last one) and the species is switched on there
+    (checkpoint.f90:85-91)."""
+    zc = [float(z) for z in z_checkpoint]
+    if z_i_nu > z_i:
+        raise ValueError("z_i_nu > z_i: neutrinos cannot start before the initial conditions")
+    if z_i_nu == z_i:
+        return zc, 0, True
+    for i, z in enumerate(zc):
+        if z == z_i_nu:
+            return zc, i + 1, False
+    if zc[-1] > z_i_nu:
+        return zc + [float(z_i_nu)], len(zc) + 1, False
+    for i, z in enumerate(zc):
+        if z < z_i_nu:
+            return zc[:i] + [float(z_i_nu)] + zc[i:], i + 1, False
+    return zc, 0, False

@@ -45,6 +45,13 @@ static void release(cube_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   cube_timers_free(c);
+  if (c->owner) {  // meshes, kernels, plans, work area and stream belong to the owner
+    c->rho_f = c->kern_f = c->kern_f_raw = c->rho_c = c->kern_c = nullptr;
+    for (int d = 0; d < 3; d++) c->force_f[d] = c->force_c[d] = nullptr;
+    c->cufft_work = nullptr;
+    c->plan_f_r2c = c->plan_f_c2r = c->plan_c_r2c = c->plan_c_c2r = 0;
+    c->stream = nullptr;
+  }
   void* bufs[] = {c->xp[0], c->xp[1], c->vp[0], c->vp[1], c->pid[0], c->pid[1], c->pcell[0], c->pcell[1],
                   c->rhoc[0], c->rhoc[1],
                   c->vfield[0], c->vfield[1], c->cstart[0], c->cstart[1], c->dest, c->dframe, c->doff, c->lrank, c->offc, c->perm, c->rank, c->xtra,
@@ -89,9 +96,9 @@ static int make_plans(cube_ctx* c) {
   return CUBE_OK;
 }
 
-extern "C" int cube_create(const cube_params* p, const float* fine_table, const float* coarse_table, int device,
-                           cube_ctx** out) {
-  if (!p || !out || !fine_table || !coarse_table) return CUBE_ERR_ARG;
+static int create_impl(const cube_params* p, const float* fine_table, const float* coarse_table, int device,
+                       cube_ctx* owner, cube_ctx** out) {
+  if (!p || !out || (!owner && (!fine_table || !coarse_table))) return CUBE_ERR_ARG;
   *out = nullptr;
   cube_ctx* c = new (std::nothrow) cube_ctx();
   if (!c) return CUBE_ERR_NOMEM;
@@ -120,9 +127,22 @@ extern "C" int cube_create(const cube_params* p, const float* fine_table, const 
   c->ncells = (int64_t)p->nc * p->nc * p->nc;
   c->nfine = (int64_t)c->nf * c->nf * c->nf;
   c->nvbin = 1 << (8 * p->izipv);
+  if (owner) {
+    const cube_params& q = owner->p;
+    if (p->nc != q.nc || p->nnt != q.nnt || p->ncell != q.ncell || p->ncb != q.ncb || p->nf_cutoff != q.nf_cutoff ||
+        device != owner->device)
+      return bad("a linked species needs the mesh geometry and device of its owner");
+    if (owner->owner) return bad("link to the owning context");
+    if (p->pp_on) return bad("the linked species takes no PP force");
+  }
   *out = c;
   CUBE_CUDA(c, cudaSetDevice(device));
-  CUBE_CUDA(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  if (owner) {
+    c->owner = owner;
+    c->stream = owner->stream;
+  } else {
+    CUBE_CUDA(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  }
   int64_t np = p->np_max;
   for (int k = 0; k < 2; k++) {
     ALLOC(c->xp[k], 3 * np * p->izipx);
@@ -152,16 +172,27 @@ extern "C" int cube_create(const cube_params* p, const float* fine_table, const 
     ALLOC(c->codec[k].dech, 8 * c->nvbin);
     ALLOC(c->codec[k].bnd, 8 * (c->nvbin / 2 + 1));
   }
-  int64_t nfh = (int64_t)(c->nf / 2 + 1);
-  int64_t fpad = 2 * nfh * c->nf * (int64_t)c->nf;  // floats of a padded fine mesh
-  ALLOC(c->rho_f, 4 * fpad);
-  for (int d = 0; d < 3; d++) ALLOC(c->force_f[d], 4 * fpad);
-  ALLOC(c->kern_f, 4 * 3 * nfh * c->nf * (int64_t)c->nf);
-  int64_t nch = (int64_t)(p->nc / 2 + 1);
-  int64_t cpad = 2 * nch * p->nc * (int64_t)p->nc;
-  ALLOC(c->rho_c, 4 * cpad);
-  for (int d = 0; d < 3; d++) ALLOC(c->force_c[d], 4 * cpad);
-  ALLOC(c->kern_c, 4 * 3 * nch * p->nc * (int64_t)p->nc);
+  if (owner) {
+    c->rho_f = owner->rho_f;
+    c->kern_f = owner->kern_f;
+    c->rho_c = owner->rho_c;
+    c->kern_c = owner->kern_c;
+    for (int d = 0; d < 3; d++) {
+      c->force_f[d] = owner->force_f[d];
+      c->force_c[d] = owner->force_c[d];
+    }
+  } else {
+    int64_t nfh = (int64_t)(c->nf / 2 + 1);
+    int64_t fpad = 2 * nfh * c->nf * (int64_t)c->nf;  // floats of a padded fine mesh
+    ALLOC(c->rho_f, 4 * fpad);
+    for (int d = 0; d < 3; d++) ALLOC(c->force_f[d], 4 * fpad);
+    ALLOC(c->kern_f, 4 * 3 * nfh * c->nf * (int64_t)c->nf);
+    int64_t nch = (int64_t)(p->nc / 2 + 1);
+    int64_t cpad = 2 * nch * p->nc * (int64_t)p->nc;
+    ALLOC(c->rho_c, 4 * cpad);
+    for (int d = 0; d < 3; d++) ALLOC(c->force_c[d], 4 * cpad);
+    ALLOC(c->kern_c, 4 * 3 * nch * p->nc * (int64_t)p->nc);
+  }
   {
     int nb = (p->nc + 3) / 4;
     c->pp_brick_cap = nb * nb * nb;
@@ -175,14 +206,36 @@ extern "C" int cube_create(const cube_params* p, const float* fine_table, const 
   }
   ALLOC(c->dstats, sizeof(DevStats));
   CUBE_CUDA(c, cudaMallocHost((void**)&c->hstats, sizeof(DevStats)));
-  int r = make_plans(c);
-  if (r) return r;
+  int r;
+  if (owner) {
+    c->plan_f_r2c = owner->plan_f_r2c;
+    c->plan_f_c2r = owner->plan_f_c2r;
+    c->plan_c_r2c = owner->plan_c_r2c;
+    c->plan_c_c2r = owner->plan_c_c2r;
+    c->cufft_work = owner->cufft_work;
+    c->cufft_work_bytes = owner->cufft_work_bytes;
+  } else {
+    r = make_plans(c);
+    if (r) return r;
+  }
   r = cube_build_tables(c);
   if (r) return r;
-  r = cube_kernels_init(c, fine_table, coarse_table);
-  if (r) return r;
+  if (!owner) {
+    r = cube_kernels_init(c, fine_table, coarse_table);
+    if (r) return r;
+  }
   CUBE_CUDA(c, cudaStreamSynchronize(c->stream));
   return CUBE_OK;
+}
+
+extern "C" int cube_create(const cube_params* p, const float* fine_table, const float* coarse_table, int device,
+                           cube_ctx** out) {
+  return create_impl(p, fine_table, coarse_table, device, nullptr, out);
+}
+
+extern "C" int cube_create_linked(const cube_params* p, cube_ctx* owner, cube_ctx** out) {
+  if (!owner) return CUBE_ERR_ARG;
+  return create_impl(p, nullptr, nullptr, owner->device, owner, out);
 }
 
 extern "C" int cube_destroy(cube_ctx* c) {
@@ -287,6 +340,31 @@ extern "C" int cube_particle_mesh(cube_ctx* c, float a_mid, float dt, cube_stats
   c->sigma_vi = c->sigma_vi_new;  // pm.f90:193
   if ((r = cube_coarse_forces_impl(c, st, pre))) return r;
   return cube_coarse_kick_impl(c, a_mid, dt, st, true);
+}
+
+// particle_mesh with the linked species (pm.f90:52-107, 162-189, 237-253,
+// 358-377): both species deposit into the same meshes, both are kicked by the
+// same forces with their own velocity codes; vmax is reported per species.
+extern "C" int cube_particle_mesh2(cube_ctx* c, cube_ctx* nu, float a_mid, float dt, cube_stats* st,
+                                   cube_stats* st_nu) {
+  int r = check_ready(c);
+  if (r) return r;
+  if (!nu || nu->owner != c) return cube_fail(c, CUBE_ERR_ARG, "the second species must be linked to this context");
+  if (!nu->have_state) return cube_fail(c, CUBE_ERR_STATE, "no state uploaded for the linked species");
+  const float pre[2] = {a_mid, dt};
+  if ((r = cube_fine_density_impl(c, nullptr, false))) return r;
+  if ((r = cube_fine_density_impl(nu, nullptr, true))) return cube_fail(c, r, nu->err);
+  if ((r = cube_fine_spectral_impl(c, st, pre))) return r;
+  if ((r = cube_fine_kick_impl(c, a_mid, dt, true))) return r;
+  if ((r = cube_fine_kick_impl(nu, a_mid, dt, true))) return cube_fail(c, r, nu->err);
+  c->sigma_vi = c->sigma_vi_new;  // pm.f90:193-194
+  nu->sigma_vi = nu->sigma_vi_new;
+  if ((r = cube_coarse_density_impl(c, nullptr, false))) return r;
+  if ((r = cube_coarse_density_impl(nu, nullptr, true))) return cube_fail(c, r, nu->err);
+  if ((r = cube_coarse_spectral_impl(c, st, pre))) return r;
+  if ((r = cube_coarse_kick_impl(c, a_mid, dt, st, true))) return r;
+  if ((r = cube_coarse_kick_impl(nu, a_mid, dt, st_nu, true))) return cube_fail(c, r, nu->err);
+  return CUBE_OK;
 }
 
 extern "C" int64_t cube_nplocal(const cube_ctx* c) { return c ? c->np : -1; }

@@ -46,6 +46,9 @@ struct cube_ctx {
   cube_params p{};
   int device = 0;
   cudaStream_t stream = nullptr;
+  // a second particle species (the neutrinos of CUBEnu) shares the meshes,
+  // FFT plans, force kernels and stream of the context it is linked to
+  cube_ctx* owner = nullptr;
   std::string err;
   // derived sizes
   int nt = 0, nf = 0, ntiles = 0, nvbin = 0;
@@ -554,8 +557,9 @@ int cube_kernels_init(cube_ctx* c, const float* fine_table, const float* coarse_
 int cube_scan_counts(cube_ctx* c, const int32_t* counts, int64_t* starts, int64_t n);
 int cube_update_x_impl(cube_ctx* c, float dt_old, float dt, float vz_max, cube_stats* st);
 int cube_pp_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st);
-int cube_fine_density_impl(cube_ctx* c, cube_stats* st);
-int cube_coarse_density_impl(cube_ctx* c, cube_stats* st);
+// density deposits; accumulate: add to the mesh (the linked species) instead of writing it
+int cube_fine_density_impl(cube_ctx* c, cube_stats* st, bool accumulate = false);
+int cube_coarse_density_impl(cube_ctx* c, cube_stats* st, bool accumulate = false);
 // pre (a_mid, dt) non-null: after the maxima, the force meshes are rewritten
 // as the mesh part of the kick term, force*a_mid*dt/6/pi, and the kick that
 // follows is given pre=true (fused step only; the stage calls keep forces)
@@ -563,6 +567,8 @@ int cube_fine_forces_impl(cube_ctx* c, cube_stats* st, const float* pre = nullpt
 int cube_fine_kick_impl(cube_ctx* c, float a_mid, float dt, bool pre = false);
 int cube_coarse_forces_impl(cube_ctx* c, cube_stats* st, const float* pre = nullptr);
 int cube_coarse_kick_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st, bool pre = false);
+int cube_fine_spectral_impl(cube_ctx* c, cube_stats* st, const float* pre);
+int cube_coarse_spectral_impl(cube_ctx* c, cube_stats* st, const float* pre);
 int cube_pk_deposit(cube_ctx* c, int ng, float* rho, unsigned long long* total);
 int dep_shift(float mass);  // deposits' fixed point: total = integer * 2^-dep_shift(mass)
 int cube_state_in(cube_ctx* c, int64_t np, const void* xp, const void* vp, const int32_t* pid,

@@ -6,6 +6,8 @@
 //   xp    xp(3,nplocal)  int8/int16        vp  vp(3,nplocal) int8/int16
 //   np    rhoc(nt,nt,nt,nnt,nnt,nnt) int32  vc  vfield(3,nt,...,nnt) real(4)
 //   id    pid(nplocal) int32 (written when the context carries particle ids)
+// A context linked to another (the second species) writes and reads the
+// *_nu files; its counts, formats and sigma_vi live in the owner's header.
 // <z> is z formatted as Fortran f7.3 with the blanks removed (z2str,
 // basic_functions.fh:36-42).  The state moves through pinned host buffers and
 // the files are written (read) by one host thread each, as the reference's
@@ -31,10 +33,10 @@ std::string f73(float z) {
   return i == std::string::npos ? s : s.substr(i);
 }
 
-std::string file_name(const char* dir, float z, int image, const char* what) {
+std::string file_name(const char* dir, float z, int image, const char* what, bool nu = false) {
   std::string d(dir);
   if (!d.empty() && d.back() != '/') d += '/';
-  return d + f73(z) + "_" + what + "_" + std::to_string(image) + ".bin";
+  return d + f73(z) + "_" + what + (nu ? "_nu" : "") + "_" + std::to_string(image) + ".bin";
 }
 
 struct FileJob {
@@ -94,12 +96,15 @@ extern "C" int cube_checkpoint_write(cube_ctx* c, const char* dir, float z, int 
   s.ncb = c->p.ncb;
   s.image = image;
   s.sigma_vi = c->sigma_vi;  // checkpoint.f90:31
-  std::vector<FileJob> jobs = {{file_name(dir, z, image, "info"), &s, sizeof s},
-                               {file_name(dir, z, image, "xp"), hx, bx},
-                               {file_name(dir, z, image, "vp"), hv, bv},
-                               {file_name(dir, z, image, "np"), hr, br},
-                               {file_name(dir, z, image, "vc"), hf, bf}};
-  if (c->p.with_pid) jobs.push_back({file_name(dir, z, image, "id"), hi, bi});
+  // the linked species writes xp_nu, vp_nu, np_nu, vc_nu, id_nu (checkpoint.f90:19-23, 55-70);
+  // its counts travel in the owner's header (nplocal_nu)
+  const bool nu = c->owner != nullptr;
+  std::vector<FileJob> jobs = {{file_name(dir, z, image, "xp", nu), hx, bx},
+                               {file_name(dir, z, image, "vp", nu), hv, bv},
+                               {file_name(dir, z, image, "np", nu), hr, br},
+                               {file_name(dir, z, image, "vc", nu), hf, bf}};
+  if (!nu) jobs.insert(jobs.begin(), FileJob{file_name(dir, z, image, "info"), &s, sizeof s});
+  if (c->p.with_pid) jobs.push_back({file_name(dir, z, image, "id", nu), hi, bi});
   run_jobs(jobs, true);
   for (const FileJob& j : jobs)
     if (!j.ok) return cube_fail(c, CUBE_ERR_ARG, "could not write " + j.path);
@@ -113,29 +118,32 @@ extern "C" int cube_checkpoint_read(cube_ctx* c, const char* dir, float z, int i
   std::vector<FileJob> head = {{file_name(dir, z, image, "info"), &s, sizeof s}};
   run_jobs(head, false);
   if (!head[0].ok) return cube_fail(c, CUBE_ERR_ARG, "could not read " + head[0].path);
-  // particle_initialization.f90:41-45
-  if (s.izipx != c->p.izipx || s.izipv != c->p.izipv) return cube_fail(c, CUBE_ERR_ARG, "zip format incompatible");
+  // the linked species reads the *_nu files with its counts, formats and
+  // sigma from the owner's header (particle_initialization.f90:35-45, 65-77)
+  const bool nu = c->owner != nullptr;
+  const int64_t hz = nu ? s.izipx_nu : s.izipx, hv_ = nu ? s.izipv_nu : s.izipv, hn = nu ? s.nplocal_nu : s.nplocal;
+  if (hz != c->p.izipx || hv_ != c->p.izipv) return cube_fail(c, CUBE_ERR_ARG, "zip format incompatible");
   if (s.nt != c->nt || s.nnt != c->p.nnt) return cube_fail(c, CUBE_ERR_ARG, "tile geometry differs from the context");
-  if (s.nplocal < 0 || s.nplocal > c->p.np_max) return cube_fail(c, CUBE_ERR_IMAGE_OVERFLOW, "nplocal exceeds np_max");
-  const int64_t np = s.nplocal, ncell = c->ncells;
+  if (hn < 0 || hn > c->p.np_max) return cube_fail(c, CUBE_ERR_IMAGE_OVERFLOW, "nplocal exceeds np_max");
+  const int64_t np = hn, ncell = c->ncells;
   const size_t bx = 3 * (size_t)np * c->p.izipx, bv = 3 * (size_t)np * c->p.izipv, bi = 4 * (size_t)np;
   const size_t br = 4 * (size_t)ncell, bf = 12 * (size_t)ncell;
   Pinned h;
   CUBE_CUDA(c, cudaMallocHost(&h.p, bx + bv + bi + br + bf + 64));
   unsigned char* base = static_cast<unsigned char*>(h.p);
   unsigned char *hx = base, *hv = hx + bx, *hi = hv + bv, *hr = hi + bi, *hf = hr + br;
-  std::vector<FileJob> jobs = {{file_name(dir, z, image, "xp"), hx, bx},
-                               {file_name(dir, z, image, "vp"), hv, bv},
-                               {file_name(dir, z, image, "np"), hr, br},
-                               {file_name(dir, z, image, "vc"), hf, bf}};
-  if (c->p.with_pid) jobs.push_back({file_name(dir, z, image, "id"), hi, bi});
+  std::vector<FileJob> jobs = {{file_name(dir, z, image, "xp", nu), hx, bx},
+                               {file_name(dir, z, image, "vp", nu), hv, bv},
+                               {file_name(dir, z, image, "np", nu), hr, br},
+                               {file_name(dir, z, image, "vc", nu), hf, bf}};
+  if (c->p.with_pid) jobs.push_back({file_name(dir, z, image, "id", nu), hi, bi});
   run_jobs(jobs, false);
   for (const FileJob& j : jobs)
     if (!j.ok) return cube_fail(c, CUBE_ERR_ARG, "could not read " + j.path + " (missing or wrong size)");
   int r = cube_state_in(c, np, hx, hv, c->p.with_pid ? (const int32_t*)hi : nullptr, (const int32_t*)hr,
                         (const float*)hf);
   if (r) return r;
-  c->sigma_vi = s.sigma_vi;  // particle_initialization.f90:38
+  c->sigma_vi = nu ? s.sigma_vi_nu : s.sigma_vi;  // particle_initialization.f90:38-39
   if (hdr) *hdr = s;
   return CUBE_OK;
 }

@@ -92,6 +92,7 @@ struct DepArgs {
   unsigned long long* total;  // sum of all owned cells in fixed point (exact)
   int ng;                     // power-spectrum mesh (kPk only)
   float qscale, qinv;         // fixed-point scale 2^s and 2^-s (dep_shift)
+  int accumulate;             // add to the mesh (a second species) instead of writing it
 };
 
 
@@ -179,7 +180,8 @@ __global__ void __launch_bounds__(256) k_deposit_det(DepArgs a) {
     mysum += ((unsigned long long)hi << 32) | lo;
     // (hi*2^32 + lo) * 2^-s as float
     float r = __fmaf_rn((float)lo, a.qinv, __fmul_rn((float)hi, __fmul_rn(a.qinv, 4294967296.0f)));
-    a.rho[mesh_idx(n, MPC * C0[0] + x, MPC * C0[1] + y, MPC * C0[2] + z)] = r;
+    float* cell = a.rho + mesh_idx(n, MPC * C0[0] + x, MPC * C0[1] + y, MPC * C0[2] + z);
+    *cell = a.accumulate ? __fadd_rn(*cell, r) : r;
   }
   for (int o = 16; o > 0; o >>= 1) mysum += __shfl_xor_sync(0xffffffffu, mysum, o);
   if ((threadIdx.x & 31) == 0) atomicAdd(&btot, mysum);
@@ -521,13 +523,13 @@ int cube_kernels_init(cube_ctx* c, const float* fine_table, const float* coarse_
 }
 
 // ----------------------------------------------------------------- fine
-int cube_fine_density_impl(cube_ctx* c, cube_stats* st) {
+int cube_fine_density_impl(cube_ctx* c, cube_stats* st, bool accumulate) {
   cudaStream_t s = c->stream;
   Geo g = make_geo(c);
   CUBE_CUDA(c, cudaMemsetAsync(c->dstats, 0, sizeof(DevStats), s));
   const int sh = dep_shift(c->p.mass_p);
   DepArgs a{g, c->xp[c->cur], c->rhoc[c->cur], c->cstart[c->cur], c->p.mass_p, c->rho_f, &c->dstats->rhof_fix, 0,
-            std::ldexp(1.0f, sh), std::ldexp(1.0f, -sh)};
+            std::ldexp(1.0f, sh), std::ldexp(1.0f, -sh), accumulate ? 1 : 0};
   cube_phase_begin(c, PH_F_DEPOSIT);
   int r = launch_deposit<4, 8, 4, 4, 1, 0>(c, a);
   cube_phase_end(c, PH_F_DEPOSIT);
@@ -541,11 +543,16 @@ int cube_fine_density_impl(cube_ctx* c, cube_stats* st) {
 }
 
 int cube_fine_forces_impl(cube_ctx* c, cube_stats* st, const float* pre) {
+  int r0 = cube_fine_density_impl(c, nullptr, false);
+  if (r0) return r0;
+  return cube_fine_spectral_impl(c, st, pre);
+}
+
+// forces from the density on the fine mesh (pm.f90:112-126)
+int cube_fine_spectral_impl(cube_ctx* c, cube_stats* st, const float* pre) {
   cudaStream_t s = c->stream;
   int64_t nfh = c->nf / 2 + 1;
   int64_t nspec = nfh * c->nf * (int64_t)c->nf;
-  int r0 = cube_fine_density_impl(c, nullptr);
-  if (r0) return r0;
   cube_phase_begin(c, PH_F_R2C);
   CUBE_FFT(c, cufftExecR2C(c->plan_f_r2c, c->rho_f, (cufftComplex*)c->rho_f));
   cube_phase_end(c, PH_F_R2C);
@@ -610,7 +617,7 @@ int cube_fine_kick_impl(cube_ctx* c, float a_mid, float dt, bool pre) {
 int cube_pk_deposit(cube_ctx* c, int ng, float* rho, unsigned long long* total) {
   const int sh = dep_shift(1.0f);
   DepArgs a{make_geo(c), c->xp[c->cur], c->rhoc[c->cur], c->cstart[c->cur], 1.0f, rho, total, ng,
-            std::ldexp(1.0f, sh), std::ldexp(1.0f, -sh)};
+            std::ldexp(1.0f, sh), std::ldexp(1.0f, -sh), 0};
   int nc = c->p.nc;
   if (ng == nc) return launch_deposit<1, 8, 8, 8, 1, 1, true>(c, a);
   if (ng == 2 * nc) return launch_deposit<2, 8, 8, 4, 1, 1, true>(c, a);
@@ -619,13 +626,13 @@ int cube_pk_deposit(cube_ctx* c, int ng, float* rho, unsigned long long* total) 
 }
 
 // --------------------------------------------------------------- coarse
-int cube_coarse_density_impl(cube_ctx* c, cube_stats* st) {
+int cube_coarse_density_impl(cube_ctx* c, cube_stats* st, bool accumulate) {
   Geo g = make_geo(c);
   CUBE_CUDA(c, cudaMemsetAsync(&c->dstats->f2_coarse_bits, 0, 4, c->stream));
   CUBE_CUDA(c, cudaMemsetAsync(&c->dstats->rhoc_fix, 0, 8, c->stream));
   const int sh = dep_shift(c->p.mass_p);
   DepArgs a{g, c->xp[c->cur], c->rhoc[c->cur], c->cstart[c->cur], c->p.mass_p, c->rho_c, &c->dstats->rhoc_fix, 0,
-            std::ldexp(1.0f, sh), std::ldexp(1.0f, -sh)};
+            std::ldexp(1.0f, sh), std::ldexp(1.0f, -sh), accumulate ? 1 : 0};
   cube_phase_begin(c, PH_C_DEPOSIT);
   int r = launch_deposit<1, 8, 8, 8, 1, 1>(c, a);
   cube_phase_end(c, PH_C_DEPOSIT);
@@ -639,12 +646,17 @@ int cube_coarse_density_impl(cube_ctx* c, cube_stats* st) {
 }
 
 int cube_coarse_forces_impl(cube_ctx* c, cube_stats* st, const float* pre) {
+  int r0 = cube_coarse_density_impl(c, nullptr, false);
+  if (r0) return r0;
+  return cube_coarse_spectral_impl(c, st, pre);
+}
+
+// forces from the density on the coarse mesh (pm.f90:275-315)
+int cube_coarse_spectral_impl(cube_ctx* c, cube_stats* st, const float* pre) {
   cudaStream_t s = c->stream;
   int nc = c->p.nc;
   int64_t nch = nc / 2 + 1;
   int64_t cspec = nch * nc * (int64_t)nc;
-  int r0 = cube_coarse_density_impl(c, nullptr);
-  if (r0) return r0;
   cube_phase_begin(c, PH_C_FFT);
   CUBE_FFT(c, cufftExecR2C(c->plan_c_r2c, c->rho_c, (cufftComplex*)c->rho_c));
   k_green3<<<cube_grid(cspec, 256), 256, 0, s>>>((const float2*)c->rho_c, c->kern_c, cspec, (float2*)c->force_c[0],

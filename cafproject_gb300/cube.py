@@ -32,7 +32,7 @@ EXPORTS = ["cube_create", "cube_destroy", "cube_last_error", "cube_upload_state"
            "cube_pm_coarse_forces", "cube_pm_coarse_kick", "cube_get_field", "cube_set_field", "cube_nplocal",
            "cube_synchronize", "cube_timing", "cube_timing_read", "cube_phase_name", "cube_stream",
            "cube_codec_check", "cube_codec_check_static", "cube_arith_check", "cube_pk_nbin",
-           "cube_power_spectrum", "cube_checkpoint_write", "cube_checkpoint_read", "cube_ic_zeldovich", "cube_set_option"]
+           "cube_power_spectrum", "cube_checkpoint_write", "cube_checkpoint_read", "cube_ic_zeldovich", "cube_create_linked", "cube_particle_mesh2", "cube_set_option"]
 CODEC_STATIC_MAX = 16384
 OPT_EXACT_KICKS = 1
 OPT_PP_LEVEL = 2
@@ -142,6 +142,8 @@ def load_library(path=None):
     L.cube_checkpoint_write.argtypes = [P, ctypes.c_char_p, F, ctypes.c_int, P]
     L.cube_checkpoint_read.argtypes = [P, ctypes.c_char_p, F, ctypes.c_int, P]
     L.cube_ic_zeldovich.argtypes = [P, P, F, ctypes.c_uint32, P, P]
+    L.cube_create_linked.argtypes = [P, P, P]
+    L.cube_particle_mesh2.argtypes = [P, P, F, F, P, P]
     L.cube_set_option.argtypes = [P, ctypes.c_int, I64]
     _lib = L
     return L
@@ -161,13 +163,19 @@ def force_tables():
 class CubeGPU:
     """One image of CUBE's state resident on one GPU."""
 
-    def __init__(self, params: CubeParams, device=0):
+    def __init__(self, params: CubeParams, device=0, owner=None):
+        """owner: a CubeGPU whose meshes this context shares as a second
+        particle species (cube_create_linked); close it before the owner."""
         self.p = params
         self.L = load_library()
-        fine, coarse = force_tables()
         self._cp = params.to_c()
         h = ctypes.c_void_p()
-        rc = self.L.cube_create(ctypes.byref(self._cp), _ptr(fine), _ptr(coarse), device, ctypes.byref(h))
+        if owner is None:
+            fine, coarse = force_tables()
+            rc = self.L.cube_create(ctypes.byref(self._cp), _ptr(fine), _ptr(coarse), device, ctypes.byref(h))
+        else:
+            rc = self.L.cube_create_linked(ctypes.byref(self._cp), owner.h, ctypes.byref(h))
+        self.owner = owner
         self.h = h
         if rc:
             msg = self.L.cube_last_error(h).decode() if h.value else ""
@@ -252,6 +260,14 @@ class CubeGPU:
         st = CubeStats()
         self._check(self.L.cube_pp_force(self.h, float(a_mid), float(dt), ctypes.byref(st)))
         return st.as_dict()
+
+    def particle_mesh2(self, nu, a_mid, dt):
+        """particle_mesh of this species and the linked species nu together;
+        returns (stats, stats of nu)."""
+        st, sn = CubeStats(), CubeStats()
+        self._check(self.L.cube_particle_mesh2(self.h, nu.h, float(a_mid), float(dt), ctypes.byref(st),
+                                               ctypes.byref(sn)))
+        return st.as_dict(), sn.as_dict()
 
     def particle_mesh(self, a_mid, dt):
         st = CubeStats()

@@ -140,6 +140,15 @@ enum cube_field {
 int cube_create(const cube_params* p, const float* fine_table, const float* coarse_table, int device,
                 cube_ctx** out);
 int cube_destroy(cube_ctx* ctx);
+
+/* A second particle species (CUBEnu's neutrinos, initialize.f90:90-136): a
+   context with its own compressed state, codec and sigma_vi (p gives its
+   izipx/izipv, mass_p and np_max; the mesh geometry must equal the owner's,
+   pp_on must be 0) that shares the owner's meshes, force kernels, FFT plans
+   and stream.  Destroy it before its owner.  cube_update_x, the checkpoint
+   calls (files named *_nu) and cube_power_spectrum work on it as on any
+   context; cube_particle_mesh2 advances both species together. */
+int cube_create_linked(const cube_params* p, cube_ctx* owner, cube_ctx** out);
 const char* cube_last_error(const cube_ctx* ctx);
 
 /* Upload / download the disjoint state (particle_initialization.f90:34-78,
@@ -155,7 +164,10 @@ int cube_download_state(cube_ctx* ctx, int64_t* nplocal, void* xp, void* vp, int
    Fortran f7.3 without blanks.  Write fills nplocal, izipx/v, nnt, nt, ncell,
    ncb, image and sigma_vi from the context and takes the other header fields
    from hdr; read checks the zip format and tile geometry, uploads the state,
-   sets sigma_vi and returns the header in hdr (may be NULL). */
+   sets sigma_vi and returns the header in hdr (may be NULL).  On a linked
+   context (the second species) they use the _xp_nu_, _vp_nu_, _np_nu_,
+   _vc_nu_, _id_nu_ files, write no info file, and read nplocal_nu, izipx_nu,
+   izipv_nu and sigma_vi_nu from the owner's info file. */
 int cube_checkpoint_write(cube_ctx* ctx, const char* dir, float z, int image, const cube_sim_header* hdr);
 int cube_checkpoint_read(cube_ctx* ctx, const char* dir, float z, int image, cube_sim_header* hdr);
 
@@ -193,6 +205,12 @@ int cube_pp_force(cube_ctx* ctx, float a_mid, float dt, cube_stats* st);
    sigma_vi_new), then sigma_vi=sigma_vi_new, then coarse PM kick; returns
    the force maxima and vmax. */
 int cube_particle_mesh(cube_ctx* ctx, float a_mid, float dt, cube_stats* st);
+
+/* particle_mesh of two species (pm.f90:52-107, 162-194, 237-253, 358-377):
+   the linked species nu deposits into the same meshes with its own mass, both
+   are kicked by the same forces with their own velocity codes, sigma_vi and
+   vmax (st_nu). */
+int cube_particle_mesh2(cube_ctx* ctx, cube_ctx* nu, float a_mid, float dt, cube_stats* st, cube_stats* st_nu);
 
 /* Stages of particle_mesh, for parity tests that inspect or inject fields:
    density only (CIC deposit, pm.f90:52-107 / 205-267), forces (deposit +

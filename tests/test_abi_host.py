@@ -124,3 +124,14 @@ def test_sim_header_matches_reference_layout():
     assert ctypes.sizeof(SimHeader) == 17 * 8 + 22 * 4 == 224
     assert SimHeader.a.offset == 136 and SimHeader.vz_max.offset == 220
     assert SimHeader.sigma_vi.offset == 136 + 4 * 17
+
+
+def test_neutrino_switch_on_checkpoints():
+    # initialize.f90:90-136
+    f = cosmology.neutrino_checkpoints
+    assert f([10.0, 5.0, 0.0], 49.0, 49.0) == ([10.0, 5.0, 0.0], 0, True)
+    assert f([10.0, 5.0, 0.0], 49.0, 5.0) == ([10.0, 5.0, 0.0], 2, False)       # already a checkpoint
+    assert f([10.0, 2.0, 0.0], 49.0, 5.0) == ([10.0, 5.0, 2.0, 0.0], 2, False)  # inserted
+    assert f([10.0, 8.0], 49.0, 5.0) == ([10.0, 8.0, 5.0], 3, False)            # appended after the last
+    with pytest.raises(ValueError):
+        f([0.0], 10.0, 20.0)
