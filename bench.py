@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--e2e-steps", type=int, default=0)
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-form line")
+    ap.add_argument("--adjoint-only", action="store_true", help="run only the differentiable-form measurement")
     return ap.parse_args()
 
 
@@ -310,6 +312,59 @@ def run_gb300(args, ws, rank, lrank):
                 cpu=cpu, n=int(ntot), p=p, t_ic=t_ic, gpu_launches=gpu_launches(p, args.steps))
 
 
+def run_adjoint(args, lrank, reps=3):
+    """Adjoint / forward cost of the differentiable form on its workload:
+    128^3 particles, 256^3 mesh, 256 Mpc/h, 10 steps z=9 -> 0, checkpoint every
+    2 steps, loss = sum (rho_final - rho_target)^2 with the target from a
+    second seed.  Forward = IC + 10 steps + final density; adjoint = density
+    adjoint + backward (segment re-runs included) + IC adjoint.  Device times
+    from CUDA events on the library's stream."""
+    import torch
+
+    from cafproject_gb300.dpm import DiffPM
+
+    sim = DiffPM(256, 128, 9.0, 0.0, 10, ckpt_every=2, device=lrank, box=256.0)
+    try:
+        target = sim.density(sim.forward(sim.noise(args.seed + 1))[0])
+        noise = sim.noise(args.seed)
+        stream = torch.cuda.ExternalStream(sim.stream())
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        fw, bw, tot_f, tot_b = [], [], [], []
+        for i in range(args.warmup + reps):
+            torch.cuda.synchronize()
+            x, v = sim.forward(noise)
+            rho = sim.density(x)
+            grho = 2.0 * (rho - target)
+            torch.cuda.synchronize()
+            info0 = sim.info()
+            gx = sim.density_adjoint(x, grho)
+            gn = sim.backward(gx, torch.zeros_like(v))
+            info1 = sim.info()
+            # the two mesh passes of the loss, timed alone on the library's stream
+            torch.cuda.synchronize()
+            ev[0].record(stream)
+            sim.density(x)
+            ev[1].record(stream)
+            ev[2].record(stream)
+            sim.density_adjoint(x, grho)
+            ev[3].record(stream)
+            torch.cuda.synchronize()
+            if i >= args.warmup:
+                fw.append(info0["forward_ms"] + ev[0].elapsed_time(ev[1]))
+                bw.append(info1["backward_ms"] + ev[2].elapsed_time(ev[3]))
+                tot_f.append(info0["forward_ms"])
+                tot_b.append(info1["backward_ms"])
+        f, b = statistics.median(fw), statistics.median(bw)
+        assert torch.isfinite(gn).all()
+        return {"workload": "dpm128: 128^3 particles, 256^3 mesh, 256 Mpc/h, 10 steps z=9->0, checkpoint every 2",
+                "forward_ms": round(f, 3), "adjoint_ms": round(b, 3), "ratio": round(b / f, 3), "target_ratio": 3.0,
+                "graph_forward_ms": round(statistics.median(tot_f), 3),
+                "graph_backward_ms": round(statistics.median(tot_b), 3), "reps": reps,
+                "gradient_checks": "tests/test_gpu_dpm.py (FP64 autograd and central differences)"}
+    finally:
+        sim.close()
+
+
 def gpu_launches(p, steps):
     """Launches of this library's kernels per step (cuFFT kernels not counted)."""
     upd = 1 + 2 + 3 + 2 + 1 + 1  # dest, counting ranks (2), scan (3), place + vfield, scatter, sigma
@@ -389,7 +444,12 @@ def main():
                     "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
             print(json.dumps(line), flush=True)
         return
+    if args.adjoint_only:
+        if rank == 0:
+            print(json.dumps({"adjoint": run_adjoint(args, lrank)}), flush=True)
+        return
     r = run_gb300(args, ws, rank, lrank)
+    adj = run_adjoint(args, lrank) if (rank == 0 and ws == 1 and not args.no_adjoint) else None
     if rank == 0:
         p = r["p"]
         line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -404,6 +464,8 @@ def main():
                 "phases": r["phases"]}
         if r["cpu"]:
             line["cpu_baseline"] = r["cpu"]
+        if adj:
+            line["adjoint"] = adj
         print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist

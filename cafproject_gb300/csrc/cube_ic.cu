@@ -99,8 +99,9 @@ __device__ __forceinline__ float hash_uniform(uint64_t idx, uint32_t s) {
   return (float)(h >> 8) * (1.0f / 16777216.0f);
 }
 
-// Gaussian white noise: Box-Muller on the pairs (2i, 2i+1) along x (:292-300)
-__global__ void k_ic_noise(float* r, int nf, uint32_t s) {
+// Gaussian white noise: Box-Muller on the pairs (2i, 2i+1) along x (:292-300);
+// rows of pitch floats
+__global__ void k_ic_noise(float* r, int nf, int pitch, uint32_t s) {
   const int64_t npairs = (int64_t)nf * nf * (nf / 2);
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < npairs; q += (int64_t)gridDim.x * blockDim.x) {
     const int64_t row = q / (nf / 2);
@@ -108,7 +109,7 @@ __global__ void k_ic_noise(float* r, int nf, uint32_t s) {
     const uint64_t i0 = (uint64_t)row * nf + x;
     const float u1 = hash_uniform(i0, s), u2 = hash_uniform(i0 + 1, s);
     const float rr = sqrtf(-2.0f * logf(1.0f - u2)), th = 2.0f * CUBE_PI_F * u1;
-    float* o = r + row * (nf + 2) + x;
+    float* o = r + row * pitch + x;
     o[0] = rr * cosf(th);
     o[1] = rr * sinf(th);
   }
@@ -153,6 +154,8 @@ struct ScaleArgs {
   const float* ld2;      // log Delta^2 table
   int ntab, nf;
   float kfac;            // 2 pi / box
+  float* fout;           // when set: store the factor (times fscale) here instead of scaling ck
+  float fscale;
 };
 
 // ck *= sqrt(Delta^2/(4 pi) * nf/kr) * nf/kr * KK  (:306-330, 505-541)
@@ -161,7 +164,10 @@ __global__ void k_ic_scale(ScaleArgs a) {
   const int64_t n = (int64_t)nh * nf * nf;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     if (i == 0) {
-      a.ck[0] = make_float2(0.f, 0.f);
+      if (a.fout)
+        a.fout[0] = 0.f;
+      else
+        a.ck[0] = make_float2(0.f, 0.f);
       continue;
     }
     const int x = (int)(i % nh), y = (int)((i / nh) % nf), z = (int)(i / ((int64_t)nh * nf));
@@ -179,6 +185,10 @@ __global__ void k_ic_scale(ScaleArgs a) {
     const float t = (lx - a.lk[lo]) / (a.lk[hi] - a.lk[lo]);
     const float d2 = expf(a.ld2[lo] + (a.ld2[hi] - a.ld2[lo]) * t);
     const float f = sqrtf(d2 / (4.0f * (float)kPi) * ((float)nf / kr)) * ((float)nf / kr) * a.kk[i].x;
+    if (a.fout) {
+      a.fout[i] = f * a.fscale;
+      continue;
+    }
     const float2 c = a.ck[i];
     a.ck[i] = make_float2(c.x * f, c.y * f);
   }
@@ -324,7 +334,62 @@ __global__ void k_ic_encode(const double* res, int64_t n3, CodecView cv, int izi
     store_code(vp, i, izipv, codec_encode(cv, res[i]));
 }
 
+// The corrected potential kernel's spectrum in kp (a padded nf^3 mesh, in
+// place; :433-503) and the log Delta^2 table in dtab (2 x 1000 floats); fills
+// sa for k_ic_scale except ck / fout.
+int ic_kernel_spectrum(cube_ctx* c, int nf, cufftHandle r2c, cufftHandle c2r, float* kp, float* dtab,
+                       const cube_cosmology& cs, double a, ScaleArgs& sa) {
+  cudaStream_t s = c->stream;
+  const int64_t nspec = (int64_t)(nf / 2 + 1) * nf * nf;
+  k_ic_kern<<<cube_grid(nspec, 256), 256, 0, s>>>((float2*)kp, nf);
+  CUBE_CUDA(c, cudaGetLastError());
+  CUBE_FFT(c, cufftExecC2R(c2r, (cufftComplex*)kp, kp));
+  {  // phi8: the mean of the six points at 8 cells on the axes
+    auto at_ = [nf](int64_t x, int64_t y, int64_t z) { return x + (int64_t)(nf + 2) * (y + (int64_t)nf * z); };
+    const int64_t at[6] = {at_(8, 0, 0), at_(0, 8, 0), at_(0, 0, 8), at_(nf - 8, 0, 0), at_(0, nf - 8, 0), at_(0, 0, nf - 8)};
+    float h[6];
+    for (int i = 0; i < 6; i++)
+      CUBE_CUDA(c, cudaMemcpyAsync(&h[i], kp + at[i], 4, cudaMemcpyDeviceToHost, s));
+    CUBE_CUDA(c, cudaStreamSynchronize(s));
+    const float inv = 1.0f / ((float)nf * nf * nf);
+    float phi8 = 0.f;
+    for (int i = 0; i < 6; i++) phi8 += h[i] * inv;
+    phi8 /= 6.0f;
+    k_ic_kern_correct<<<cube_grid((int64_t)nf * nf, 1, 8), 256, 0, s>>>(kp, nf, phi8);
+    CUBE_CUDA(c, cudaGetLastError());
+  }
+  CUBE_FFT(c, cufftExecR2C(r2c, kp, (cufftComplex*)kp));
+  std::vector<float> lk, ld2;
+  delta2_table(cs, nf, a, lk, ld2);
+  CUBE_CUDA(c, cudaMemcpyAsync(dtab, lk.data(), 4 * lk.size(), cudaMemcpyHostToDevice, s));
+  CUBE_CUDA(c, cudaMemcpyAsync(dtab + lk.size(), ld2.data(), 4 * ld2.size(), cudaMemcpyHostToDevice, s));
+  CUBE_CUDA(c, cudaStreamSynchronize(s));  // the host tables go out of scope
+  sa = ScaleArgs{nullptr, (const float2*)kp, dtab, dtab + lk.size(), (int)lk.size(), nf, (float)(2 * kPi / cs.box),
+                 nullptr, 1.0f};
+  return CUBE_OK;
+}
+
 }  // namespace
+
+int cube_ic_filter(cube_ctx* c, const cube_cosmology& cs, double a, int n, cufftHandle r2c, cufftHandle c2r,
+                   float* scratch, float* dtab, float* filter) {
+  ScaleArgs sa;
+  int r = ic_kernel_spectrum(c, n, r2c, c2r, scratch, dtab, cs, a, sa);
+  if (r) return r;
+  sa.fout = filter;
+  sa.fscale = 1.0f / ((float)n * (float)n * (float)n);
+  k_ic_scale<<<cube_grid((int64_t)(n / 2 + 1) * n * n, 256), 256, 0, c->stream>>>(sa);
+  CUBE_CUDA(c, cudaGetLastError());
+  return CUBE_OK;
+}
+
+uint32_t cube_ic_seed(uint32_t seed) { return fmix32((uint32_t)((uint64_t)seed * 0x9E3779B1ull + 0x7F4A7C15ull)); }
+
+void cube_ic_noise(float* r, int n, int pitch, uint32_t seed, cudaStream_t s) {
+  k_ic_noise<<<cube_grid((int64_t)n * n * (n / 2), 256), 256, 0, s>>>(r, n, pitch, cube_ic_seed(seed));
+}
+
+double cube_ic_vfactor(double a, double om, double ol) { return vfactor(a, om, ol); }
 
 extern "C" int cube_ic_zeldovich(cube_ctx* c, const cube_cosmology* cs, float z_init, uint32_t seed, float* sigma_vi,
                                  float* vmax) {
@@ -343,38 +408,17 @@ extern "C" int cube_ic_zeldovich(cube_ctx* c, const cube_cosmology* cs, float z_
   const int64_t nspec = (int64_t)(nf / 2 + 1) * nf * nf;
   const int k = c->cur, alt = 1 - k;
   // 1. noise and its spectrum
-  const uint32_t s0 = fmix32((uint32_t)((uint64_t)seed * 0x9E3779B1ull + 0x7F4A7C15ull));
-  k_ic_noise<<<cube_grid((int64_t)nf * nf * (nf / 2), 256), 256, 0, s>>>(c->rho_f, nf, s0);
+  cube_ic_noise(c->rho_f, nf, nf + 2, seed, s);
   CUBE_CUDA(c, cudaGetLastError());
   CUBE_FFT(c, cufftExecR2C(c->plan_f_r2c, c->rho_f, (cufftComplex*)c->rho_f));
-  // 2. corrected potential kernel, in force plane 0
+  // 2. corrected potential kernel in force plane 0, tables in force plane 1
   float* kp = c->force_f[0];
-  k_ic_kern<<<cube_grid(nspec, 256), 256, 0, s>>>((float2*)kp, nf);
-  CUBE_CUDA(c, cudaGetLastError());
-  CUBE_FFT(c, cufftExecC2R(c->plan_f_c2r, (cufftComplex*)kp, kp));
-  {  // phi8: the mean of the six points at 8 cells on the axes
-    auto at_ = [nf](int64_t x, int64_t y, int64_t z) { return x + (int64_t)(nf + 2) * (y + (int64_t)nf * z); };
-    const int64_t at[6] = {at_(8, 0, 0), at_(0, 8, 0), at_(0, 0, 8), at_(nf - 8, 0, 0), at_(0, nf - 8, 0), at_(0, 0, nf - 8)};
-    float h[6];
-    for (int i = 0; i < 6; i++)
-      CUBE_CUDA(c, cudaMemcpyAsync(&h[i], kp + at[i], 4, cudaMemcpyDeviceToHost, s));
-    CUBE_CUDA(c, cudaStreamSynchronize(s));
-    const float inv = 1.0f / ((float)nf * nf * nf);
-    float phi8 = 0.f;
-    for (int i = 0; i < 6; i++) phi8 += h[i] * inv;
-    phi8 /= 6.0f;
-    k_ic_kern_correct<<<cube_grid((int64_t)nf * nf, 1, 8), 256, 0, s>>>(kp, nf, phi8);
-    CUBE_CUDA(c, cudaGetLastError());
-  }
-  CUBE_FFT(c, cufftExecR2C(c->plan_f_r2c, kp, (cufftComplex*)kp));
+  float* dtab = reinterpret_cast<float*>(c->force_f[1]);
+  ScaleArgs sa;
+  int r = ic_kernel_spectrum(c, nf, c->plan_f_r2c, c->plan_f_c2r, kp, dtab, *cs, a, sa);
+  if (r) return r;
   // 3. scaled spectrum times the kernel, then phi
-  std::vector<float> lk, ld2;
-  delta2_table(*cs, nf, a, lk, ld2);
-  float* dtab = reinterpret_cast<float*>(c->force_f[1]);  // tables in force plane 1 for the moment
-  CUBE_CUDA(c, cudaMemcpyAsync(dtab, lk.data(), 4 * lk.size(), cudaMemcpyHostToDevice, s));
-  CUBE_CUDA(c, cudaMemcpyAsync(dtab + lk.size(), ld2.data(), 4 * ld2.size(), cudaMemcpyHostToDevice, s));
-  ScaleArgs sa{(float2*)c->rho_f, (const float2*)kp, dtab, dtab + lk.size(), (int)lk.size(), nf,
-               (float)(2 * kPi / cs->box)};
+  sa.ck = (float2*)c->rho_f;
   k_ic_scale<<<cube_grid(nspec, 256), 256, 0, s>>>(sa);
   CUBE_CUDA(c, cudaGetLastError());
   CUBE_FFT(c, cufftExecC2R(c->plan_f_c2r, (cufftComplex*)c->rho_f, c->rho_f));
@@ -388,7 +432,7 @@ extern "C" int cube_ic_zeldovich(cube_ctx* c, const cube_cosmology* cs, float z_
               c->dstats->vmax_bits};
   k_ic_particles<<<cube_grid(n, 256), 256, 0, s>>>(pa, make_geo(c));
   CUBE_CUDA(c, cudaGetLastError());
-  int r = cube_scan_counts(c, c->rhoc[k], c->cstart[k], c->ncells);
+  r = cube_scan_counts(c, c->rhoc[k], c->cstart[k], c->ncells);
   if (r) return r;
   int32_t* fill = reinterpret_cast<int32_t*>(c->rank);
   CUBE_CUDA(c, cudaMemsetAsync(fill, 0, 4 * (size_t)c->ncells, s));

@@ -571,6 +571,13 @@ int cube_fine_spectral_impl(cube_ctx* c, cube_stats* st, const float* pre);
 int cube_coarse_spectral_impl(cube_ctx* c, cube_stats* st, const float* pre);
 int cube_pk_deposit(cube_ctx* c, int ng, float* rho, unsigned long long* total);
 int dep_shift(float mass);  // deposits' fixed point: total = integer * 2^-dep_shift(mass)
+// initial-condition pieces shared with the differentiable form (cube_ic.cu):
+// the real filter noise -> phi on an n^3 lattice (Delta^2 scaling times the
+// corrected potential kernel, 1/n^3 folded in), the counter-hash noise, and a^2 H
+int cube_ic_filter(cube_ctx* c, const cube_cosmology& cs, double a, int n, cufftHandle r2c, cufftHandle c2r,
+                   float* scratch, float* dtab, float* filter);
+void cube_ic_noise(float* r, int n, int pitch, uint32_t seed, cudaStream_t s);
+double cube_ic_vfactor(double a, double om, double ol);
 int cube_state_in(cube_ctx* c, int64_t np, const void* xp, const void* vp, const int32_t* pid,
                   const int32_t* rhoc, const float* vfield);
 int cube_state_out(cube_ctx* c, int64_t* np, void* xp, void* vp, int32_t* pid, int32_t* rhoc, float* vfield);

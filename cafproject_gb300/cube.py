@@ -32,7 +32,10 @@ EXPORTS = ["cube_create", "cube_destroy", "cube_last_error", "cube_upload_state"
            "cube_pm_coarse_forces", "cube_pm_coarse_kick", "cube_get_field", "cube_set_field", "cube_nplocal",
            "cube_synchronize", "cube_timing", "cube_timing_read", "cube_phase_name", "cube_stream",
            "cube_codec_check", "cube_codec_check_static", "cube_arith_check", "cube_pk_nbin",
-           "cube_power_spectrum", "cube_checkpoint_write", "cube_checkpoint_read", "cube_ic_zeldovich", "cube_create_linked", "cube_particle_mesh2", "cube_set_option"]
+           "cube_power_spectrum", "cube_checkpoint_write", "cube_checkpoint_read", "cube_ic_zeldovich", "cube_create_linked", "cube_particle_mesh2", "cube_set_option",
+           "cube_dpm_create", "cube_dpm_destroy", "cube_dpm_last_error", "cube_dpm_stream", "cube_dpm_nparticles",
+           "cube_dpm_set_schedule", "cube_dpm_noise", "cube_dpm_forward", "cube_dpm_backward", "cube_dpm_density",
+           "cube_dpm_density_adjoint", "cube_dpm_tables", "cube_dpm_info"]
 CODEC_STATIC_MAX = 16384
 OPT_EXACT_KICKS = 1
 OPT_PP_LEVEL = 2

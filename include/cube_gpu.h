@@ -292,6 +292,54 @@ int cube_arith_check(cube_ctx* ctx, int64_t* mismatches);
 int cube_codec_check_static(cube_ctx* ctx, float sigma, const double* v, int64_t n, int32_t* direct,
                             int32_t* table);
 
+/* ------------------------------------------------------------------------
+   Differentiable form (no reference counterpart: the reference has no
+   gradients).  A single-level PM integrator on decoded FP32 positions --
+   deposit, Green's multiply (-4 pi/khat^2), central-difference force, kick,
+   drift with the coefficients of the reference's step (drift = dt_mid of
+   update_particle.f90:66, kick = a_mid*dt/(6 pi) of pm.f90:162) -- from
+   Zel'dovich initial conditions of white noise on the npd^3 particle lattice
+   (the filter of cube_ic_zeldovich), with hand-written adjoint kernels.
+   Positions are displacements d from each particle's lattice point (the
+   centre of mesh cell step*l, step = ng/npd) in mesh cells, unwrapped;
+   particles in lattice order l = x + npd*(y + npd*z); arrays (3, np) float.  Every pointer of the pass calls is
+   DEVICE memory on the context's device; the calls return after the
+   context's stream has drained.  cube_dpm_backward applies to the last
+   cube_dpm_forward (its checkpoints); the state is kept at the start of
+   every ckpt_every steps and the rest recomputed. */
+typedef struct cube_dpm cube_dpm;
+typedef struct cube_dpm_params {
+  int32_t ng;          /* mesh cells per dimension (even, >= 16) */
+  int32_t npd;         /* particles and noise points per dimension (even, >= 16, divides ng) */
+  int32_t max_steps;   /* schedule capacity */
+  int32_t ckpt_every;  /* steps per recomputation segment (1 keeps every step) */
+  float z_init;        /* redshift of the initial conditions */
+} cube_dpm_params;
+
+int cube_dpm_create(const cube_dpm_params* params, const cube_cosmology* cosmo, int device, cube_dpm** out);
+int cube_dpm_destroy(cube_dpm* ctx);
+const char* cube_dpm_last_error(const cube_dpm* ctx);
+void* cube_dpm_stream(cube_dpm* ctx);
+int64_t cube_dpm_nparticles(const cube_dpm* ctx);
+/* per-step drift (dt_mid) and kick (a_mid*dt/(6 pi)) coefficients, host arrays */
+int cube_dpm_set_schedule(cube_dpm* ctx, int nsteps, const float* drift, const float* kick);
+/* npd^3 Gaussian white noise of a seed (the generator of cube_ic_zeldovich) */
+int cube_dpm_noise(cube_dpm* ctx, uint32_t seed, float* noise);
+/* noise (npd^3) -> final displacements and velocities (3, np) */
+int cube_dpm_forward(cube_dpm* ctx, const float* noise, float* x, float* v);
+/* cotangents of the final (x, v) -> of the noise; gx0 / gv0 (optional)
+   receive those of the initial state */
+int cube_dpm_backward(cube_dpm* ctx, const float* gx, const float* gv, float* gnoise, float* gx0, float* gv0);
+/* CIC density (ng^3, mean 1) of displacements x, and its adjoint gx = (d rho/d x)^T grho */
+int cube_dpm_density(cube_dpm* ctx, const float* x, float* rho);
+int cube_dpm_density_adjoint(cube_dpm* ctx, const float* x, const float* grho, float* gx);
+/* HOST copies of the IC filter ((npd/2+1) npd^2) and Green's function
+   ((ng/2+1) ng^2), both with the inverse transform's 1/n^3 folded in */
+int cube_dpm_tables(cube_dpm* ctx, float* ic_filter, float* green);
+/* particle mass, a^2 H at z_init, and the device times of the last forward
+   and backward pass (CUDA events around each graph launch) */
+int cube_dpm_info(const cube_dpm* ctx, float* mass, float* vf, float* fwd_ms, float* bwd_ms);
+
 #ifdef __cplusplus
 }
 #endif
