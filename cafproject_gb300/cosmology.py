@@ -126,6 +126,36 @@ class TimeState:
                              f32(f32(np.sqrt(f32(pp_stats["f2_max_pp"]))) * am * GG))
 
 
+def fixed_schedule(z_init, z_final, nsteps, omega_m=0.3, omega_l=0.7, spacing="log"):
+    """A fixed step schedule from z_init to z_final: nsteps equal steps in
+    ln a ("log") or in a ("linear").  Each step's dt is the one whose Friedmann
+    step (``expansion``) covers the step's da, found by bisection; a_mid is
+    a + da/2 as in ``TimeState.timestep``.  Returns float32 arrays (dt,
+    a_mid, a) with a the nsteps+1 scale factors."""
+    a0, a1 = 1.0 / (1.0 + z_init), 1.0 / (1.0 + z_final)
+    if spacing == "log":
+        a = np.exp(np.linspace(np.log(a0), np.log(a1), nsteps + 1)).astype(np.float32)
+    else:
+        a = np.linspace(a0, a1, nsteps + 1).astype(np.float32)
+    dts, amids = np.zeros(nsteps, f32), np.zeros(nsteps, f32)
+    for i in range(nsteps):
+        target = float(a[i + 1]) - float(a[i])
+        lo, hi = 0.0, 1.0
+        while sum(float(d) for d in expansion(a[i], hi, omega_m, omega_l)) < target:
+            hi *= 2
+        for _ in range(60):
+            mid = 0.5 * (lo + hi)
+            if sum(float(d) for d in expansion(a[i], mid, omega_m, omega_l)) < target:
+                lo = mid
+            else:
+                hi = mid
+        dt = f32(hi)
+        d1, d2 = expansion(a[i], dt, omega_m, omega_l)
+        dts[i] = dt
+        amids[i] = f32(a[i] + f32(f32(d1 + d2) / f32(2)))
+    return dts, amids, a
+
+
 def neutrino_checkpoints(z_checkpoint, z_i, z_i_nu):
     """When the second species (neutrinos) switches on (initialize.f90:90-136).
 

@@ -111,9 +111,8 @@ static int create_impl(const cube_params* p, const float* fine_table, const floa
   };
   if (p->nc <= 0 || p->nnt <= 0 || p->nc % p->nnt) return bad("nc must be a positive multiple of nnt");
   // LRCKCORR rescales the coarse modes with |k|<=8 by 1/Im FFT(raw kernel)
-  // (kernel_c.f90:111-113); at nc<=16 that sphere reaches the Nyquist plane,
-  // where the odd kernel's transform is zero.
-  if (p->nc <= 16) return bad("nc must exceed 16 (coarse kernel correction needs |k|<=8 below Nyquist)");
+  // (kernel_c.f90:111-113); below nc = 16 that sphere wraps past Nyquist
+  if (p->nc < 16) return bad("nc must be at least 16 (coarse kernel correction needs |k|<=8 up to Nyquist)");
   if (p->ncell != 4) return bad("ncell must be 4");
   if (p->izipx < 1 || p->izipx > 2 || p->izipv < 1 || p->izipv > 2) return bad("izipx/izipv must be 1 or 2");
   c->nt = p->nc / p->nnt;

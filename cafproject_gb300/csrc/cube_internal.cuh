@@ -42,6 +42,37 @@ struct DevStats {
   unsigned long long rhof_fix, rhoc_fix;  // deposited mass in 2^-32 fixed point
 };
 
+// Scalars of one step when the step runs inside a captured CUDA graph
+// (cube_batch_*).  A head kernel derives them on the device at the start of
+// every step from the box's schedule and the previous step's results, with
+// the eager host path's arithmetic; kernels read them through a StepDev
+// pointer, null on the eager path, where the same values arrive as kernel
+// arguments.
+struct StepHost {
+  float dt_mid, a_mid, dt;
+  int nlayer;
+  float tau[3];  // coarse kick: 0.7 of the last vmax
+  float kick_f;  // PP kick factor a_mid*dt/6/pi, float and double
+  double kick;
+  float cf_vi;   // vcoef(sigma_vi) as float (the encode estimate only)
+  int pad;
+};
+struct StepDev {
+  StepHost h;
+  float sigma_new, cf_new;  // update_x's sigma_vi_new and its vcoef
+  // carried from step to step on the device
+  float sigma_vi, vz_max;   // codec sigma of the state; sim%vz_max for nlayer
+  float vmax_prev[3];       // the last coarse-kick vmax (0 before the first)
+  int istep;                // steps done
+};
+// what the host reads back after a graph step: the stats of each stage
+struct StepOut {
+  DevStats upd, pp, fine, coarse;
+  double sums[3];  // sigma statistics (update_particle.f90:171-224)
+  float sigma_new;
+  int pad;
+};
+
 struct cube_ctx {
   cube_params p{};
   int device = 0;
@@ -91,6 +122,11 @@ struct cube_ctx {
   int codec_next = 0;
   float sigma_vi = 0.f, sigma_vi_new = 0.f;
   float vmax_prev[3] = {0.f, 0.f, 0.f};  // last coarse-kick vmax (0: unknown)
+  // graph mode (cube_batch_*): step scalars on the device, codec slot 0 holds
+  // sigma_vi and slot 1 sigma_vi_new, no host synchronisation inside a step
+  bool graph_mode = false;
+  StepDev* sd = nullptr;    // device
+  StepOut* sout = nullptr;  // device (owned by the batch)
   unsigned long long kick_exact_lanes = 0;
   int opt_exact_kicks = 0;
   int opt_rank_walk = 0;   // force the general visit-order rank walker
@@ -309,13 +345,15 @@ struct CodecView {
   const long long* bnd;
   int half, nmax;  // nvbin/2, nvbin/2-1
   float cf, amp;   // vcoef(sigma) and (nvbin-1)/pi as floats (estimate only)
+  const float* cfp;  // when set, cf is read from the device (graph mode)
 };
+__device__ __forceinline__ float codec_cf(const CodecView& k) { return k.cfp ? __ldg(k.cfp) : k.cf; }
 __device__ __forceinline__ double codec_decode(const CodecView& k, int code) { return __ldg(k.dec + code + k.half); }
 __device__ __forceinline__ float2 codec_decode_ff(const CodecView& k, int code) {
   return __ldg(k.dech + code + k.half);
 }
 __device__ __forceinline__ long long codec_encode(const CodecView& k, double v) {
-  return v_encode_tab(v, k.bnd, k.nmax, k.cf, k.amp);
+  return v_encode_tab(v, k.bnd, k.nmax, codec_cf(k), k.amp);
 }
 
 // ---------------------------------------------------------------------------
@@ -343,7 +381,7 @@ __device__ __forceinline__ long long f2d_bits(float f) {
 // an edge in another binade is at least as far as that binade's end.
 __device__ __forceinline__ bool certify_abs(long long ab, float E, const CodecView& k, long long* n_out) {
   float af = approx_float_pos(ab);
-  float u0 = k.amp * atanf(k.cf * af);
+  float u0 = k.amp * atanf(codec_cf(k) * af);
   int m = (int)(u0 + 0.5f);
   long long n = m < 0 ? 0 : (m > k.nmax ? k.nmax : m);
   // the FP32 estimate is within a few hundredths of a code: probe its bin with
@@ -553,6 +591,9 @@ __device__ __forceinline__ void for_box_particles(const int* pref, const long lo
 int cube_build_tables(cube_ctx* c);
 // decode/encode tables for up to two sigma values at once (built on demand)
 int cube_codec_pair(cube_ctx* c, float s1, float s2, CodecView* v1, CodecView* v2);
+// graph mode: tables of a slot from a device sigma; a view reading cf from the device
+int cube_codec_build_dev(cube_ctx* c, int slot, const float* sigp);
+void cube_codec_view_dev(const cube_ctx* c, int slot, const float* cfp, CodecView* v);
 int cube_kernels_init(cube_ctx* c, const float* fine_table, const float* coarse_table);
 int cube_scan_counts(cube_ctx* c, const int32_t* counts, int64_t* starts, int64_t n);
 int cube_update_x_impl(cube_ctx* c, float dt_old, float dt, float vz_max, cube_stats* st);

@@ -41,7 +41,9 @@ __global__ void k_take_imag(const float2* __restrict__ spec, int64_t n, float sc
 }
 
 // LRCKCORR (kernel_c.f90:102-116): for |k|<=8 and k_d != 0 replace K by
-// K*0.25*pi*ksin_d/sum(ksin^2)/Im(FFT(raw)).
+// K*0.25*pi*ksin_d/sum(ksin^2)/Im(FFT(raw)).  At nc = 16 the sphere reaches the
+// Nyquist plane, where the odd raw kernel's transform is exactly zero and the
+// reference would divide 0 by 0; there K keeps its value (also zero).
 __global__ void k_lrck(float* __restrict__ kern, const float2* __restrict__ raw, int nc, int dim) {
   int nh = nc / 2 + 1;
   int64_t n = (int64_t)nh * nc * nc;
@@ -56,6 +58,7 @@ __global__ void k_lrck(float* __restrict__ kern, const float2* __restrict__ raw,
     float s[3];
     for (int d = 0; d < 3; d++) s[d] = 2.f * sinf(CUBE_PI_F * k[d] / (float)nc);
     float ss = (s[0] * s[0] + s[1] * s[1]) + s[2] * s[2];
+    if (raw[i].y == 0.f) continue;
     float v = kern[i];
     v = v * 0.25f;
     v = v * CUBE_PI_F;
@@ -222,7 +225,11 @@ __device__ __forceinline__ float f2sum(float a, float b, float c) {
 // kPre: then rewrite each force value as its kick factor force*a_mid*dt/6/pi
 template <bool kPre>
 __global__ void k_f2max(float* __restrict__ f0, float* __restrict__ f1, float* __restrict__ f2, int n,
-                        unsigned int* __restrict__ out, float a_mid, float dt) {
+                        unsigned int* __restrict__ out, float a_mid, float dt, const StepDev* sd) {
+  if (sd) {  // graph mode
+    a_mid = sd->h.a_mid;
+    dt = sd->h.dt;
+  }
   const int64_t rows = (int64_t)n * n;
   const int h = n >> 1;
   float m = 0.f;
@@ -273,7 +280,11 @@ struct KickArgs {
   int vmax_only;           // recompute the exact vmax of every lane, write nothing
   int exact_only;          // skip the certified fast path
   unsigned long long* nexact;
+  const StepDev* sd;       // graph mode: a_mid, dt, tau from the device
 };
+__device__ __forceinline__ float kick_amid(const KickArgs& a) { return a.sd ? __ldg(&a.sd->h.a_mid) : a.a_mid; }
+__device__ __forceinline__ float kick_dt(const KickArgs& a) { return a.sd ? __ldg(&a.sd->h.dt) : a.dt; }
+__device__ __forceinline__ float kick_tau(const KickArgs& a, int d) { return a.sd ? __ldg(&a.sd->h.tau[d]) : a.tau[d]; }
 
 // The kick velocity of the reference is the FP64 chain
 //   v = decode; v = v + t1; ...; v = v + t8       (pm.f90:145-153)
@@ -287,7 +298,13 @@ struct KickArgs {
 // chain, so the stored code is always the reference's.
 // kPre: the meshes hold force*a_mid*dt/6/pi already (k_f2max<true>)
 template <bool kFine, bool kPre>
-__global__ void k_kick(KickArgs a) {
+__global__ void __launch_bounds__(256, 4) k_kick(KickArgs a) {
+  if (a.vmax_only && a.sd) {  // graph mode: the exact vmax rerun runs only when some component needs it
+    bool need = false;
+    for (int d = 0; d < 3; d++)
+      if (!(__uint_as_float(*(volatile unsigned int*)&a.vmax_bits[d]) >= kick_tau(a, d))) need = true;
+    if (!need) return;
+  }
   const Geo& g = a.g;
   float vm[3] = {0.f, 0.f, 0.f};
   unsigned long long nex = 0;
@@ -324,7 +341,7 @@ __global__ void k_kick(KickArgs a) {
     for (int d = 0; d < 3; d++) {
       const float* F = a.f[d];
       float t[8];
-#define KT(c, wa, wb, wc) (kPre ? kick_w(__ldg(F + (c)), wa, wb, wc) : kick_term(__ldg(F + (c)), a.a_mid, a.dt, wa, wb, wc))
+#define KT(c, wa, wb, wc) (kPre ? kick_w(__ldg(F + (c)), wa, wb, wc) : kick_term(__ldg(F + (c)), kick_amid(a), kick_dt(a), wa, wb, wc))
       t[0] = KT(c111, d1[0], d1[1], d1[2]);
       t[1] = KT(c211, d2[0], d1[1], d1[2]);
       t[2] = KT(c121, d1[0], d2[1], d1[2]);
@@ -351,7 +368,7 @@ __global__ void k_kick(KickArgs a) {
       if (!kFine) {
         vfd = a.vfield[3 * cell + d];
         float ub = (fabsf(vf) + E + fabsf(vfd)) * 1.000001f;
-        need_vmax = a.vmax_only || ub >= a.tau[d];
+        need_vmax = a.vmax_only || ub >= kick_tau(a, d);
       }
       long long out;
       if (ok && !need_vmax) {
@@ -567,10 +584,10 @@ int cube_fine_spectral_impl(cube_ctx* c, cube_stats* st, const float* pre) {
   cube_phase_begin(c, PH_F_F2MAX);
   if (pre)
     k_f2max<true><<<cube_grid((int64_t)c->nf * c->nf, 1, 8), 256, 0, s>>>(
-        c->force_f[0], c->force_f[1], c->force_f[2], c->nf, &c->dstats->f2_fine_bits, pre[0], pre[1]);
+        c->force_f[0], c->force_f[1], c->force_f[2], c->nf, &c->dstats->f2_fine_bits, pre[0], pre[1], c->graph_mode ? c->sd : nullptr);
   else
     k_f2max<false><<<cube_grid((int64_t)c->nf * c->nf, 1, 8), 256, 0, s>>>(
-        c->force_f[0], c->force_f[1], c->force_f[2], c->nf, &c->dstats->f2_fine_bits, 0.f, 0.f);
+        c->force_f[0], c->force_f[1], c->force_f[2], c->nf, &c->dstats->f2_fine_bits, 0.f, 0.f, nullptr);
   cube_phase_end(c, PH_F_F2MAX);
   CUBE_CUDA(c, cudaGetLastError());
   if (st) {
@@ -584,8 +601,14 @@ int cube_fine_spectral_impl(cube_ctx* c, cube_stats* st, const float* pre) {
 
 int cube_fine_kick_impl(cube_ctx* c, float a_mid, float dt, bool pre) {
   KickArgs k{};
-  int r = cube_codec_pair(c, c->sigma_vi, c->sigma_vi_new, &k.cin, &k.cout);
-  if (r) return r;
+  if (c->graph_mode) {  // decode with sigma_vi (slot 0), encode with sigma_vi_new (slot 1)
+    cube_codec_view_dev(c, 0, &c->sd->h.cf_vi, &k.cin);
+    cube_codec_view_dev(c, 1, &c->sd->cf_new, &k.cout);
+    k.sd = c->sd;
+  } else {
+    int r = cube_codec_pair(c, c->sigma_vi, c->sigma_vi_new, &k.cin, &k.cout);
+    if (r) return r;
+  }
   k.g = make_geo(c);
   k.np = c->np;
   k.xp = c->xp[c->cur];
@@ -665,10 +688,10 @@ int cube_coarse_spectral_impl(cube_ctx* c, cube_stats* st, const float* pre) {
     CUBE_FFT(c, cufftExecC2R(c->plan_c_c2r, (cufftComplex*)c->force_c[d], c->force_c[d]));
   if (pre)
     k_f2max<true><<<cube_grid((int64_t)nc * nc, 1, 8), 256, 0, s>>>(c->force_c[0], c->force_c[1], c->force_c[2], nc,
-                                                                    &c->dstats->f2_coarse_bits, pre[0], pre[1]);
+                                                                    &c->dstats->f2_coarse_bits, pre[0], pre[1], c->graph_mode ? c->sd : nullptr);
   else
     k_f2max<false><<<cube_grid((int64_t)nc * nc, 1, 8), 256, 0, s>>>(c->force_c[0], c->force_c[1], c->force_c[2], nc,
-                                                                     &c->dstats->f2_coarse_bits, 0.f, 0.f);
+                                                                     &c->dstats->f2_coarse_bits, 0.f, 0.f, nullptr);
   cube_phase_end(c, PH_C_FFT);
   CUBE_CUDA(c, cudaGetLastError());
   if (st) {
@@ -682,8 +705,15 @@ int cube_coarse_spectral_impl(cube_ctx* c, cube_stats* st, const float* pre) {
 
 int cube_coarse_kick_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st, bool pre) {
   KickArgs k{};
-  int r = cube_codec_pair(c, c->sigma_vi, c->sigma_vi, &k.cin, &k.cout);
-  if (r) return r;
+  int r;
+  if (c->graph_mode) {  // sigma_vi is now sigma_vi_new (slot 1) for both
+    cube_codec_view_dev(c, 1, &c->sd->cf_new, &k.cin);
+    cube_codec_view_dev(c, 1, &c->sd->cf_new, &k.cout);
+    k.sd = c->sd;
+  } else {
+    r = cube_codec_pair(c, c->sigma_vi, c->sigma_vi, &k.cin, &k.cout);
+    if (r) return r;
+  }
   int cur = c->cur, alt = 1 - cur;
   CUBE_CUDA(c, cudaMemsetAsync(c->dstats->vmax_bits, 0, 12, c->stream));
   CUBE_CUDA(c, cudaMemsetAsync(&c->dstats->nexact, 0, 8, c->stream));
@@ -713,6 +743,21 @@ int cube_coarse_kick_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st, bo
     k_kick<false, false><<<cube_grid(c->np, 256), 256, 0, c->stream>>>(k);
   cube_phase_end(c, PH_C_KICK);
   CUBE_CUDA(c, cudaGetLastError());
+  if (c->graph_mode) {
+    // the exact rerun decides on the device whether it runs; the stats of the
+    // whole particle_mesh go to the host's copy
+    k.vmax_only = 1;
+    if (pre)
+      k_kick<false, true><<<cube_grid(c->np, 256), 256, 0, c->stream>>>(k);
+    else
+      k_kick<false, false><<<cube_grid(c->np, 256), 256, 0, c->stream>>>(k);
+    CUBE_CUDA(c, cudaGetLastError());
+    CUBE_CUDA(c, cudaMemcpyAsync(&c->sout->coarse, c->dstats, sizeof(DevStats), cudaMemcpyDeviceToDevice, c->stream));
+    void* t = c->vp[cur];
+    c->vp[cur] = c->vp[alt];
+    c->vp[alt] = t;
+    return CUBE_OK;
+  }
   r = cube_stats_fetch(c);
   if (r) return r;
   float vm[3];

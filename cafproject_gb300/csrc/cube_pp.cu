@@ -71,7 +71,10 @@ struct PPArgs {
   int* list[4];    // work of levels 1..4: bricks, bricks, cells, cells
   int* nlist;      // their lengths
   DevStats* st;
+  const StepDev* sd;  // graph mode: the kick factors from the device
 };
+__device__ __forceinline__ float pp_kick_f(const PPArgs& a) { return a.sd ? __ldg(&a.sd->h.kick_f) : a.kick_f; }
+__device__ __forceinline__ double pp_kick_d(const PPArgs& a) { return a.sd ? __ldg(&a.sd->h.kick) : a.kick; }
 
 __device__ __forceinline__ float fine_off(int code, int izipx) {
   // ncell*(int(xp+ishift)+rshift)*x_resolution: exact in real(4)
@@ -126,14 +129,14 @@ __device__ __forceinline__ float pp_kick(const PPArgs& a, int64_t p, const long 
     int code = load_code(a.vp, 3 * p + d, g.izipv);
     // vreal=vreal+f_tot*a_mid*dt/6/pi (ext_pp_force.f90:116), then the code
     float dh = codec_decode_ff(a.cv, code).x;
-    float kf = __fmul_rn(F[d], a.kick_f);
+    float kf = __fmul_rn(F[d], pp_kick_f(a));
     float vf = __fadd_rn(dh, kf);
     float E = 1.25f * (fabsf(kf) * 1.3e-7f + (2.f * fabsf(dh) + fabsf(vf)) * 6.0e-8f);
     long long n = 0, out;
     if (!a.exact_only && certify_abs(f2d_bits(vf) & 0x7fffffffffffffffLL, E, a.cv, &n)) {
       out = vf < 0.f ? -n : n;
     } else {
-      out = pp_kick_exact(a.cv, code, F[d], a.kick);
+      out = pp_kick_exact(a.cv, code, F[d], pp_kick_d(a));
     }
     store_code(a.vp, 3 * p + d, g.izipv, out);
     if (a.fpp) a.fpp[3 * p + d] = F[d];
@@ -349,8 +352,14 @@ __global__ void k_pp_list_all(int* list, int n, int* count) {
 
 int cube_pp_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st) {
   PPArgs a{};
-  int r = cube_codec_pair(c, c->sigma_vi, c->sigma_vi, &a.cv, nullptr);
-  if (r) return r;
+  int r;
+  if (c->graph_mode) {
+    cube_codec_view_dev(c, 0, &c->sd->h.cf_vi, &a.cv);
+    a.sd = c->sd;
+  } else {
+    r = cube_codec_pair(c, c->sigma_vi, c->sigma_vi, &a.cv, nullptr);
+    if (r) return r;
+  }
   CUBE_CUDA(c, cudaMemsetAsync(c->dstats, 0, sizeof(DevStats), c->stream));
   a.g = make_geo(c);
   a.np = c->np;
@@ -397,6 +406,10 @@ int cube_pp_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st) {
   k_pp_dense<<<persist, PP_THREADS, 0, c->stream>>>(a);
   CUBE_CUDA(c, cudaGetLastError());
   cube_phase_end(c, PH_PP);
+  if (c->graph_mode) {
+    CUBE_CUDA(c, cudaMemcpyAsync(&c->sout->pp, c->dstats, sizeof(DevStats), cudaMemcpyDeviceToDevice, c->stream));
+    return CUBE_OK;
+  }
   CUBE_CUDA(c, cudaMemcpyAsync(c->pp_nlist_host, c->pp_nlist, 4 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   r = cube_stats_fetch(c);
   if (r) return r;

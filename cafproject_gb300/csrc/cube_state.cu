@@ -171,8 +171,10 @@ int cube_build_tables(cube_ctx* c) {
   return CUBE_OK;
 }
 
-__global__ void k_decode_table(const float* __restrict__ tan_tab, int nv, float sigma, double* __restrict__ dec,
-                               float2* __restrict__ dech) {
+// sigp, when set, supplies sigma from the device (graph mode)
+__global__ void k_decode_table(const float* __restrict__ tan_tab, int nv, float sigma, const float* sigp,
+                               double* __restrict__ dec, float2* __restrict__ dech) {
+  if (sigp) sigma = *sigp;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < nv) {
     double d = __ddiv_rn((double)tan_tab[i], vcoef(sigma));
@@ -184,21 +186,58 @@ __global__ void k_decode_table(const float* __restrict__ tan_tab, int nv, float 
 
 // bnd[n] = bit pattern of the smallest double a >= 0 with
 // u(a) = real(nvbin-1)*atan(vcoef*a)/pi >= n - 0.5, i.e. where nint(u) reaches n
-// (update_particle.f90:117).  Bisection over the ordered non-negative doubles:
-// u(0) = 0 < 0.5 and u(+inf) = (nvbin-1)/2 * pi/pi_f > nvbin/2 - 1.5.
-__global__ void k_encode_bounds(float sigma, int nvbin, long long* __restrict__ bnd) {
+// (update_particle.f90:117).  Bisection over the ordered non-negative doubles,
+// keeping u(lo) < n - 0.5 <= u(hi): u(0) = 0 < 0.5 and u(+inf) =
+// (nvbin-1)/2 * pi/pi_f > nvbin/2 - 1.5.  The bracket starts from the
+// closed-form inverse tan(thr*pi/(nvbin-1))/vcoef (a few ulps off) and widens
+// geometrically until it holds, so a boundary costs about a dozen FP64 atan
+// evaluations instead of 64; the result is the same smallest double.
+__device__ __forceinline__ double enc_u(long long bits, double c, int nvbin) {
+  return __ddiv_rn(__dmul_rn((double)(nvbin - 1), atan(__dmul_rn(c, __longlong_as_double(bits)))), (double)CUBE_PI_F);
+}
+__global__ void k_encode_bounds(float sigma, const float* sigp, int nvbin, long long* __restrict__ bnd) {
+  if (sigp) sigma = *sigp;
   int n = blockIdx.x * blockDim.x + threadIdx.x + 1;
   int nmax = nvbin / 2 - 1;
   if (n == 1) bnd[0] = 0;
   if (n > nmax) return;
   double c = vcoef(sigma);
   double thr = (double)n - 0.5;
-  long long lo = 0, hi = 0x7ff0000000000000LL;
+  const long long kInf = 0x7ff0000000000000LL;
+  long long lo = 0, hi = kInf;
+  const double a = tan(thr * (double)CUBE_PI_F / (double)(nvbin - 1)) / c;
+  if (a > 0.0 && a < 1.0e300) {
+    const long long g = __double_as_longlong(a);
+    long long step = 16;
+    if (enc_u(g, c, nvbin) >= thr) {
+      hi = g;
+      for (int it = 0; it < 40; it++) {
+        const long long t = g - step;
+        if (t <= 0) break;
+        if (enc_u(t, c, nvbin) < thr) {
+          lo = t;
+          break;
+        }
+        hi = t;
+        step *= 4;
+      }
+    } else {
+      lo = g;
+      for (int it = 0; it < 40; it++) {
+        const long long t = g + step;
+        if (t >= kInf) break;
+        if (enc_u(t, c, nvbin) >= thr) {
+          hi = t;
+          break;
+        }
+        lo = t;
+        step *= 4;
+      }
+    }
+  }
   while (hi - lo > 1) {
     long long mid = lo + (hi - lo) / 2;
-    double u = __ddiv_rn(__dmul_rn((double)(nvbin - 1), atan(__dmul_rn(c, __longlong_as_double(mid)))),
-                         (double)CUBE_PI_F);
-    if (u >= thr)
+    if (enc_u(mid, c, nvbin) >= thr)
       hi = mid;
     else
       lo = mid;
@@ -214,16 +253,26 @@ static void view_of(const cube_ctx* c, const cube_ctx::Codec& k, CodecView* v) {
   v->nmax = c->nvbin / 2 - 1;
   v->cf = (float)vcoef_host(k.sigma);
   v->amp = (float)((double)(c->nvbin - 1) / (double)CUBE_PI_F);
+  v->cfp = nullptr;
 }
 
-static int build_codec(cube_ctx* c, int slot, float sigma) {
+static int build_codec(cube_ctx* c, int slot, float sigma, const float* sigp = nullptr) {
   cube_ctx::Codec& k = c->codec[slot];
-  k_decode_table<<<(c->nvbin + 255) / 256, 256, 0, c->stream>>>(c->tan_tab, c->nvbin, sigma, k.dec, k.dech);
+  k_decode_table<<<(c->nvbin + 255) / 256, 256, 0, c->stream>>>(c->tan_tab, c->nvbin, sigma, sigp, k.dec, k.dech);
   int nmax = c->nvbin / 2 - 1;
-  k_encode_bounds<<<(nmax + 127) / 128, 128, 0, c->stream>>>(sigma, c->nvbin, k.bnd);
+  k_encode_bounds<<<(nmax + 127) / 128, 128, 0, c->stream>>>(sigma, sigp, c->nvbin, k.bnd);
   CUBE_CUDA(c, cudaGetLastError());
   k.sigma = sigma;
   return CUBE_OK;
+}
+
+// graph mode: the tables of slot from the sigma in device memory, and a view
+// of a slot whose estimate coefficient is read from the device
+int cube_codec_build_dev(cube_ctx* c, int slot, const float* sigp) { return build_codec(c, slot, -1.f, sigp); }
+void cube_codec_view_dev(const cube_ctx* c, int slot, const float* cfp, CodecView* v) {
+  view_of(c, c->codec[slot], v);
+  v->cf = 0.f;
+  v->cfp = cfp;
 }
 
 // Make the tables for s1 and s2 resident (at most two slots; the slot of the

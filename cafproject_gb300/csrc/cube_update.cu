@@ -54,7 +54,15 @@ struct UpdArgs {
   void* vp_new;
   int32_t* pid_new;
   int32_t* pcell_new;
+  const StepDev* sd;  // graph mode: dt_mid and nlayer from the device
 };
+
+__device__ __forceinline__ float dtm(const UpdArgs& a) { return a.sd ? __ldg(&a.sd->h.dt_mid) : a.dt_mid; }
+__device__ __forceinline__ int nlay(const UpdArgs& a) { return a.sd ? __ldg(&a.sd->h.nlayer) : a.nlayer; }
+// graph mode runs both rank paths' launches; each skips itself on the device:
+// the walker unless the counting path flagged itself inapplicable, the
+// counting path's placement when it did
+__device__ __forceinline__ bool counting_failed(const UpdArgs& a) { return (*(volatile int*)&a.st->flags & 12) != 0; }
 
 
 // global coarse coordinate of tile-local cell l (1-based) of tile coordinate t
@@ -113,9 +121,9 @@ __global__ void k_dest(UpdArgs a) {
       // fast path: v = dec+vfield, P = dt_mid*v, deltax = P/4 in FP32 with bound Edx
       float dh = codec_decode_ff(a.cv, vcode).x;
       float vfa = __fadd_rn(dh, vfd);
-      float Pf = __fmul_rn(a.dt_mid, vfa);
+      float Pf = __fmul_rn(dtm(a), vfa);
       float dxf = __fmul_rn(Pf, 0.25f);
-      float Edx = 0.25f * (fabsf(a.dt_mid) * (fabsf(dh) + fabsf(vfa)) * 1.2e-7f + fabsf(Pf) * 6.0e-8f);
+      float Edx = 0.25f * (fabsf(dtm(a)) * (fabsf(dh) + fabsf(vfa)) * 1.2e-7f + fabsf(Pf) * 6.0e-8f);
       float offf = __fmul_rn(pos_off_f(xcode, g.izipx), g.izipx == 1 ? 1.0f / 256.0f : 1.0f / 65536.0f);
       nval[d] = 0;
       oa[d] = ob[d] = ga[d] = gb[d] = 0;
@@ -132,7 +140,7 @@ __global__ void k_dest(UpdArgs a) {
         if (clo == chi && !a.exact_only) {
           ig = (int)chi;
         } else {
-          ig = dest_exact(a.cv, vcode, vfd, a.dt_mid, Ls, offf);
+          ig = dest_exact(a.cv, vcode, vfd, dtm(a), Ls, offf);
         }
         if (ig < 1 - 2 * g.ncb || ig > g.nt + 2 * g.ncb) {
           far = true;
@@ -318,7 +326,7 @@ __global__ void k_rank_base(UpdArgs a) {
 #pragma unroll
     for (int i = 0; i < 3; i++) {
       int kl = Dl[2] + i - 1;
-      key[i] = ((kl + g.ncb - 1) % a.nlayer) * 4096 + kl + 8;
+      key[i] = ((kl + g.ncb - 1) % nlay(a)) * 4096 + kl + 8;
     }
     int zo[3] = {0, 1, 2};  // slab index dz+1
     if (key[1] < key[0]) { int t = key[0]; key[0] = key[1]; key[1] = t; t = zo[0]; zo[0] = zo[1]; zo[1] = t; }
@@ -353,6 +361,7 @@ __global__ void k_rank_base(UpdArgs a) {
 }
 
 __global__ void k_rank_place(UpdArgs a) {
+  if (a.sd && counting_failed(a)) return;
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.np; p += (int64_t)gridDim.x * blockDim.x) {
     int32_t D = a.dest[p];
     if (D < 0) continue;
@@ -364,6 +373,7 @@ __global__ void k_rank_place(UpdArgs a) {
 }
 
 __global__ void k_vfield_new(UpdArgs a) {
+  if (a.sd && counting_failed(a)) return;
   for (int64_t D = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; D < a.ncells;
        D += (int64_t)gridDim.x * blockDim.x) {
     float acc[3];
@@ -384,6 +394,7 @@ __global__ void k_vfield_new(UpdArgs a) {
 
 // U2: one thread per destination cell walks the sources in visit order.
 __global__ void k_rank(UpdArgs a) {
+  if (a.sd && !counting_failed(a)) return;
   const Geo& g = a.g;
   int R = min(a.st->max_disp, 2 * g.ncb);
   int64_t nx = (int64_t)(a.st->ndup_list < (unsigned long long)a.xtra_cap ? a.st->ndup_list : (unsigned long long)a.xtra_cap);
@@ -401,11 +412,11 @@ __global__ void k_rank(UpdArgs a) {
     for (int o = -R; o <= R; o++) {
       int kl = Dl[2] + o;
       if (kl < 1 - g.ncb || kl > g.nt + g.ncb) continue;
-      int lay = (kl + g.ncb - 1) % a.nlayer;
+      int lay = (kl + g.ncb - 1) % nlay(a);
       int pos = nz++;
       while (pos > 0) {
         int ko = Dl[2] + dz[pos - 1];
-        int lo = (ko + g.ncb - 1) % a.nlayer;
+        int lo = (ko + g.ncb - 1) % nlay(a);
         if (lo > lay || (lo == lay && ko > kl)) {
           dz[pos] = dz[pos - 1];
           pos--;
@@ -477,12 +488,12 @@ __device__ __forceinline__ void write_particle(const UpdArgs& a, int64_t p, int3
     float2 dd = codec_decode_ff(a.cv, vcode);
     // drift in code units: FP32 estimate of dt_mid*(dec+vfield)*scale with its bound
     float vfa = __fadd_rn(dd.x, vfd);
-    float Pf = __fmul_rn(a.dt_mid, vfa);
-    float EP = scale * 1.25f * (fabsf(a.dt_mid) * (fabsf(dd.x) + fabsf(vfa)) * 1.2e-7f + fabsf(Pf) * 6.0e-8f);
+    float Pf = __fmul_rn(dtm(a), vfa);
+    float EP = scale * 1.25f * (fabsf(dtm(a)) * (fabsf(dd.x) + fabsf(vfa)) * 1.2e-7f + fabsf(Pf) * 6.0e-8f);
     long long dx;
     if (a.exact_only || !nint_certified(__fmul_rn(Pf, scale), EP, &dx)) {
       double v = __dadd_rn(codec_decode(a.cv, vcode), (double)vfd);
-      dx = llround(__dmul_rn(__dmul_rn((double)a.dt_mid, v), (double)scale));
+      dx = llround(__dmul_rn(__dmul_rn((double)dtm(a), v), (double)scale));
     }
     long long x = load_code(a.xp, 3 * p + d, g.izipx);
     store_code(a.xp_new, 3 * idx + d, g.izipx, x + dx);
@@ -578,9 +589,102 @@ __global__ void k_sigma(const void* __restrict__ vp, const int32_t* __restrict__
   }
 }
 
+// graph mode: sigma_vi_new from the block partials on the device, with the
+// host path's arithmetic (the same summation order, correctly rounded sqrt
+// and division), its vcoef for the encode estimate, and the sums for the host
+__global__ void k_sigma_final(const double* __restrict__ part, int nb, double npg, StepDev* sd, StepOut* so) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  double s[3] = {0.0, 0.0, 0.0};
+  for (int b = 0; b < nb; b++)
+    for (int t = 0; t < 3; t++) s[t] += part[3 * b + t];
+  const double std_res = sqrt(s[1] / npg);
+  const float sn = (float)(std_res / (double)sqrtf(3.0f));  // update_particle.f90:224
+  sd->sigma_new = sn;
+  sd->cf_new = sn > 0.f ? (float)vcoef(sn) : 0.f;
+  if (so) {
+    for (int t = 0; t < 3; t++) so->sums[t] = s[t];
+    so->sigma_new = sn;
+  }
+}
+
 }  // namespace
 
+// update_x inside a captured graph (cube_batch_*): the step scalars come from
+// c->sd, both rank paths are launched and each decides on the device whether
+// it runs, the extra-copy list is walked up to its device count, and
+// sigma_vi_new and its codec tables (slot 1) are computed on the device.  The
+// particle count of an image never changes (the box is periodic), so every
+// grid is fixed.  Stats land in c->sout->upd; the host checks them after the
+// step.
+static int update_x_graph(cube_ctx* c) {
+  Geo g = make_geo(c);
+  int k = c->cur, kn = 1 - k;
+  CodecView cv;
+  cube_codec_view_dev(c, 0, &c->sd->h.cf_vi, &cv);
+  CUBE_CUDA(c, cudaMemsetAsync(c->dstats, 0, sizeof(DevStats), c->stream));
+  UpdArgs a{};
+  a.g = g;
+  a.np = c->np;
+  a.ncells = c->ncells;
+  a.dt_mid = 0.f;
+  a.nlayer = 1;
+  a.sd = c->sd;
+  a.xp = c->xp[k];
+  a.vp = c->vp[k];
+  a.pid = c->pid[k];
+  a.pcell = c->pcell[k];
+  a.vfield = c->vfield[k];
+  a.cstart = c->cstart[k];
+  a.cv = cv;
+  a.exact_only = c->opt_exact_kicks;
+  a.dest = c->dest;
+  a.dframe = c->dframe;
+  a.doff = c->doff;
+  a.lrank = c->lrank;
+  a.offc = c->offc;
+  a.perm = c->perm;
+  a.rank = c->rank;
+  a.xtra = c->xtra;
+  a.xtra_cap = c->xtra_cap;
+  a.st = c->dstats;
+  a.cnt_new = c->rhoc[kn];
+  a.vfield_new = c->vfield[kn];
+  a.cstart_new = c->cstart[kn];
+  a.xp_new = c->xp[kn];
+  a.vp_new = c->vp[kn];
+  a.pid_new = c->pid[kn];
+  a.pcell_new = c->pcell[kn];
+  const int B = 256;
+  cudaStream_t s = c->stream;
+  CUBE_CUDA(c, cudaMemsetAsync(c->rank, 0xFF, 4 * (size_t)c->np, s));
+  k_dest<<<cube_grid(c->np, B), B, 0, s>>>(a);
+  CUBE_CUDA(c, cudaMemsetAsync(c->offc, 0, sizeof(uint16_t) * NOFF * (size_t)c->ncells, s));
+  k_rank_local<<<cube_grid(c->np, 256), 256, 0, s>>>(a);
+  k_rank_base<<<cube_grid(c->ncells, 256), 256, 0, s>>>(a);
+  k_rank<<<cube_grid(c->ncells, 128, 32), 128, 0, s>>>(a);
+  CUBE_CUDA(c, cudaGetLastError());
+  int r = cube_scan_counts(c, c->rhoc[kn], c->cstart[kn], c->ncells);
+  if (r) return r;
+  k_rank_place<<<cube_grid(c->np, B), B, 0, s>>>(a);
+  k_vfield_new<<<cube_grid(c->ncells, 128, 32), 128, 0, s>>>(a);
+  k_scatter<<<cube_grid(c->np, B), B, 0, s>>>(a);
+  k_scatter_xtra<<<cube_grid(c->xtra_cap, B, 2), B, 0, s>>>(a);
+  const int nb = c->red_blocks;
+  k_sigma<<<nb, 256, 0, s>>>(c->vp[kn], c->pcell[kn], c->vfield[kn], c->np, c->ncells, cv.dech, c->nvbin, c->p.izipv,
+                             c->red_tmp);
+  const double npg = (double)(c->npglobal > 0 ? c->npglobal : c->np);
+  k_sigma_final<<<1, 32, 0, s>>>(c->red_tmp, nb, npg, c->sd, c->sout);
+  CUBE_CUDA(c, cudaGetLastError());
+  CUBE_CUDA(c, cudaMemcpyAsync(&c->sout->upd, c->dstats, sizeof(DevStats), cudaMemcpyDeviceToDevice, s));
+  r = cube_codec_build_dev(c, 1, &c->sd->sigma_new);
+  if (r) return r;
+  c->cur = kn;
+  c->rank_walked = 0;
+  return CUBE_OK;
+}
+
 int cube_update_x_impl(cube_ctx* c, float dt_old, float dt, float vz_max, cube_stats* st) {
+  if (c->graph_mode) return update_x_graph(c);
   Geo g = make_geo(c);
   int k = c->cur, kn = 1 - k;
   float dt_mid = (dt_old + dt) / 2.0f;  // update_particle.f90:32

@@ -35,7 +35,9 @@ EXPORTS = ["cube_create", "cube_destroy", "cube_last_error", "cube_upload_state"
            "cube_power_spectrum", "cube_checkpoint_write", "cube_checkpoint_read", "cube_ic_zeldovich", "cube_create_linked", "cube_particle_mesh2", "cube_set_option",
            "cube_dpm_create", "cube_dpm_destroy", "cube_dpm_last_error", "cube_dpm_stream", "cube_dpm_nparticles",
            "cube_dpm_set_schedule", "cube_dpm_noise", "cube_dpm_forward", "cube_dpm_backward", "cube_dpm_density",
-           "cube_dpm_density_adjoint", "cube_dpm_tables", "cube_dpm_info"]
+           "cube_dpm_density_adjoint", "cube_dpm_tables", "cube_dpm_info",
+           "cube_batch_create", "cube_batch_destroy", "cube_batch_last_error", "cube_batch_set_schedule",
+           "cube_batch_autotune", "cube_batch_step", "cube_batch_history", "cube_batch_ctx", "cube_batch_time"]
 CODEC_STATIC_MAX = 16384
 OPT_EXACT_KICKS = 1
 OPT_PP_LEVEL = 2
@@ -187,12 +189,20 @@ class CubeGPU:
             self.h = None
             raise CubeError(rc, msg)
 
+    @classmethod
+    def borrow(cls, handle, params):
+        """A view of a context owned elsewhere (a box of a cube_batch): the
+        same methods, and close() leaves the context alone."""
+        g = cls.__new__(cls)
+        g.p, g.L, g._cp, g.owner, g.h, g._borrowed = params, load_library(), params.to_c(), None, handle, True
+        return g
+
     def _check(self, rc):
         if rc:
             raise CubeError(rc, self.L.cube_last_error(self.h).decode())
 
     def close(self):
-        if self.h is not None and self.h.value:
+        if self.h is not None and self.h.value and not getattr(self, "_borrowed", False):
             self.L.cube_destroy(self.h)
         self.h = None
 

@@ -54,27 +54,13 @@ def schedule(z_init, z_final, nsteps, omega_m=0.3, omega_l=0.7):
     drift is dt_mid = (dt_old + dt)/2 (update_particle.f90:32, dt_old = 0 on
     the first step) and the kick a_mid*dt/(6 pi) (pm.f90:162).
     Returns (drift, kick, a) with a the nsteps+1 scale factors."""
-    a0, a1 = 1.0 / (1.0 + z_init), 1.0 / (1.0 + z_final)
-    a = np.linspace(a0, a1, nsteps + 1).astype(np.float32)
+    dts, amids, a = cm.fixed_schedule(z_init, z_final, nsteps, omega_m, omega_l, spacing="linear")
     drift, kick = np.zeros(nsteps, np.float32), np.zeros(nsteps, np.float32)
     dt_old = np.float32(0)
     for i in range(nsteps):
-        target = float(a[i + 1]) - float(a[i])
-        lo, hi = 0.0, 1.0
-        while sum(cm.expansion(a[i], hi, omega_m, omega_l)) < target:
-            hi *= 2
-        for _ in range(60):
-            mid = 0.5 * (lo + hi)
-            if sum(float(d) for d in cm.expansion(a[i], mid, omega_m, omega_l)) < target:
-                lo = mid
-            else:
-                hi = mid
-        dt = np.float32(hi)
-        d1, d2 = cm.expansion(a[i], dt, omega_m, omega_l)
-        a_mid = np.float32(a[i] + np.float32(np.float32(d1 + d2) / np.float32(2)))
-        drift[i] = np.float32((dt_old + dt) / np.float32(2))
-        kick[i] = np.float32(a_mid * dt * cm.GG)
-        dt_old = dt
+        drift[i] = np.float32((dt_old + dts[i]) / np.float32(2))
+        kick[i] = np.float32(amids[i] * dts[i] * cm.GG)
+        dt_old = dts[i]
     return drift, kick, a
 
 

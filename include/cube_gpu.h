@@ -293,6 +293,48 @@ int cube_codec_check_static(cube_ctx* ctx, float sigma, const double* v, int64_t
                             int32_t* table);
 
 /* ------------------------------------------------------------------------
+   Batched ensemble (no reference counterpart: the reference runs one
+   universe per job and batches jobs with shell scripts).  Independent boxes,
+   each a single-tile image with its own sizes, cosmology and seed (Zel'dovich
+   initial conditions of cube_ic_zeldovich) and its own fixed step schedule.
+   CUBE_BATCH_GRAPH advances every box one step per launch of a captured CUDA
+   graph (one branch per box, the plain path's kernels, every per-step
+   decision on the device); CUBE_BATCH_SERIAL runs the same schedule through
+   the plain entry points one box after another.  Both give the same state. */
+typedef struct cube_batch cube_batch;
+typedef struct cube_batch_box {
+  cube_params params;    /* nnt = 1 */
+  cube_cosmology cosmo;
+  float z_init;
+  uint32_t seed;
+} cube_batch_box;
+typedef struct cube_batch_stats {  /* one box, one step */
+  float sigma_vi_new;
+  float f2_max_fine, f2_max_coarse, f2_max_pp;
+  float vmax[3];
+  int32_t flags;       /* update_x flags: 1 displacement, 2 rank, 4/8 walker used */
+  int64_t npairs, itest1, ndup;
+  double sum_r;        /* sigma sum of squares */
+} cube_batch_stats;
+#define CUBE_BATCH_GRAPH 0
+#define CUBE_BATCH_SERIAL 1
+int cube_batch_create(const cube_batch_box* boxes, int nbox, const float* fine_table, const float* coarse_table,
+                      int device, int mode, cube_batch** out);
+int cube_batch_destroy(cube_batch* batch);
+const char* cube_batch_last_error(const cube_batch* batch);
+/* dt and a_mid per box and step, host arrays [nbox][nsteps]; dt_old of the
+   first step is 0 (timestep.f90:4) */
+int cube_batch_set_schedule(cube_batch* batch, int nsteps, const float* dt, const float* a_mid);
+/* per distinct box geometry, the PP start level (its staging tile shapes)
+   with the least device time; levels[nbox] receives the choice */
+int cube_batch_autotune(cube_batch* batch, int32_t* levels);
+/* advance every box nsteps steps of its schedule */
+int cube_batch_step(cube_batch* batch, int nsteps);
+int cube_batch_history(cube_batch* batch, int step, cube_batch_stats* out);  /* nbox entries */
+int cube_batch_ctx(cube_batch* batch, int box, cube_ctx** ctx);  /* the box's context */
+int cube_batch_time(const cube_batch* batch, float* last_ms, float* last_dev_ms, int64_t* steps_done);
+
+/* ------------------------------------------------------------------------
    Differentiable form (no reference counterpart: the reference has no
    gradients).  A single-level PM integrator on decoded FP32 positions --
    deposit, Green's multiply (-4 pi/khat^2), central-difference force, kick,

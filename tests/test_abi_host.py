@@ -42,13 +42,13 @@ def test_stats_struct_layout():
 def test_cube_create_rejects_bad_sizes(built_lib):
     from cafproject_gb300 import cube
     L = cube.load_library()
-    bad = P.CubeParams(nc=16, nnt=1).to_c()
+    bad = P.CubeParams(nc=14, nnt=1).to_c()
     fine, coarse = cube.force_tables()
     h = ctypes.c_void_p()
     rc = L.cube_create(ctypes.byref(bad), fine.ctypes.data_as(ctypes.c_void_p),
                        coarse.ctypes.data_as(ctypes.c_void_p), 0, ctypes.byref(h))
     assert rc == 1  # CUBE_ERR_ARG before any device call
-    assert b"exceed 16" in L.cube_last_error(h)
+    assert b"at least 16" in L.cube_last_error(h)
     L.cube_destroy(h)
 
 

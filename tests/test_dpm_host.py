@@ -74,3 +74,19 @@ def test_green_table_is_the_discrete_laplacian_inverse():
     s = (2 * np.sin(np.pi * k / ng)) ** 2
     k2 = s[: ng // 2 + 1][None, None, :] + s[None, :, None] + s[:, None, None]
     assert np.allclose((g * k2)[k2 > 0], -4 * np.pi)
+
+
+def test_fixed_log_schedule_and_ensemble():
+    from cafproject_gb300 import batch as B
+    from cafproject_gb300 import cosmology as cm
+    dt, am, a = cm.fixed_schedule(19.0, 0.0, 50, 0.3, 0.7, "log")
+    assert abs(a[0] - 0.05) < 1e-7 and abs(a[-1] - 1.0) < 1e-6
+    r = a[1:] / a[:-1]
+    assert np.allclose(r, r[0], rtol=1e-4)  # equal steps in ln a
+    assert np.all((am > a[:-1]) & (am < a[1:]))
+    ens = B.ensemble(256)
+    sizes = sorted({p.nc * 2 for p, _ in ens})
+    assert sizes == [32, 48, 64, 96, 128]
+    assert all(0.25 <= p.omega_m <= 0.35 and 0.7 <= p.s8 <= 0.9 for p, _ in ens)
+    assert all(p.nf == 4 * p.nc and p.nnt == 1 for p, _ in ens)  # fine mesh: twice the particle grid
+    assert [s for _, s in ens] == list(range(1, 257))
