@@ -96,17 +96,21 @@ __device__ __forceinline__ float from_fix(long long q) {
   return neg ? -r : r;
 }
 
-// one pair: accumulate the force of a particle at offset r (FP32)
+// one pair: accumulate the force of a particle at offset r (FP32).  1/|r|
+// comes from the hardware reciprocal square root (a few ulps; the pair sum's
+// tolerance against the reference's FP64 is 1e-5), which spares the IEEE
+// square root and division their multi-instruction sequences.
 __device__ __forceinline__ void pair_force(const PPArgs& a, float rx, float ry, float rz, long long* acc) {
   // explicit roundings: every kernel evaluates the same bits for a pair
   float r2 = __fmaf_rn(rx, rx, __fmaf_rn(ry, ry, __fmul_rn(rz, rz)));
-  float rm = __fsqrt_rn(r2);
-  if (!(rm > a.rsoft)) return;  // merge(force,0,rmag>rsoft); self pairs have rm=0
+  float ri = rsqrtf(r2);        // +inf for the self pair
+  float rm = __fmul_rn(r2, ri);  // NaN for the self pair
+  if (!(rm > a.rsoft)) return;  // merge(force,0,rmag>rsoft); self pairs excluded
   float rc = __fmul_rn(rm, a.inv_cut);
   float rc3 = __fmul_rn(__fmul_rn(rc, rc), rc);
   // pcut = 1 - 1.75 rc^3 + 0.75 rc^5  (ext_pp_force.f90:107)
   float pcut = __fmaf_rn(__fmul_rn(0.75f, rc3), __fmul_rn(rc, rc), __fmaf_rn(-1.75f, rc3, 1.0f));
-  float s = __fdiv_rn(__fmul_rn(a.mass, pcut), __fmul_rn(r2, rm));
+  float s = __fmul_rn(__fmul_rn(a.mass, pcut), __fmul_rn(__fmul_rn(ri, ri), ri));
   acc[0] += to_fix(__fmul_rn(s, rx));
   acc[1] += to_fix(__fmul_rn(s, ry));
   acc[2] += to_fix(__fmul_rn(s, rz));
@@ -161,7 +165,7 @@ __device__ __forceinline__ void pp_reduce(const PPArgs& a, unsigned long long np
 struct PPSmem {
   int pref[PNS_MAX + 1];         // ring-and-block particles before each staged cell
   long long sstart[PNS_MAX];     // first particle of each staged cell
-  int nst;                       // staged particles
+  int ncore, nring;              // staged particles of the block (slots from 0 up) and of the ring (from CAP-1 down)
 };
 
 struct PPAcc {
@@ -171,8 +175,10 @@ struct PPAcc {
 
 // Pair forces + kicks for the B[0]xB[1]xB[2] coarse cells starting at C0.
 // The particles of the block and of the fine-cell layer around it are staged
-// (compacted), binned by fine cell (counting sort of slot numbers), and every
-// particle of the block then walks its 27 neighbouring fine-cell bins.
+// (compacted: the block's own from slot 0 up, the ring's from CAP-1 down, so
+// the force loop runs over the block's particles without idle lanes), binned
+// by fine cell (counting sort of slot numbers), and every particle of the
+// block then walks its 27 neighbouring fine-cell bins.
 // Returns false (nothing kicked) when more than PP_CAP particles would be
 // staged.  Block-uniform control flow; ends with a barrier.
 template <int CAP>
@@ -194,7 +200,7 @@ __device__ bool pp_block(const PPArgs& a, const int C0[3], const int B[3], PPSme
     sm.sstart[t] = a.cstart[c];
   }
   for (int t = threadIdx.x; t < (NF + 2) / 2; t += blockDim.x) bins32[t] = 0u;
-  if (threadIdx.x == 0) sm.nst = 0;
+  if (threadIdx.x == 0) sm.ncore = sm.nring = 0;
   __syncthreads();
   const int total = block_exclusive_scan(sm.pref, NS);
   // stage the particles whose fine cell lies in the block or its fine ring
@@ -202,16 +208,17 @@ __device__ bool pp_block(const PPArgs& a, const int C0[3], const int B[3], PPSme
     const int sl[3] = {sx - 1, row % S1 - 1, row / S1 - 1};
     float x[3];
     int fi[3];
-    bool in = true;
+    bool in = true, core = true;
 #pragma unroll
     for (int d = 0; d < 3; d++) {
       x[d] = __fadd_rn((float)(4 * sl[d]), fine_off(load_code(a.xp, 3 * p + d, g.izipx), g.izipx));
       fi[d] = (int)floorf(x[d]) + 1;  // 0 .. 4B+1 inside the staged region
       in = in && fi[d] >= 0 && fi[d] <= 4 * B[d] + 1;
+      core = core && fi[d] >= 1 && fi[d] <= 4 * B[d];
     }
     if (!in) return;
-    int slot = atomicAdd(&sm.nst, 1);
-    if (slot >= CAP) return;
+    const int slot = core ? atomicAdd(&sm.ncore, 1) : CAP - 1 - atomicAdd(&sm.nring, 1);
+    if (slot < 0 || slot >= CAP) return;
     int f = fi[0] + F0 * (fi[1] + F1 * fi[2]);
     const unsigned sh = 16u * (unsigned)(f & 1);
     int r = (int)((atomicAdd(&bins32[f >> 1], 1u << sh) >> sh) & 0xffffu);
@@ -219,19 +226,18 @@ __device__ bool pp_block(const PPArgs& a, const int C0[3], const int B[3], PPSme
     kinfo[slot] = (unsigned)f | ((unsigned)r << 13);
   });
   __syncthreads();
-  const int nst = sm.nst;
+  const int ncore = sm.ncore, nring = sm.nring, nst = ncore + nring;
   if (nst > CAP) return false;
   block_exclusive_scan_u16(bins, NF);
   if (threadIdx.x == 0) bins[NF] = (unsigned short)nst;
-  for (int t = threadIdx.x; t < nst; t += blockDim.x) {
+  for (int i = threadIdx.x; i < nst; i += blockDim.x) {
+    const int t = i < ncore ? i : CAP - nring + (i - ncore);
     unsigned k = kinfo[t];
     order[bins[k & 8191u] + (int)(k >> 13)] = (unsigned short)t;
   }
   __syncthreads();
-  for (int t = threadIdx.x; t < nst; t += blockDim.x) {
+  for (int t = threadIdx.x; t < ncore; t += blockDim.x) {
     float4 q = pts[t];
-    int fx = (int)floorf(q.x) + 1, fy = (int)floorf(q.y) + 1, fz = (int)floorf(q.z) + 1;
-    if (fx < 1 || fy < 1 || fz < 1 || fx > 4 * B[0] || fy > 4 * B[1] || fz > 4 * B[2]) continue;  // ring
     int f = (int)(kinfo[t] & 8191u);
     long long F[3] = {0, 0, 0};
     // the three bins dx = -1..1 of one (dy, dz) row are consecutive: one range

@@ -30,9 +30,17 @@ def test_oracle_reproduces_golden_fixtures():
     g = _gold()
     new = _mk().make()
     assert set(new) == set(g)
+    import platform
+    same_libm = platform.machine() == "x86_64"  # where the fixtures were made
     for k, v in g.items():
         if k == "pk_xi":
             np.testing.assert_allclose(new[k], v, rtol=1e-12, equal_nan=True)
+        elif k.endswith("_vp") and not same_libm:
+            # velocity codes go through libm's tan/atan, whose last bit differs
+            # between glibc's x86 (FMA) and aarch64 implementations: a code at a
+            # rounding boundary may move by one
+            d = np.abs(np.asarray(new[k]).astype(np.int64) - v.astype(np.int64))
+            assert d.max() <= 1 and (d > 0).mean() < 1e-3, k
         else:
             np.testing.assert_array_equal(np.asarray(new[k]), v, err_msg=k)
 
