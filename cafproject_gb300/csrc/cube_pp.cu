@@ -18,7 +18,7 @@
 // Five levels keep dense regions correct without a host round trip; each
 // level lists what did not fit for the next one:
 //   0. one block per brick of 4^3 coarse cells, 1536 staged particles at most
-//      (several blocks per SM);
+//      (several blocks per SM; a uniform brick stages about 1100);
 //   1. listed bricks again, one 1024-thread block per SM with 8960 of room;
 //   2. the cells of bricks listed by level 1, one at a time, 1536 of room;
 //   3. listed cells with 8960 of room;
