@@ -254,6 +254,69 @@ __global__ void k_ic_particles(PartArgs a, Geo g) {
   }
 }
 
+// Thermal velocities of a massive-neutrino species (the sampling of
+// CUBEnu/initial_conditions_mnu.f90:95-115): a speed q * fd with q drawn from
+// the relativistic Fermi-Dirac distribution q^2/(e^q + 1) by inverse-CDF
+// lookup with linear interpolation, an isotropic direction (cos theta uniform
+// in [-1, 1), phi uniform in [0, 2 pi)), added to each particle's Zel'dovich
+// velocity; vmax recomputed.  Three counter-hash streams per particle.
+constexpr int kFdTab = 4096;
+__global__ void k_ic_thermal(double* vel, int64_t n, const float* __restrict__ qtab, const float* __restrict__ ctab,
+                             float fd, uint32_t s, unsigned int* vmax_bits) {
+  float vm[3] = {0.f, 0.f, 0.f};
+  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < n; l += (int64_t)gridDim.x * blockDim.x) {
+    const float u = hash_uniform(3 * (uint64_t)l, s), uc = hash_uniform(3 * (uint64_t)l + 1, s),
+                up = hash_uniform(3 * (uint64_t)l + 2, s);
+    int lo = 0, hi = kFdTab - 1;  // ctab[lo] <= u < ctab[hi]
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (ctab[mid] <= u) lo = mid;
+      else hi = mid;
+    }
+    const float t = (u - ctab[lo]) / fmaxf(ctab[hi] - ctab[lo], 1e-30f);
+    const float q = qtab[lo] + (qtab[hi] - qtab[lo]) * t;
+    const float sp = q * fd, ct = 2.0f * uc - 1.0f, st = sqrtf(fmaxf(1.0f - ct * ct, 0.f));
+    float sn, cs;
+    sincospif(2.0f * up, &sn, &cs);
+    const double dv[3] = {(double)(sp * st * cs), (double)(sp * st * sn), (double)(sp * ct)};
+    for (int d = 0; d < 3; d++) {
+      const double v = vel[3 * l + d] + dv[d];
+      vel[3 * l + d] = v;
+      vm[d] = fmaxf(vm[d], (float)fabs(v));
+    }
+  }
+  for (int d = 0; d < 3; d++) {
+    float v = vm[d];
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0) atomic_max_pos(&vmax_bits[d], v);
+  }
+}
+
+// the Fermi-Dirac momentum CDF on kFdTab points of q in [0, 30]: the integral
+// of q^2/(e^q+1) by composite Simpson on a 16x finer grid, normalised
+void fd_table(std::vector<float>& q, std::vector<float>& c) {
+  const int n = kFdTab, sub = 16;
+  const double qmax = 30.0, h = qmax / ((double)(n - 1) * sub);
+  auto f = [](double x) { return x * x / (std::exp(x) + 1.0); };
+  std::vector<double> cum(n, 0.0);
+  double acc = 0.0;
+  for (int i = 1; i < n; i++) {
+    const double a = (double)(i - 1) * sub * h;
+    for (int k = 0; k < sub; k++) {
+      const double x0 = a + k * h;
+      acc += h / 6.0 * (f(x0) + 4.0 * f(x0 + h / 2) + f(x0 + h));
+    }
+    cum[i] = acc;
+  }
+  q.resize(n);
+  c.resize(n);
+  for (int i = 0; i < n; i++) {
+    q[i] = (float)((double)i * qmax / (n - 1));
+    c[i] = (float)(cum[i] / acc);
+  }
+  c[n - 1] = 1.0f;
+}
+
 // slot of each Lagrangian particle inside its cell (arbitrary order)
 __global__ void k_ic_place(const int32_t* cid, int64_t n, const int64_t* cstart, int32_t* fill, int32_t* perm) {
   for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < n; l += (int64_t)gridDim.x * blockDim.x) {
@@ -391,8 +454,22 @@ void cube_ic_noise(float* r, int n, int pitch, uint32_t seed, cudaStream_t s) {
 
 double cube_ic_vfactor(double a, double om, double ol) { return vfactor(a, om, ol); }
 
+static int ic_impl(cube_ctx* c, const cube_cosmology* cs, float z_init, uint32_t seed, float m_nu_ev,
+                   uint32_t thermal_seed, float* sigma_vi, float* vmax);
+
 extern "C" int cube_ic_zeldovich(cube_ctx* c, const cube_cosmology* cs, float z_init, uint32_t seed, float* sigma_vi,
                                  float* vmax) {
+  return ic_impl(c, cs, z_init, seed, 0.f, 0u, sigma_vi, vmax);
+}
+
+extern "C" int cube_ic_zeldovich_nu(cube_ctx* c, const cube_cosmology* cs, float z_init, uint32_t seed, float m_nu_ev,
+                                    uint32_t thermal_seed, float* sigma_vi, float* vmax) {
+  if (!(m_nu_ev > 0.f)) return cube_fail(c, CUBE_ERR_ARG, "the neutrino mass must be positive");
+  return ic_impl(c, cs, z_init, seed, m_nu_ev, thermal_seed, sigma_vi, vmax);
+}
+
+static int ic_impl(cube_ctx* c, const cube_cosmology* cs, float z_init, uint32_t seed, float m_nu_ev,
+                   uint32_t thermal_seed, float* sigma_vi, float* vmax) {
   if (!c || !cs) return CUBE_ERR_ARG;
   const cube_params& p = c->p;
   if (cs->np_nc < 1 || p.ncell % cs->np_nc) return cube_fail(c, CUBE_ERR_ARG, "np_nc must divide ncell");
@@ -400,8 +477,20 @@ extern "C" int cube_ic_zeldovich(cube_ctx* c, const cube_cosmology* cs, float z_
   const int64_t n = (int64_t)npd * npd * npd;
   if (n > p.np_max) return cube_fail(c, CUBE_ERR_IMAGE_OVERFLOW, "np_max is below the particle count of the grid");
   if (nf % 2) return cube_fail(c, CUBE_ERR_ARG, "fine mesh must be even");
-  if ((size_t)24 * n > sizeof(float) * (size_t)(nf + 2) * nf * nf)
-    return cube_fail(c, CUBE_ERR_ARG, "velocity scratch exceeds a fine force plane");
+  // FP64 velocities and residuals (24 bytes per particle each) live in two
+  // force planes when they fit (a particle per 8 fine cells and sparser),
+  // else in buffers of their own for the duration of the call
+  const bool fits = (size_t)24 * n <= sizeof(float) * (size_t)(nf + 2) * nf * nf;
+  struct Scratch {
+    void* p = nullptr;
+    ~Scratch() {
+      if (p) cudaFree(p);
+    }
+  } own;
+  if (!fits) {
+    cudaError_t e = cudaMalloc(&own.p, (size_t)48 * n);
+    if (e != cudaSuccess) return cube_fail(c, CUBE_ERR_NOMEM, "initial-condition velocity scratch");
+  }
   CUBE_CUDA(c, cudaSetDevice(c->device));
   cudaStream_t s = c->stream;
   const double a = 1.0 / (1.0 + z_init);
@@ -424,7 +513,7 @@ extern "C" int cube_ic_zeldovich(cube_ctx* c, const cube_cosmology* cs, float z_
   CUBE_FFT(c, cufftExecC2R(c->plan_f_c2r, (cufftComplex*)c->rho_f, c->rho_f));
   // 4. particles on the Lagrangian grid
   int32_t* cid = c->dest;
-  double* vel = reinterpret_cast<double*>(c->force_f[1]);
+  double* vel = fits ? reinterpret_cast<double*>(c->force_f[1]) : static_cast<double*>(own.p);
   CUBE_CUDA(c, cudaMemsetAsync(c->rhoc[k], 0, 4 * (size_t)c->ncells, s));
   CUBE_CUDA(c, cudaMemsetAsync(c->dstats, 0, sizeof(DevStats), s));
   PartArgs pa{c->rho_f, nf, nc, c->nt, p.nnt, cs->np_nc, p.ncell / cs->np_nc, p.ncell, p.izipx,
@@ -432,6 +521,23 @@ extern "C" int cube_ic_zeldovich(cube_ctx* c, const cube_cosmology* cs, float z_
               c->dstats->vmax_bits};
   k_ic_particles<<<cube_grid(n, 256), 256, 0, s>>>(pa, make_geo(c));
   CUBE_CUDA(c, cudaGetLastError());
+  if (m_nu_ev > 0.f) {
+    // thermal speeds: k_B T_nu c / m_nu = 50.2476 km/s / m_nu[eV] / a
+    // (initial_conditions_mnu.f90:33), in simulation units through
+    // vsim2phys = (150/a) box sqrt(omega_m) / nf_global (initial_conditions.f90:175)
+    const double vsim2phys = 150.0 / a * (double)cs->box * std::sqrt((double)cs->omega_m) / (double)nf;
+    const float fd = (float)(50.2476 / (double)m_nu_ev / a / vsim2phys);
+    std::vector<float> qt, ct;
+    fd_table(qt, ct);
+    float* tab = reinterpret_cast<float*>(c->force_f[0]);  // the kernel spectrum is no longer needed
+    CUBE_CUDA(c, cudaMemcpyAsync(tab, qt.data(), 4 * qt.size(), cudaMemcpyHostToDevice, s));
+    CUBE_CUDA(c, cudaMemcpyAsync(tab + kFdTab, ct.data(), 4 * ct.size(), cudaMemcpyHostToDevice, s));
+    CUBE_CUDA(c, cudaMemsetAsync(c->dstats->vmax_bits, 0, 12, s));
+    k_ic_thermal<<<cube_grid(n, 256), 256, 0, s>>>(vel, n, tab, tab + kFdTab, fd, cube_ic_seed(thermal_seed ^ 0x5bd1e995u),
+                                                   c->dstats->vmax_bits);
+    CUBE_CUDA(c, cudaGetLastError());
+    CUBE_CUDA(c, cudaStreamSynchronize(s));  // the host tables go out of scope
+  }
   r = cube_scan_counts(c, c->rhoc[k], c->cstart[k], c->ncells);
   if (r) return r;
   int32_t* fill = reinterpret_cast<int32_t*>(c->rank);
@@ -440,7 +546,7 @@ extern "C" int cube_ic_zeldovich(cube_ctx* c, const cube_cosmology* cs, float z_
   k_ic_cells<<<cube_grid(c->ncells, 128), 128, 0, s>>>(c->cstart[k], c->ncells, c->perm, vel, c->vfield[k]);
   CUBE_CUDA(c, cudaGetLastError());
   // 5. the new order, residuals and sigma
-  double* res = reinterpret_cast<double*>(c->force_f[2]);
+  double* res = fits ? reinterpret_cast<double*>(c->force_f[2]) : static_cast<double*>(own.p) + 3 * n;
   const int nb = cube_grid(n, 256, 4);
   double* part = reinterpret_cast<double*>(c->rho_f);  // phi is no longer needed
   GatherArgs ga{c->perm, cid, c->xp[alt], vel, c->vfield[k], p.izipx, npd, p.ncell / cs->np_nc, nf,

@@ -32,7 +32,7 @@ EXPORTS = ["cube_create", "cube_destroy", "cube_last_error", "cube_upload_state"
            "cube_pm_coarse_forces", "cube_pm_coarse_kick", "cube_get_field", "cube_set_field", "cube_nplocal",
            "cube_synchronize", "cube_timing", "cube_timing_read", "cube_phase_name", "cube_stream",
            "cube_codec_check", "cube_codec_check_static", "cube_arith_check", "cube_pk_nbin",
-           "cube_power_spectrum", "cube_checkpoint_write", "cube_checkpoint_read", "cube_ic_zeldovich", "cube_create_linked", "cube_particle_mesh2", "cube_set_option",
+           "cube_power_spectrum", "cube_checkpoint_write", "cube_checkpoint_read", "cube_ic_zeldovich", "cube_ic_zeldovich_nu", "cube_create_linked", "cube_particle_mesh2", "cube_set_option",
            "cube_dpm_create", "cube_dpm_destroy", "cube_dpm_last_error", "cube_dpm_stream", "cube_dpm_nparticles",
            "cube_dpm_set_schedule", "cube_dpm_noise", "cube_dpm_forward", "cube_dpm_backward", "cube_dpm_density",
            "cube_dpm_density_adjoint", "cube_dpm_tables", "cube_dpm_info",
@@ -147,6 +147,7 @@ def load_library(path=None):
     L.cube_checkpoint_write.argtypes = [P, ctypes.c_char_p, F, ctypes.c_int, P]
     L.cube_checkpoint_read.argtypes = [P, ctypes.c_char_p, F, ctypes.c_int, P]
     L.cube_ic_zeldovich.argtypes = [P, P, F, ctypes.c_uint32, P, P]
+    L.cube_ic_zeldovich_nu.argtypes = [P, P, F, ctypes.c_uint32, F, ctypes.c_uint32, P, P]
     L.cube_create_linked.argtypes = [P, P, P]
     L.cube_particle_mesh2.argtypes = [P, P, F, F, P, P]
     L.cube_set_option.argtypes = [P, ctypes.c_int, I64]
@@ -345,6 +346,19 @@ class CubeGPU:
         vm = (ctypes.c_float * 3)()
         self._check(self.L.cube_ic_zeldovich(self.h, ctypes.byref(cs), float(z_init), int(seed) & 0xFFFFFFFF,
                                              ctypes.byref(sig), vm))
+        return np.float32(sig.value), [float(v) for v in vm]
+
+    def ic_zeldovich_nu(self, z_init, seed, m_nu_ev, thermal_seed, omega_b=0.045):
+        """Neutrino initial conditions: the Zel'dovich state of seed's field
+        plus Fermi-Dirac thermal velocities for m_nu_ev; returns (sigma_vi, vmax[3])."""
+        p = self.p
+        cs = Cosmology(box=p.box, omega_m=p.omega_m, omega_l=p.omega_l, h0=p.h0, s8=p.s8, n_s=p.n_s,
+                       omega_b=omega_b, np_nc=p.np_nc)
+        sig = ctypes.c_float()
+        vm = (ctypes.c_float * 3)()
+        self._check(self.L.cube_ic_zeldovich_nu(self.h, ctypes.byref(cs), float(z_init), int(seed) & 0xFFFFFFFF,
+                                                float(m_nu_ev), int(thermal_seed) & 0xFFFFFFFF, ctypes.byref(sig),
+                                                vm))
         return np.float32(sig.value), [float(v) for v in vm]
 
     def checkpoint_write(self, directory, z, image=1, **header):

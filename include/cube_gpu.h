@@ -179,6 +179,15 @@ int cube_checkpoint_read(cube_ctx* ctx, const char* dir, float z, int image, cub
    dimension.  Uses the fine-mesh buffers as scratch. */
 int cube_ic_zeldovich(cube_ctx* ctx, const cube_cosmology* cosmo, float z_init, uint32_t seed, float* sigma_vi,
                       float* vmax);
+/* The same for a massive-neutrino species (CUBEnu; replaces the thermal part
+   of CUBEnu/initial_conditions_mnu.f90:95-115): each particle's Zel'dovich
+   velocity plus an isotropic thermal velocity of speed q * 50.2476 km/s /
+   m_nu[eV] / a, q drawn from the relativistic Fermi-Dirac distribution
+   q^2/(e^q+1) by inverse CDF, in simulation units (vsim2phys of
+   initial_conditions.f90:175).  seed sets the density field (give the
+   CDM's seed for the same field), thermal_seed the thermal draws. */
+int cube_ic_zeldovich_nu(cube_ctx* ctx, const cube_cosmology* cosmo, float z_init, uint32_t seed, float m_nu_ev,
+                         uint32_t thermal_seed, float* sigma_vi, float* vmax);
 
 /* sigma_vi / sigma_vi_new module variables (variables.f90:36). */
 int cube_set_sigma(cube_ctx* ctx, float sigma_vi, float sigma_vi_new);

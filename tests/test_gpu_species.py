@@ -108,3 +108,82 @@ def test_linked_species_needs_the_owner_geometry():
             C.CubeGPU(P.CubeParams(nc=24, nnt=2, pp_on=True), owner=a)
     finally:
         a.close()
+
+
+def _decoded(g, sigma):
+    """v = tan(pi*code/(nvbin-1)) / (sqrt(pi/2)/(sigma*2.5)) + vfield(cell), FP64 on the host."""
+    s = g.download()
+    nv = 2 ** (8 * g.p.izipv)
+    cf = np.sqrt(np.float32(np.pi / 2)) / (np.float64(sigma) * 2.5)
+    rel = np.tan(np.pi * s["vp"].astype(np.float64) / (nv - 1)) / cf
+    cell = np.repeat(np.arange(g.p.nc ** 3), s["rhoc"])
+    return rel + s["vfield"].reshape(-1, 3)[cell].astype(np.float64), s["pid"]
+
+
+def test_neutrino_thermal_velocities_follow_fermi_dirac():
+    # one particle per fine cell (np_nc = 4), z = 10, m_nu = 0.05 eV; the same
+    # density field with and without the thermal draws
+    p = P.CubeParams(nc=32, nnt=1, pp_on=False, box=200.0, np_nc=4, mass_p=1.0)
+    z, m = 10.0, 0.05
+    gz, gn = C.CubeGPU(p), C.CubeGPU(p)
+    try:
+        sz, _ = gz.ic_zeldovich(z, 5)
+        sn, vm = gn.ic_zeldovich_nu(z, 5, m, 9)
+        vz, pz = _decoded(gz, sz)
+        vn, pn = _decoded(gn, sn)
+    finally:
+        gz.close()
+        gn.close()
+    assert np.array_equal(pz, pn)  # thermal velocities move no particle
+    a = 1.0 / (1.0 + z)
+    vsim2phys = 150.0 / a * p.box * np.sqrt(p.omega_m) / p.nf
+    fd = 50.2476 / m / a / vsim2phys
+    dv = (vn - vz) / fd
+    q = np.sqrt((dv ** 2).sum(1))
+    # the relativistic Fermi-Dirac momentum distribution q^2/(e^q+1)
+    x = np.linspace(0, 30, 300001)
+    pdf = x * x / (np.exp(x) + 1)
+    cdf = np.cumsum(pdf)
+    cdf /= cdf[-1]
+    qs = np.sort(q)
+    ks = np.abs(np.interp(qs, x, cdf) - np.arange(1, len(qs) + 1) / len(qs)).max()
+    mean_q = (x * pdf).sum() / pdf.sum()
+    print("neutrino thermal speeds: KS %.2e, <q> %.4f (FD %.4f), sigma_vi %.3f" % (ks, q.mean(), mean_q, sn))
+    assert ks < 3e-3
+    assert abs(q.mean() / mean_q - 1) < 3e-3
+    # isotropic: no mean direction, equal variance per axis
+    assert np.abs(dv.mean(0)).max() < 5e-3 * mean_q
+    var = (dv ** 2).mean(0)
+    assert np.abs(var / var.mean() - 1).max() < 5e-3
+    assert max(vm) > 3 * fd  # vmax includes the thermal tail
+
+
+def test_two_species_step_with_thermal_neutrinos():
+    # CDM (np_nc = 2) and thermal neutrinos (np_nc = 4) sharing the meshes;
+    # neutrinos outrun one coarse cell per step, so their re-sort takes the
+    # general walker
+    from cafproject_gb300.cosmology import TimeState
+    pc = P.CubeParams(nc=32, nnt=1, pp_on=True, box=200.0, np_nc=2, mass_p=7.98)
+    pn = P.CubeParams(nc=32, nnt=1, pp_on=False, box=200.0, np_nc=4, mass_p=0.0025, np_max=int(1.25 * 128 ** 3))
+    g = C.CubeGPU(pc)
+    nu = C.CubeGPU(pn, owner=g)
+    try:
+        sc, vc = g.ic_zeldovich(10.0, 5)
+        sn, vn = nu.ic_zeldovich_nu(10.0, 5, 0.05, 9)
+        ts = TimeState(a=np.float32(1 / 11.0))
+        ts.vz_max = np.float32(max(vc[2], vn[2]))
+        ts.dt_vmax = np.float32(np.float32(18.0) / np.float32(max(max(vc), max(vn))))
+        for _ in range(2):
+            dt, a_mid = ts.timestep()
+            uc = g.update_x(ts.dt_old, dt, ts.vz_max)
+            un = nu.update_x(ts.dt_old, dt, ts.vz_max)
+            pp = g.ext_pp_force(a_mid, dt)
+            st, stn = g.particle_mesh2(nu, a_mid, dt)
+            ts.constrain({"f2_max_fine": st["f2_max_fine"], "f2_max_coarse": st["f2_max_coarse"],
+                          "vmax": [max(st["vmax"][d], stn["vmax"][d]) for d in range(3)]}, pp, pc.ncell)
+            assert uc["nplocal"] == 64 ** 3 and un["nplocal"] == 128 ** 3
+        assert un["rank_walked"] == 1 and un["max_disp"] > 1
+        assert max(stn["vmax"]) > 10 * max(st["vmax"])
+    finally:
+        nu.close()
+        g.close()
