@@ -410,7 +410,7 @@ def run_batched(args, lrank, nsteps=50):
 def gpu_launches(p, steps):
     """Launches of this library's kernels per step (cuFFT kernels not counted)."""
     upd = 1 + 2 + 3 + 2 + 1 + 1  # dest, counting ranks (2), scan (3), place + vfield, scatter, sigma
-    pp = 3 if p.pp_on else 0     # staged bricks, staged cells, dense cells
+    pp = 6 if p.pp_on else 0     # five pair levels (bricks, large bricks, cells, large cells, global), kick
     fine = 4                     # deposit, green, maxima + kick factors, kick
     coarse = 4
     codec = 2                    # decode table and encode boundaries for the new sigma

@@ -192,6 +192,7 @@ static int create_impl(const cube_params* p, const float* fine_table, const floa
     for (int d = 0; d < 3; d++) ALLOC(c->force_c[d], 4 * cpad);
     ALLOC(c->kern_c, 4 * 3 * nch * p->nc * (int64_t)p->nc);
   }
+  if (p->pp_on) ALLOC(c->fpp, 12 * (size_t)np);
   {
     int nb = (p->nc + 3) / 4;
     c->pp_brick_cap = nb * nb * nb;

@@ -144,7 +144,7 @@ struct cube_ctx {
   float* force_c[3] = {nullptr, nullptr, nullptr};
   float* kern_c = nullptr;      // scaled by 1/nc^3 (exact: power of two)
   // PP
-  float* fpp = nullptr;         // optional per-particle PP force (3*np), debug only
+  float* fpp = nullptr;         // per-particle PP force (3*np_max): pair kernels -> kick pass
   int* pp_list[4] = {nullptr, nullptr, nullptr, nullptr};  // work of PP levels 1-4 (bricks, bricks, cells, cells)
   int* pp_nlist = nullptr;          // their lengths
   int* pp_nlist_host = nullptr;     // pinned copy of the last call's lengths

@@ -23,9 +23,11 @@
 //   2. the cells of bricks listed by level 1, one at a time, 1536 of room;
 //   3. listed cells with 8960 of room;
 //   4. cells still too dense, from global memory, one block per cell.
-// The kick adds F*a_mid*dt/(6 pi) in FP64 as one product with the precomputed
-// factor -- the FP32 pair sum already sets this kick's tolerance against the
-// reference's FP64 sum -- and the velocity code is the exact code of
+// The kick (a pass of its own over the particles in storage order, from the
+// per-particle sums the pair kernels leave) adds F*a_mid*dt/(6 pi) in FP64 as
+// one product with the precomputed factor -- the FP32 pair sum already sets
+// this kick's tolerance against the reference's FP64 sum -- and the velocity
+// code is the exact code of
 // update_particle.f90:117 (certified FP32 fast path, FP64 when ambiguous).
 #include <cmath>
 
@@ -66,7 +68,7 @@ struct PPArgs {
   double kick;   // a_mid*dt/6/pi
   float kick_f;  // the same rounded to float (fast path)
   int exact_only;
-  float* fpp;    // optional per-particle force output
+  float* fpp;    // per-particle summed pair force (3 per particle), pair kernels -> kick pass
   int nb;        // bricks per dimension
   int* list[4];    // work of levels 1..4: bricks, bricks, cells, cells
   int* nlist;      // their lengths
@@ -124,28 +126,39 @@ __device__ __noinline__ long long pp_kick_exact(CodecView cv, int code, float F,
   return codec_encode(cv, v);
 }
 
-// kick + exact velocity code of one particle; returns |F|^2
-__device__ __forceinline__ float pp_kick(const PPArgs& a, int64_t p, const long long* acc) {
-  const Geo& g = a.g;
+// the summed pair force of particle p, kept for the kick pass; returns |F|^2
+__device__ __forceinline__ float pp_store_force(const PPArgs& a, int64_t p, const long long* acc) {
   float F[3];
-  for (int d = 0; d < 3; d++) F[d] = from_fix(acc[d]);
   for (int d = 0; d < 3; d++) {
-    int code = load_code(a.vp, 3 * p + d, g.izipv);
-    // vreal=vreal+f_tot*a_mid*dt/6/pi (ext_pp_force.f90:116), then the code
-    float dh = codec_decode_ff(a.cv, code).x;
-    float kf = __fmul_rn(F[d], pp_kick_f(a));
-    float vf = __fadd_rn(dh, kf);
-    float E = 1.25f * (fabsf(kf) * 1.3e-7f + (2.f * fabsf(dh) + fabsf(vf)) * 6.0e-8f);
-    long long n = 0, out;
-    if (!a.exact_only && certify_abs(f2d_bits(vf) & 0x7fffffffffffffffLL, E, a.cv, &n)) {
-      out = vf < 0.f ? -n : n;
-    } else {
-      out = pp_kick_exact(a.cv, code, F[d], pp_kick_d(a));
-    }
-    store_code(a.vp, 3 * p + d, g.izipv, out);
-    if (a.fpp) a.fpp[3 * p + d] = F[d];
+    F[d] = from_fix(acc[d]);
+    a.fpp[3 * p + d] = F[d];
   }
   return F[0] * F[0] + F[1] * F[1] + F[2] * F[2];
+}
+
+// kick + exact velocity code of every particle, in storage order (coalesced
+// code and force accesses; the pair kernels visit particles in staging order)
+__global__ void __launch_bounds__(256) k_pp_kick(PPArgs a) {
+  const Geo& g = a.g;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.np; p += (int64_t)gridDim.x * blockDim.x) {
+    float F[3];
+    for (int d = 0; d < 3; d++) F[d] = a.fpp[3 * p + d];
+    for (int d = 0; d < 3; d++) {
+      int code = load_code(a.vp, 3 * p + d, g.izipv);
+      // vreal=vreal+f_tot*a_mid*dt/6/pi (ext_pp_force.f90:116), then the code
+      float dh = codec_decode_ff(a.cv, code).x;
+      float kf = __fmul_rn(F[d], pp_kick_f(a));
+      float vf = __fadd_rn(dh, kf);
+      float E = 1.25f * (fabsf(kf) * 1.3e-7f + (2.f * fabsf(dh) + fabsf(vf)) * 6.0e-8f);
+      long long n = 0, out;
+      if (!a.exact_only && certify_abs(f2d_bits(vf) & 0x7fffffffffffffffLL, E, a.cv, &n)) {
+        out = vf < 0.f ? -n : n;
+      } else {
+        out = pp_kick_exact(a.cv, code, F[d], pp_kick_d(a));
+      }
+      store_code(a.vp, 3 * p + d, g.izipv, out);
+    }
+  }
 }
 
 __device__ __forceinline__ void pp_reduce(const PPArgs& a, unsigned long long npairs, unsigned long long nwork,
@@ -252,7 +265,7 @@ __device__ bool pp_block(const PPArgs& a, const int C0[3], const int B[3], PPSme
         }
       }
     acc.nwork++;
-    acc.f2max = fmaxf(acc.f2max, pp_kick(a, (int64_t)__float_as_int(q.w), F));
+    acc.f2max = fmaxf(acc.f2max, pp_store_force(a, (int64_t)__float_as_int(q.w), F));
   }
   __syncthreads();
   return true;
@@ -342,7 +355,7 @@ __global__ void __launch_bounds__(PP_THREADS) k_pp_dense(PPArgs a) {
             }
           }
       acc.nwork++;
-      acc.f2max = fmaxf(acc.f2max, pp_kick(a, p, f));
+      acc.f2max = fmaxf(acc.f2max, pp_store_force(a, p, f));
     }
   }
   pp_reduce(a, acc.npairs, acc.nwork, acc.f2max);
@@ -357,6 +370,7 @@ __global__ void k_pp_list_all(int* list, int n, int* count) {
 }  // namespace
 
 int cube_pp_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st) {
+  if (!c->fpp) return cube_fail(c, CUBE_ERR_ARG, "PP is off for this context (pp_on = 0)");
   PPArgs a{};
   int r;
   if (c->graph_mode) {
@@ -410,6 +424,7 @@ int cube_pp_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st) {
   if (start <= 2) k2<<<persist, PP_THREADS, PP_SMEM, c->stream>>>(a);
   if (start <= 3) k3<<<one_per_sm, PP_THREADS1, PP_SMEM1, c->stream>>>(a);
   k_pp_dense<<<persist, PP_THREADS, 0, c->stream>>>(a);
+  k_pp_kick<<<cube_grid(c->np, 256), 256, 0, c->stream>>>(a);
   CUBE_CUDA(c, cudaGetLastError());
   cube_phase_end(c, PH_PP);
   if (c->graph_mode) {
