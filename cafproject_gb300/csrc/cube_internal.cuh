@@ -379,20 +379,24 @@ __device__ __forceinline__ long long f2d_bits(float f) {
 // non-negative double, E >= 0) is n: returns true and n when the whole
 // interval lies in one code bin.  Distances are counted in ulps of ab's binade;
 // an edge in another binade is at least as far as that binade's end.
-__device__ __forceinline__ bool certify_abs(long long ab, float E, const CodecView& k, long long* n_out) {
+// the three parts of certify_abs: the FP32 estimate of the bin, the probe of
+// its two edges, and the check on the edges the probe (or a walk) found
+__device__ __forceinline__ long long certify_estimate(long long ab, const CodecView& k) {
   float af = approx_float_pos(ab);
   float u0 = k.amp * atanf(codec_cf(k) * af);
   int m = (int)(u0 + 0.5f);
-  long long n = m < 0 ? 0 : (m > k.nmax ? k.nmax : m);
-  // the FP32 estimate is within a few hundredths of a code: probe its bin with
-  // two independent loads, walk only when it fell on the wrong side of an edge
-  long long lb = n > 0 ? __ldg(k.bnd + n) : 0;
-  long long ub = n < k.nmax ? __ldg(k.bnd + n + 1) : 0x7fffffffffffffffLL;
+  return m < 0 ? 0 : (m > k.nmax ? k.nmax : m);
+}
+__device__ __forceinline__ void certify_probe(long long n, const CodecView& k, long long& lb, long long& ub) {
+  lb = n > 0 ? __ldg(k.bnd + n) : 0;
+  ub = n < k.nmax ? __ldg(k.bnd + n + 1) : 0x7fffffffffffffffLL;
+}
+__device__ __forceinline__ bool certify_finish(long long ab, float E, const CodecView& k, long long n, long long lb,
+                                               long long ub, long long* n_out) {
   if (ab < lb || ab >= ub) {
     while (n < k.nmax && __ldg(k.bnd + n + 1) <= ab) n++;
     while (n > 0 && __ldg(k.bnd + n) > ab) n--;
-    lb = n > 0 ? __ldg(k.bnd + n) : 0;
-    ub = n < k.nmax ? __ldg(k.bnd + n + 1) : 0x7fffffffffffffffLL;
+    certify_probe(n, k, lb, ub);
   }
   *n_out = n;
   int e = (int)((ab >> 52) & 0x7ff);
@@ -411,6 +415,26 @@ __device__ __forceinline__ bool certify_abs(long long ab, float E, const CodecVi
     if (ux - ab <= kk) return false;
   }
   return true;
+}
+__device__ __forceinline__ bool certify_abs(long long ab, float E, const CodecView& k, long long* n_out) {
+  // the FP32 estimate is within a few hundredths of a code: probe its bin with
+  // two independent loads, walk only when it fell on the wrong side of an edge
+  const long long n = certify_estimate(ab, k);
+  long long lb, ub;
+  certify_probe(n, k, lb, ub);
+  return certify_finish(ab, E, k, n, lb, ub, n_out);
+}
+// certify_abs of three values with the table probes of all three issued
+// together, so no value's loads wait for another's
+__device__ __forceinline__ void certify_abs3(const long long ab[3], const float E[3], const CodecView& k,
+                                             long long n_out[3], bool ok[3]) {
+  long long n[3], lb[3], ub[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) n[d] = certify_estimate(ab[d], k);
+#pragma unroll
+  for (int d = 0; d < 3; d++) certify_probe(n[d], k, lb[d], ub[d]);
+#pragma unroll
+  for (int d = 0; d < 3; d++) ok[d] = certify_finish(ab[d], E[d], k, n[d], lb[d], ub[d], &n_out[d]);
 }
 
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {

@@ -141,20 +141,32 @@ __device__ __forceinline__ float pp_store_force(const PPArgs& a, int64_t p, cons
 __global__ void __launch_bounds__(256) k_pp_kick(PPArgs a) {
   const Geo& g = a.g;
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.np; p += (int64_t)gridDim.x * blockDim.x) {
-    float F[3];
-    for (int d = 0; d < 3; d++) F[d] = a.fpp[3 * p + d];
+    float F[3], vf[3], E[3];
+    int code[3];
+    long long ab[3], n[3];
+    bool ok[3];
+#pragma unroll
     for (int d = 0; d < 3; d++) {
-      int code = load_code(a.vp, 3 * p + d, g.izipv);
+      F[d] = a.fpp[3 * p + d];
+      code[d] = load_code(a.vp, 3 * p + d, g.izipv);
+    }
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
       // vreal=vreal+f_tot*a_mid*dt/6/pi (ext_pp_force.f90:116), then the code
-      float dh = codec_decode_ff(a.cv, code).x;
+      float dh = codec_decode_ff(a.cv, code[d]).x;
       float kf = __fmul_rn(F[d], pp_kick_f(a));
-      float vf = __fadd_rn(dh, kf);
-      float E = 1.25f * (fabsf(kf) * 1.3e-7f + (2.f * fabsf(dh) + fabsf(vf)) * 6.0e-8f);
-      long long n = 0, out;
-      if (!a.exact_only && certify_abs(f2d_bits(vf) & 0x7fffffffffffffffLL, E, a.cv, &n)) {
-        out = vf < 0.f ? -n : n;
+      vf[d] = __fadd_rn(dh, kf);
+      E[d] = 1.25f * (fabsf(kf) * 1.3e-7f + (2.f * fabsf(dh) + fabsf(vf[d])) * 6.0e-8f);
+      ab[d] = f2d_bits(vf[d]) & 0x7fffffffffffffffLL;
+    }
+    certify_abs3(ab, E, a.cv, n, ok);
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      long long out;
+      if (!a.exact_only && ok[d]) {
+        out = vf[d] < 0.f ? -n[d] : n[d];
       } else {
-        out = pp_kick_exact(a.cv, code, F[d], pp_kick_d(a));
+        out = pp_kick_exact(a.cv, code[d], F[d], pp_kick_d(a));
       }
       store_code(a.vp, 3 * p + d, g.izipv, out);
     }
