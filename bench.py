@@ -8,7 +8,9 @@ z=49 from the Eisenstein-Hu no-wiggle spectrum (synthetic, seeded).
 
 One step is the reference's loop body (CUBEnu/work/main/main.f90:102-118):
 timestep (host) -> update_x -> buffer_grid -> buffer_x -> ext_pp_force ->
-particle_mesh -> buffer_v, every call through the C ABI of libcube_gb300.so.
+particle_mesh -> buffer_v, every call through the C ABI of libcube_gb300.so
+(ext_pp_force and particle_mesh as the one call cube_pp_particle_mesh, which
+runs PP beside the PM force chain with the same results).
 
 ``value``: N*K / device time of K steps (CUDA events on the library's
 stream), state resident in HBM.  ``e2e``: the same metric when every step also
@@ -216,13 +218,18 @@ def run_gb300(args, ws, rank, lrank):
     ts.dt_vmax = np.float32(np.float32(18.0) / np.float32(max(vm)))
     stream = torch.cuda.ExternalStream(g.stream())
 
-    def step():
+    def step(fused=True):
         dt, a_mid = ts.timestep()
         g.update_x(ts.dt_old, dt, ts.vz_max)
         g.buffer_grid()
         g.buffer_x()
-        pps = g.ext_pp_force(a_mid, dt) if p.pp_on else None
-        pms = g.particle_mesh(a_mid, dt)
+        if p.pp_on and fused:  # ext_pp_force + particle_mesh, PP beside the PM force chain
+            pps, pms = g.pp_particle_mesh(a_mid, dt)
+        elif p.pp_on:
+            pps = g.ext_pp_force(a_mid, dt)
+            pms = g.particle_mesh(a_mid, dt)
+        else:
+            pps, pms = None, g.particle_mesh(a_mid, dt)
         g.buffer_v()
         ts.constrain(pms, pps, p.ncell)
         return pms
@@ -250,11 +257,12 @@ def run_gb300(args, ws, rank, lrank):
     ntot = allreduce_sum(float(n0), ws, dev)
     value = replica_throughput(n0 * args.steps, ms / 1000.0, ws, dev)
 
-    # per-phase device time (timers on, a separate pass so the headline is unperturbed)
+    # per-phase device time (timers on, a separate pass so the headline is
+    # unperturbed; PP and PM as separate calls so no phase overlaps another)
     g.timing(True)
     kph = max(1, min(args.steps, 3))
     for _ in range(kph):
-        step()
+        step(fused=False)
     tphase = g.timing_read()
     g.timing(False)
     ab = algorithmic_bytes(p, n0)

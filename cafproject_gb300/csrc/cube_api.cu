@@ -62,6 +62,11 @@ static void release(cube_ctx* c) {
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (c->hstats) cudaFreeHost(c->hstats);
+  if (c->hstats_pp) cudaFreeHost(c->hstats_pp);
+  if (c->dstats_pp) cudaFree(c->dstats_pp);
+  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+  if (c->ev_pp) cudaEventDestroy(c->ev_pp);
+  if (c->stream_pp) cudaStreamDestroy(c->stream_pp);
   if (c->pp_nlist_host) cudaFreeHost(c->pp_nlist_host);
   if (c->plan_f_r2c) cufftDestroy(c->plan_f_r2c);
   if (c->plan_f_c2r) cufftDestroy(c->plan_f_c2r);
@@ -192,7 +197,14 @@ static int create_impl(const cube_params* p, const float* fine_table, const floa
     for (int d = 0; d < 3; d++) ALLOC(c->force_c[d], 4 * cpad);
     ALLOC(c->kern_c, 4 * 3 * nch * p->nc * (int64_t)p->nc);
   }
-  if (p->pp_on) ALLOC(c->fpp, 12 * (size_t)np);
+  if (p->pp_on) {
+    ALLOC(c->fpp, 12 * (size_t)np);
+    ALLOC(c->dstats_pp, sizeof(DevStats));
+    CUBE_CUDA(c, cudaMallocHost((void**)&c->hstats_pp, sizeof(DevStats)));
+    CUBE_CUDA(c, cudaStreamCreateWithFlags(&c->stream_pp, cudaStreamNonBlocking));
+    CUBE_CUDA(c, cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+    CUBE_CUDA(c, cudaEventCreateWithFlags(&c->ev_pp, cudaEventDisableTiming));
+  }
   {
     int nb = (p->nc + 3) / 4;
     c->pp_brick_cap = nb * nb * nb;
@@ -340,6 +352,51 @@ extern "C" int cube_particle_mesh(cube_ctx* c, float a_mid, float dt, cube_stats
   c->sigma_vi = c->sigma_vi_new;  // pm.f90:193
   if ((r = cube_coarse_forces_impl(c, st, pre))) return r;
   return cube_coarse_kick_impl(c, a_mid, dt, st, true);
+}
+
+// ext_pp_force followed by particle_mesh (main.f90:113-116) with PP on a
+// second stream beside the PM force chain: the fine and coarse densities,
+// transforms and maxima need only positions, so they run while PP kicks;
+// the fine kick waits for PP's kick, as in the reference's order.  Same
+// results, bit for bit, as the two calls made one after the other.
+extern "C" int cube_pp_particle_mesh(cube_ctx* c, float a_mid, float dt, cube_stats* st_pp, cube_stats* st_pm) {
+  int r = check_ready(c);
+  if (r) return r;
+  if (!c->stream_pp) return cube_fail(c, CUBE_ERR_ARG, "PP is off for this context (pp_on = 0)");
+  const float pre[2] = {a_mid, dt};
+  CUBE_CUDA(c, cudaEventRecord(c->ev_fork, c->stream));
+  CUBE_CUDA(c, cudaStreamWaitEvent(c->stream_pp, c->ev_fork, 0));
+  {  // PP's launches go to its stream with its own stats
+    cudaStream_t s0 = c->stream;
+    DevStats *d0 = c->dstats, *h0 = c->hstats;
+    c->stream = c->stream_pp;
+    c->dstats = c->dstats_pp;
+    c->hstats = c->hstats_pp;
+    r = cube_pp_launch(c, a_mid, dt);
+    if (!r) r = cudaEventRecord(c->ev_pp, c->stream_pp) == cudaSuccess ? CUBE_OK : CUBE_ERR_CUDA;
+    c->stream = s0;
+    c->dstats = d0;
+    c->hstats = h0;
+    if (r) return r;
+  }
+  if ((r = cube_fine_forces_impl(c, st_pm, pre))) return r;
+  if ((r = cube_coarse_forces_impl(c, st_pm, pre))) return r;
+  CUBE_CUDA(c, cudaStreamWaitEvent(c->stream, c->ev_pp, 0));
+  if ((r = cube_fine_kick_impl(c, a_mid, dt, true))) return r;
+  c->sigma_vi = c->sigma_vi_new;  // pm.f90:193
+  if ((r = cube_coarse_kick_impl(c, a_mid, dt, st_pm, true))) return r;
+  {  // PP's stats (its stream is done: the kicks waited for it)
+    cudaStream_t s0 = c->stream;
+    DevStats *d0 = c->dstats, *h0 = c->hstats;
+    c->stream = c->stream_pp;
+    c->dstats = c->dstats_pp;
+    c->hstats = c->hstats_pp;
+    r = cube_pp_finish(c, st_pp);
+    c->stream = s0;
+    c->dstats = d0;
+    c->hstats = h0;
+  }
+  return r;
 }
 
 // particle_mesh with the linked species (pm.f90:52-107, 162-189, 237-253,

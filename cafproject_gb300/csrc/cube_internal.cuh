@@ -149,6 +149,12 @@ struct cube_ctx {
   int* pp_nlist = nullptr;          // their lengths
   int* pp_nlist_host = nullptr;     // pinned copy of the last call's lengths
   int pp_brick_cap = 0;             // ceil(nc/4)^3
+  // PP beside the PM force chain (cube_pp_particle_mesh): its own stream,
+  // stats and pinned copy, and the fork / join events
+  cudaStream_t stream_pp = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_pp = nullptr;
+  DevStats* dstats_pp = nullptr;
+  DevStats* hstats_pp = nullptr;  // pinned
   // per-phase timers (null when disabled)
   struct CubeTimers* timers = nullptr;
   // stats
@@ -622,6 +628,8 @@ int cube_kernels_init(cube_ctx* c, const float* fine_table, const float* coarse_
 int cube_scan_counts(cube_ctx* c, const int32_t* counts, int64_t* starts, int64_t n);
 int cube_update_x_impl(cube_ctx* c, float dt_old, float dt, float vz_max, cube_stats* st);
 int cube_pp_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st);
+int cube_pp_launch(cube_ctx* c, float a_mid, float dt);
+int cube_pp_finish(cube_ctx* c, cube_stats* st);
 // density deposits; accumulate: add to the mesh (the linked species) instead of writing it
 int cube_fine_density_impl(cube_ctx* c, cube_stats* st, bool accumulate = false);
 int cube_coarse_density_impl(cube_ctx* c, cube_stats* st, bool accumulate = false);

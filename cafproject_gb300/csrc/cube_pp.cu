@@ -381,7 +381,8 @@ __global__ void k_pp_list_all(int* list, int n, int* count) {
 
 }  // namespace
 
-int cube_pp_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st) {
+// every PP launch on c->stream (stats in c->dstats); the host reads nothing
+int cube_pp_launch(cube_ctx* c, float a_mid, float dt) {
   if (!c->fpp) return cube_fail(c, CUBE_ERR_ARG, "PP is off for this context (pp_on = 0)");
   PPArgs a{};
   int r;
@@ -444,7 +445,13 @@ int cube_pp_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st) {
     return CUBE_OK;
   }
   CUBE_CUDA(c, cudaMemcpyAsync(c->pp_nlist_host, c->pp_nlist, 4 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-  r = cube_stats_fetch(c);
+  return CUBE_OK;
+}
+
+// the stats of the launches above, once they are done (itest1 check of
+// ext_pp_force.f90:141)
+int cube_pp_finish(cube_ctx* c, cube_stats* st) {
+  int r = cube_stats_fetch(c);
   if (r) return r;
   if ((int64_t)c->hstats->itest1 != c->np)
     return cube_fail(c, CUBE_ERR_COUNT_MISMATCH, "PP updated a different number of particles than nplocal");
@@ -455,4 +462,10 @@ int cube_pp_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st) {
     st->pp_dense_bricks = c->pp_nlist_host[0];
   }
   return CUBE_OK;
+}
+
+int cube_pp_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st) {
+  int r = cube_pp_launch(c, a_mid, dt);
+  if (r || c->graph_mode) return r;
+  return cube_pp_finish(c, st);
 }

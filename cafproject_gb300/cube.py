@@ -27,7 +27,7 @@ STATUS = {0: "CUBE_OK", 1: "CUBE_ERR_ARG", 2: "CUBE_ERR_CUDA", 3: "CUBE_ERR_TILE
 # every symbol include/cube_gpu.h declares
 EXPORTS = ["cube_create", "cube_destroy", "cube_last_error", "cube_upload_state", "cube_download_state",
            "cube_set_sigma", "cube_get_sigma", "cube_update_x", "cube_buffer_grid", "cube_buffer_x",
-           "cube_buffer_v", "cube_pp_force", "cube_particle_mesh", "cube_pm_fine_density", "cube_pm_coarse_density",
+           "cube_buffer_v", "cube_pp_force", "cube_particle_mesh", "cube_pp_particle_mesh", "cube_pm_fine_density", "cube_pm_coarse_density",
            "cube_pm_fine_forces", "cube_pm_fine_kick",
            "cube_pm_coarse_forces", "cube_pm_coarse_kick", "cube_get_field", "cube_set_field", "cube_nplocal",
            "cube_synchronize", "cube_timing", "cube_timing_read", "cube_phase_name", "cube_stream",
@@ -123,6 +123,7 @@ def load_library(path=None):
         getattr(L, n).argtypes = [P]
     L.cube_pp_force.argtypes = [P, F, F, P]
     L.cube_particle_mesh.argtypes = [P, F, F, P]
+    L.cube_pp_particle_mesh.argtypes = [P, F, F, P, P]
     L.cube_pm_fine_density.argtypes = [P, P]
     L.cube_pm_coarse_density.argtypes = [P, P]
     L.cube_pm_fine_forces.argtypes = [P, P]
@@ -282,6 +283,13 @@ class CubeGPU:
         self._check(self.L.cube_particle_mesh2(self.h, nu.h, float(a_mid), float(dt), ctypes.byref(st),
                                                ctypes.byref(sn)))
         return st.as_dict(), sn.as_dict()
+
+    def pp_particle_mesh(self, a_mid, dt):
+        """ext_pp_force then particle_mesh in one call, PP beside the PM
+        force chain on a second stream; returns (pp stats, pm stats)."""
+        sp, sm = CubeStats(), CubeStats()
+        self._check(self.L.cube_pp_particle_mesh(self.h, float(a_mid), float(dt), ctypes.byref(sp), ctypes.byref(sm)))
+        return sp.as_dict(), sm.as_dict()
 
     def particle_mesh(self, a_mid, dt):
         st = CubeStats()

@@ -215,6 +215,13 @@ int cube_pp_force(cube_ctx* ctx, float a_mid, float dt, cube_stats* st);
    the force maxima and vmax. */
 int cube_particle_mesh(cube_ctx* ctx, float a_mid, float dt, cube_stats* st);
 
+/* cube_pp_force followed by cube_particle_mesh (main.f90:113-116) in one
+   call: PP runs on a second stream beside the PM densities, transforms and
+   maxima (they read positions only), and the fine kick waits for PP's kick.
+   Bit for bit the results of the two calls in sequence; st_pp receives PP's
+   stats, st_pm particle_mesh's. */
+int cube_pp_particle_mesh(cube_ctx* ctx, float a_mid, float dt, cube_stats* st_pp, cube_stats* st_pm);
+
 /* particle_mesh of two species (pm.f90:52-107, 162-194, 237-253, 358-377):
    the linked species nu deposits into the same meshes with its own mass, both
    are kicked by the same forces with their own velocity codes, sigma_vi and
