@@ -101,9 +101,15 @@ int cube_scan_counts(cube_ctx* c, const int32_t* counts, int64_t* starts, int64_
 }
 
 // ---------------------------------------------------------- cell index
-// pcell[p] = cell of particle p, from the spine: one thread per cell.
-__global__ void k_fill_pcell(const int64_t* __restrict__ cstart, int64_t ncells, int32_t* __restrict__ pcell) {
+// pcell[p] = cell of particle p, from the spine: one thread per cell; a
+// negative count is flagged (bit 16 of *flags) and writes nothing.
+__global__ void k_fill_pcell(const int32_t* __restrict__ rhoc, const int64_t* __restrict__ cstart, int64_t ncells,
+                             int32_t* __restrict__ pcell, int* flags) {
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncells; c += (int64_t)gridDim.x * blockDim.x) {
+    if (rhoc && rhoc[c] < 0) {
+      atomicOr(flags, 1 << 16);
+      continue;
+    }
     for (int64_t p = cstart[c]; p < cstart[c + 1]; p++) pcell[p] = (int32_t)c;
   }
 }
@@ -112,13 +118,9 @@ int cube_state_in(cube_ctx* c, int64_t np, const void* xp, const void* vp, const
                   const float* vfield) {
   int k = c->cur;
   const cube_params& p = c->p;
-  // check the counts before touching the device state
-  int64_t tot = 0;
-  for (int64_t i = 0; i < c->ncells; i++) {
-    if (rhoc[i] < 0) return cube_fail(c, CUBE_ERR_ARG, "negative rhoc");
-    tot += rhoc[i];
-  }
-  if (tot != np) return cube_fail(c, CUBE_ERR_COUNT_MISMATCH, "sum(rhoc) != nplocal");
+  // the counts are checked on the device, after the copies (a failed check
+  // leaves the context without a state)
+  c->have_state = false;
   CUBE_CUDA(c, cudaMemcpyAsync(c->xp[k], xp, (size_t)3 * np * p.izipx, cudaMemcpyHostToDevice, c->stream));
   CUBE_CUDA(c, cudaMemcpyAsync(c->vp[k], vp, (size_t)3 * np * p.izipv, cudaMemcpyHostToDevice, c->stream));
   if (pid)
@@ -129,9 +131,17 @@ int cube_state_in(cube_ctx* c, int64_t np, const void* xp, const void* vp, const
   CUBE_CUDA(c, cudaMemcpyAsync(c->vfield[k], vfield, (size_t)12 * c->ncells, cudaMemcpyHostToDevice, c->stream));
   int r = cube_scan_counts(c, c->rhoc[k], c->cstart[k], c->ncells);
   if (r) return r;
-  k_fill_pcell<<<cube_grid(c->ncells, 256), 256, 0, c->stream>>>(c->cstart[k], c->ncells, c->pcell[k]);
+  CUBE_CUDA(c, cudaMemsetAsync(&c->dstats->flags, 0, sizeof(int), c->stream));
+  k_fill_pcell<<<cube_grid(c->ncells, 256), 256, 0, c->stream>>>(c->rhoc[k], c->cstart[k], c->ncells, c->pcell[k],
+                                                                 &c->dstats->flags);
   CUBE_CUDA(c, cudaGetLastError());
+  int64_t tot = -1;
+  int fl = 0;
+  CUBE_CUDA(c, cudaMemcpyAsync(&tot, c->cstart[k] + c->ncells, 8, cudaMemcpyDeviceToHost, c->stream));
+  CUBE_CUDA(c, cudaMemcpyAsync(&fl, &c->dstats->flags, 4, cudaMemcpyDeviceToHost, c->stream));
   CUBE_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (fl & (1 << 16)) return cube_fail(c, CUBE_ERR_ARG, "negative rhoc");
+  if (tot != np) return cube_fail(c, CUBE_ERR_COUNT_MISMATCH, "sum(rhoc) != nplocal");
   c->np = np;
   c->npglobal = np;
   c->have_state = true;

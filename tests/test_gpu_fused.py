@@ -38,3 +38,34 @@ def test_fused_pp_and_pm_match_the_two_calls():
     for key in ("xp", "vp", "pid", "rhoc", "vfield"):
         assert np.array_equal(sa[key], sb[key]), key
     assert ta[-1][2] > 0  # pairs were found
+
+
+def test_upload_rejects_inconsistent_counts():
+    # the counts are checked on the device after the copies: a sum that is
+    # not nplocal, or a negative count, is an error and leaves no state; a
+    # consistent upload afterwards works
+    from cafproject_gb300 import cube as C
+    from cafproject_gb300 import params as P
+    from cafproject_gb300 import synth
+    p = P.small(nc=24, nnt=2, pp_on=False)
+    st = synth.random_state(p, mean_per_cell=4, seed=3)
+    g = C.CubeGPU(p)
+    try:
+        bad = st["rhoc"].copy()
+        bad[5] += 1
+        with pytest.raises(C.CubeError) as e:
+            g.upload(st["xp"], st["vp"], st["pid"], bad, st["vfield"])
+        assert e.value.code == 6
+        neg = st["rhoc"].copy()
+        neg[7] -= neg[7] + 1
+        neg[8] += st["rhoc"][7] + 1
+        with pytest.raises(C.CubeError) as e:
+            g.upload(st["xp"], st["vp"], st["pid"], neg, st["vfield"])
+        assert e.value.code == 1
+        with pytest.raises(C.CubeError):
+            g.update_x(np.float32(1.0), np.float32(1.0), np.float32(0.1))  # no state
+        g.upload(st["xp"], st["vp"], st["pid"], st["rhoc"], st["vfield"])
+        assert g.nplocal() == st["xp"].shape[0]
+        assert np.array_equal(g.download()["rhoc"], st["rhoc"])
+    finally:
+        g.close()
