@@ -399,11 +399,14 @@ def run_batched(args, lrank, nsteps=50):
         t2 = time.perf_counter()
         tm = b.time()
         last = b.history(nsteps - 1)
+        per = b.step_times()
         b.close()
         out[name] = {"boxes_per_s": round(args.boxes / (t2 - t1), 3),
                      "box_steps_per_s": round(args.boxes * nsteps / (t2 - t1), 1), "steps_s": round(t2 - t1, 3),
                      "device_s": round(tm["device_ms"] / 1000.0, 3), "setup_s": round(t1 - t0, 3),
-                     "final_npairs": int(sum(h["npairs"] for h in last))}
+                     "final_npairs": int(sum(h["npairs"] for h in last)),
+                     "step_ms_first_mid_last": [round(float(per[0]), 1), round(float(per[nsteps // 2]), 1),
+                                                round(float(per[-1]), 1)]}
         if levels is not None:
             out[name]["pp_levels"] = {str(l): int((levels == l).sum()) for l in sorted(set(levels.tolist()))}
     nper = [p.nc * 2 for p, _ in ens]

@@ -52,6 +52,7 @@ def _bind(L):
     L.cube_batch_history.argtypes = [P, I, P]
     L.cube_batch_ctx.argtypes = [P, I, ctypes.POINTER(P)]
     L.cube_batch_time.argtypes = [P, P, P, P]
+    L.cube_batch_step_times.argtypes = [P, P]
     L._batch_bound = True
     return L
 
@@ -146,6 +147,13 @@ class Batch:
         ms, dev, n = ctypes.c_float(), ctypes.c_float(), ctypes.c_int64()
         self._check(self.L.cube_batch_time(self.h, ctypes.byref(ms), ctypes.byref(dev), ctypes.byref(n)))
         return {"wall_ms": ms.value, "device_ms": dev.value, "steps_done": n.value}
+
+    def step_times(self):
+        """Per step done: ms over all boxes (device time in graph mode)."""
+        n = self.time()["steps_done"]
+        ms = np.zeros(max(n, 1), np.float32)
+        self._check(self.L.cube_batch_step_times(self.h, ms.ctypes.data))
+        return ms[:n]
 
     def box(self, i):
         """The i-th box as a borrowed CubeGPU (download, power spectrum, ...)."""

@@ -57,6 +57,7 @@ struct cube_batch {
   std::vector<cudaEvent_t> join;
   int64_t steps_done = 0;
   float last_ms = 0.f, last_dev_ms = 0.f;  // wall clock / device time of the last cube_batch_step
+  std::vector<float> step_ms;              // per step: device time (graph) or wall clock (serial)
   std::string err;
 };
 
@@ -308,14 +309,28 @@ int graph_steps(cube_batch* b, int n) {
     }
   }
   const int64_t k0 = b->steps_done;
+  // an event between consecutive graph launches gives each step's device time
+  std::vector<cudaEvent_t> ev(n + 1, nullptr);
+  struct Events {
+    std::vector<cudaEvent_t>& v;
+    ~Events() {
+      for (cudaEvent_t e : v)
+        if (e) cudaEventDestroy(e);
+    }
+  } evs{ev};
+  for (cudaEvent_t& e : ev) BCUDA(b, cudaEventCreate(&e));
   BCUDA(b, cudaDeviceSynchronize());
   const auto w0 = std::chrono::steady_clock::now();
-  BCUDA(b, cudaEventRecord(b->t0, b->s0));
-  for (int k = 0; k < n; k++) BCUDA(b, cudaGraphLaunch(b->g[(k0 + k) & 1], b->s0));
-  BCUDA(b, cudaEventRecord(b->t1, b->s0));
+  BCUDA(b, cudaEventRecord(ev[0], b->s0));
+  for (int k = 0; k < n; k++) {
+    BCUDA(b, cudaGraphLaunch(b->g[(k0 + k) & 1], b->s0));
+    BCUDA(b, cudaEventRecord(ev[k + 1], b->s0));
+  }
   BCUDA(b, cudaStreamSynchronize(b->s0));
   b->last_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - w0).count();
-  BCUDA(b, cudaEventElapsedTime(&b->last_dev_ms, b->t0, b->t1));
+  BCUDA(b, cudaEventElapsedTime(&b->last_dev_ms, ev[0], ev[n]));
+  b->step_ms.resize((size_t)b->nsteps, 0.f);
+  for (int k = 0; k < n; k++) BCUDA(b, cudaEventElapsedTime(&b->step_ms[(size_t)(k0 + k)], ev[k], ev[k + 1]));
   b->steps_done = k0 + n;
   // the host's view of each context after an even or odd number of graph steps
   const int last = (int)((b->steps_done - 1) & 1);
@@ -346,10 +361,12 @@ int serial_steps(cube_batch* b, int n) {
   const int64_t k0 = b->steps_done;
   BCUDA(b, cudaDeviceSynchronize());
   const auto w0 = std::chrono::steady_clock::now();
+  b->step_ms.resize((size_t)b->nsteps, 0.f);
   for (int i = 0; i < b->nbox; i++) {
     cube_ctx* c = b->box[i];
     const float2* s = b->hsched.data() + (size_t)i * b->nsteps;
     for (int64_t k = k0; k < k0 + n; k++) {
+      const auto ws = std::chrono::steady_clock::now();
       const float dt = s[k].x, a_mid = s[k].y, dt_old = k > 0 ? s[k - 1].x : 0.f;
       cube_stats su{}, sp{}, sm{};
       int r = cube_update_x(c, dt_old, dt, b->vz[i], &su);
@@ -371,6 +388,7 @@ int serial_steps(cube_batch* b, int n) {
       o.itest1 = sp.itest1;
       o.ndup = su.ndup;
       o.sum_r = su.sum_r;
+      b->step_ms[(size_t)k] += std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - ws).count();
     }
   }
   BCUDA(b, cudaDeviceSynchronize());
@@ -466,6 +484,12 @@ extern "C" int cube_batch_time(const cube_batch* b, float* last_ms, float* last_
   if (last_ms) *last_ms = b->last_ms;
   if (last_dev_ms) *last_dev_ms = b->last_dev_ms;
   if (steps_done) *steps_done = b->steps_done;
+  return CUBE_OK;
+}
+
+extern "C" int cube_batch_step_times(const cube_batch* b, float* ms) {
+  if (!b || !ms) return CUBE_ERR_ARG;
+  for (int64_t k = 0; k < b->steps_done; k++) ms[k] = k < (int64_t)b->step_ms.size() ? b->step_ms[(size_t)k] : 0.f;
   return CUBE_OK;
 }
 

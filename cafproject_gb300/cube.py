@@ -37,7 +37,8 @@ EXPORTS = ["cube_create", "cube_destroy", "cube_last_error", "cube_upload_state"
            "cube_dpm_set_schedule", "cube_dpm_noise", "cube_dpm_forward", "cube_dpm_backward", "cube_dpm_density",
            "cube_dpm_density_adjoint", "cube_dpm_tables", "cube_dpm_info",
            "cube_batch_create", "cube_batch_destroy", "cube_batch_last_error", "cube_batch_set_schedule",
-           "cube_batch_autotune", "cube_batch_step", "cube_batch_history", "cube_batch_ctx", "cube_batch_time"]
+           "cube_batch_autotune", "cube_batch_step", "cube_batch_history", "cube_batch_ctx", "cube_batch_time",
+           "cube_batch_step_times"]
 CODEC_STATIC_MAX = 16384
 OPT_EXACT_KICKS = 1
 OPT_PP_LEVEL = 2

@@ -349,6 +349,9 @@ int cube_batch_step(cube_batch* batch, int nsteps);
 int cube_batch_history(cube_batch* batch, int step, cube_batch_stats* out);  /* nbox entries */
 int cube_batch_ctx(cube_batch* batch, int box, cube_ctx** ctx);  /* the box's context */
 int cube_batch_time(const cube_batch* batch, float* last_ms, float* last_dev_ms, int64_t* steps_done);
+/* per step done so far, the time of that step over all boxes (ms; device
+   time between graph launches, or the serial wall clock summed over boxes) */
+int cube_batch_step_times(const cube_batch* batch, float* ms);
 
 /* ------------------------------------------------------------------------
    Differentiable form (no reference counterpart: the reference has no
