@@ -98,16 +98,17 @@ __device__ __forceinline__ float from_fix(long long q) {
   return neg ? -r : r;
 }
 
-// one pair: accumulate the force of a particle at offset r (FP32).  1/|r|
-// comes from the hardware reciprocal square root (a few ulps; the pair sum's
-// tolerance against the reference's FP64 is 1e-5), which spares the IEEE
-// square root and division their multi-instruction sequences.
+// one pair: accumulate the force of a particle at offset r (FP32).  1/|r| is
+// the correctly rounded reciprocal square root, |r| = r^2 * (1/|r|), and
+// 1/|r|^3 three more roundings: within about two ulps like the square root
+// plus division it replaces, at fewer instructions (the approximate hardware
+// reciprocal square root alone moved the codes of the strongest kicks by two)
 __device__ __forceinline__ void pair_force(const PPArgs& a, float rx, float ry, float rz, long long* acc) {
   // explicit roundings: every kernel evaluates the same bits for a pair
   float r2 = __fmaf_rn(rx, rx, __fmaf_rn(ry, ry, __fmul_rn(rz, rz)));
-  float ri = rsqrtf(r2);        // +inf for the self pair
+  float ri = __frsqrt_rn(r2);    // +inf for the self pair
   float rm = __fmul_rn(r2, ri);  // NaN for the self pair
-  if (!(rm > a.rsoft)) return;  // merge(force,0,rmag>rsoft); self pairs excluded
+  if (!(rm > a.rsoft)) return;   // merge(force,0,rmag>rsoft); self pairs excluded
   float rc = __fmul_rn(rm, a.inv_cut);
   float rc3 = __fmul_rn(__fmul_rn(rc, rc), rc);
   // pcut = 1 - 1.75 rc^3 + 0.75 rc^5  (ext_pp_force.f90:107)
