@@ -407,8 +407,11 @@ def run_batched(args, lrank, nsteps=50):
                      "final_npairs": int(sum(h["npairs"] for h in last)),
                      "step_ms_first_mid_last": [round(float(per[0]), 1), round(float(per[nsteps // 2]), 1),
                                                 round(float(per[-1]), 1)]}
-        if levels is not None:
-            out[name]["pp_levels"] = {str(l): int((levels == l).sum()) for l in sorted(set(levels.tolist()))}
+        if levels is not None:  # autotuned (PP level, fine deposit shape, coarse deposit shape) per geometry
+            tuned = {}
+            for (pn, _), ch in zip(ens, levels):
+                tuned["%d^3" % (pn.nc * 2)] = [int(x) for x in ch]
+            out[name]["tuned"] = tuned
     nper = [p.nc * 2 for p, _ in ens]
     return {"workload": "%d boxes of %s^3 particles (uniform), fine mesh 2x the particle grid, PM+PP, %d steps "
                         "z=19->0 (equal in ln a), Omega_m U[0.25,0.35], sigma_8 U[0.7,0.9]"

@@ -131,9 +131,10 @@ class Batch:
         return dt, am
 
     def autotune(self):
-        lv = np.zeros(self.nbox, np.int32)
-        self._check(self.L.cube_batch_autotune(self.h, lv.ctypes.data))
-        return lv
+        """(nbox, 3) int32: PP start level, fine and coarse deposit brick shape per box."""
+        ch = np.zeros((self.nbox, 3), np.int32)
+        self._check(self.L.cube_batch_autotune(self.h, ch.ctypes.data))
+        return ch
 
     def step(self, n=1):
         self._check(self.L.cube_batch_step(self.h, int(n)))

@@ -439,6 +439,11 @@ extern "C" int cube_set_option(cube_ctx* c, int option, int64_t value) {
       if (value < 0 || value > 4) return cube_fail(c, CUBE_ERR_ARG, "PP level must be 0 to 4");
       c->opt_pp_level = (int)value;
       return CUBE_OK;
+    case CUBE_OPT_DEPOSIT_FINE:
+    case CUBE_OPT_DEPOSIT_COARSE:
+      if (value < 0 || value > 3) return cube_fail(c, CUBE_ERR_ARG, "deposit brick shape must be 0 to 3");
+      (option == CUBE_OPT_DEPOSIT_FINE ? c->opt_dep_fine : c->opt_dep_coarse) = (int)value;
+      return CUBE_OK;
     default:
       return cube_fail(c, CUBE_ERR_ARG, "unknown option");
   }

@@ -410,18 +410,60 @@ extern "C" int cube_batch_step(cube_batch* b, int nsteps) {
   return b->mode == CUBE_BATCH_GRAPH ? graph_steps(b, nsteps) : serial_steps(b, nsteps);
 }
 
-extern "C" int cube_batch_autotune(cube_batch* b, int32_t* levels) {
+namespace {
+
+// device time of f() on c's stream: the median of three runs after one
+float time_on(cube_batch* b, cube_ctx* c, int (*f)(cube_ctx*), int* err) {
+  float t[4] = {0, 0, 0, 0};
+  for (int rep = 0; rep < 4; rep++) {
+    if (cudaEventRecord(b->t0, c->stream) != cudaSuccess || (*err = f(c)) ||
+        cudaEventRecord(b->t1, c->stream) != cudaSuccess || cudaEventSynchronize(b->t1) != cudaSuccess ||
+        cudaEventElapsedTime(&t[rep], b->t0, b->t1) != cudaSuccess) {
+      if (!*err) *err = CUBE_ERR_CUDA;
+      return 0.f;
+    }
+  }
+  std::sort(t + 1, t + 4);
+  return t[2];
+}
+int fine_density_only(cube_ctx* c) { return cube_fine_density_impl(c, nullptr, false); }
+int coarse_density_only(cube_ctx* c) { return cube_coarse_density_impl(c, nullptr, false); }
+
+}  // namespace
+
+extern "C" int cube_batch_autotune(cube_batch* b, int32_t* choices) {
   if (!b) return CUBE_ERR_ARG;
   BCUDA(b, cudaSetDevice(b->device));
   if (b->steps_done || b->g[0]) return bfail(b, CUBE_ERR_STATE, "tune before the first step");
-  // per distinct box geometry: the PP start level (its staging tile shapes)
-  // with the least device time on the first such box's initial state; the
-  // levels give identical results, so only time depends on the choice
+  // per distinct box geometry, on the first such box's initial state and by
+  // device time: the fine and coarse deposits' brick shapes (their shared-
+  // memory tiles), then the PP start level (which staging tiles carry the
+  // pairs).  Every choice gives bitwise the same results; only time depends
+  // on it.  The deposits leave the particles alone; PP kicks them, so its
+  // trials run on a copy of the state that is put back afterwards.
   std::vector<int> done(b->nbox, 0);
   for (int i = 0; i < b->nbox; i++) {
     if (done[i]) continue;
     cube_ctx* c = b->box[i];
-    int best = 0;
+    int err = 0;
+    int best_f = 0, best_c = 0, best_pp = 0;
+    float bf = 1e30f, bc = 1e30f;
+    for (int v = 0; v < 4; v++) {
+      c->opt_dep_fine = v;
+      const float t = time_on(b, c, fine_density_only, &err);
+      if (err) return bfail(b, err, c->err);
+      if (t < bf) {
+        bf = t;
+        best_f = v;
+      }
+      c->opt_dep_coarse = v;
+      const float u = time_on(b, c, coarse_density_only, &err);
+      if (err) return bfail(b, err, c->err);
+      if (u < bc) {
+        bc = u;
+        best_c = v;
+      }
+    }
     if (c->p.pp_on) {
       const int64_t np = c->np;
       std::vector<char> xp(3 * (size_t)np * c->p.izipx), vp(3 * (size_t)np * c->p.izipv);
@@ -447,23 +489,29 @@ extern "C" int cube_batch_autotune(cube_batch* b, int32_t* levels) {
         }
         if (ms < bestms) {
           bestms = ms;
-          best = lev;
+          best_pp = lev;
         }
       }
       if ((r = cube_upload_state(c, n, xp.data(), vp.data(), pid.data(), rhoc.data(), vf.data())))
         return bfail(b, r, c->err);
     }
     for (int j = i; j < b->nbox; j++) {
-      const cube_params& q = b->box[j]->p;
-      if (!done[j] && q.nc == c->p.nc && q.pp_on == c->p.pp_on) {
-        b->box[j]->opt_pp_level = best;
-        b->pp_level[j] = best;
+      cube_ctx* q = b->box[j];
+      if (!done[j] && q->p.nc == c->p.nc && q->p.pp_on == c->p.pp_on) {
+        q->opt_pp_level = best_pp;
+        q->opt_dep_fine = best_f;
+        q->opt_dep_coarse = best_c;
+        b->pp_level[j] = best_pp;
         done[j] = 1;
       }
     }
   }
-  if (levels)
-    for (int i = 0; i < b->nbox; i++) levels[i] = b->pp_level[i];
+  if (choices)
+    for (int i = 0; i < b->nbox; i++) {
+      choices[3 * i] = b->box[i]->opt_pp_level;
+      choices[3 * i + 1] = b->box[i]->opt_dep_fine;
+      choices[3 * i + 2] = b->box[i]->opt_dep_coarse;
+    }
   return CUBE_OK;
 }
 

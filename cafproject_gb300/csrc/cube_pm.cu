@@ -204,6 +204,27 @@ int launch_deposit(cube_ctx* c, const DepArgs& a) {
   return CUBE_OK;
 }
 
+// The deposits' brick shapes (cube_set_option CUBE_OPT_DEPOSIT_FINE / _COARSE):
+// larger bricks re-read fewer neighbour particles, smaller ones hold less
+// shared memory per CTA (more CTAs per SM) and give small meshes more CTAs.
+// Every shape writes the same exact fixed-point sums.
+int launch_fine_deposit(cube_ctx* c, const DepArgs& a) {
+  switch (c->opt_dep_fine) {
+    case 1: return launch_deposit<4, 4, 4, 4, 1, 0>(c, a);  // 16^3 fine cells, 32 KB
+    case 2: return launch_deposit<4, 8, 4, 2, 1, 0>(c, a);  // 32x16x8, 32 KB
+    case 3: return launch_deposit<4, 4, 4, 2, 1, 0>(c, a);  // 16x16x8, 16 KB
+    default: return launch_deposit<4, 8, 4, 4, 1, 0>(c, a);  // 32x16x16, 64 KB
+  }
+}
+int launch_coarse_deposit(cube_ctx* c, const DepArgs& a) {
+  switch (c->opt_dep_coarse) {
+    case 1: return launch_deposit<1, 16, 8, 8, 1, 1>(c, a);
+    case 2: return launch_deposit<1, 8, 8, 4, 1, 1>(c, a);
+    case 3: return launch_deposit<1, 4, 4, 4, 1, 1>(c, a);
+    default: return launch_deposit<1, 8, 8, 8, 1, 1>(c, a);
+  }
+}
+
 // ------------------------------------------------------- spectral multiply
 // out_d = i*K_d*rho_k for the three components in one pass (pm.f90:119-120)
 __global__ void k_green3(const float2* __restrict__ rk, const float* __restrict__ kern, int64_t n,
@@ -548,7 +569,7 @@ int cube_fine_density_impl(cube_ctx* c, cube_stats* st, bool accumulate) {
   DepArgs a{g, c->xp[c->cur], c->rhoc[c->cur], c->cstart[c->cur], c->p.mass_p, c->rho_f, &c->dstats->rhof_fix, 0,
             std::ldexp(1.0f, sh), std::ldexp(1.0f, -sh), accumulate ? 1 : 0};
   cube_phase_begin(c, PH_F_DEPOSIT);
-  int r = launch_deposit<4, 8, 4, 4, 1, 0>(c, a);
+  int r = launch_fine_deposit(c, a);
   cube_phase_end(c, PH_F_DEPOSIT);
   if (r) return r;
   if (st) {
@@ -657,7 +678,7 @@ int cube_coarse_density_impl(cube_ctx* c, cube_stats* st, bool accumulate) {
   DepArgs a{g, c->xp[c->cur], c->rhoc[c->cur], c->cstart[c->cur], c->p.mass_p, c->rho_c, &c->dstats->rhoc_fix, 0,
             std::ldexp(1.0f, sh), std::ldexp(1.0f, -sh), accumulate ? 1 : 0};
   cube_phase_begin(c, PH_C_DEPOSIT);
-  int r = launch_deposit<1, 8, 8, 8, 1, 1>(c, a);
+  int r = launch_coarse_deposit(c, a);
   cube_phase_end(c, PH_C_DEPOSIT);
   if (r) return r;
   if (st) {

@@ -43,6 +43,8 @@ CODEC_STATIC_MAX = 16384
 OPT_EXACT_KICKS = 1
 OPT_PP_LEVEL = 2
 OPT_RANK_WALK = 3
+OPT_DEPOSIT_FINE = 4
+OPT_DEPOSIT_COARSE = 5
 NPHASE = 16
 
 

@@ -280,8 +280,18 @@ void* cube_stream(cube_ctx* ctx);
    are order-independent, so every level gives bitwise the same result; used
    to test the dense-region paths.  CUBE_OPT_RANK_WALK=3 makes cube_update_x
    use its general visit-order walker for the ranks instead of the counting
-   path it takes when every particle moved at most one cell (same result). */
-enum cube_option { CUBE_OPT_EXACT_KICKS = 1, CUBE_OPT_PP_LEVEL = 2, CUBE_OPT_RANK_WALK = 3 };
+   path it takes when every particle moved at most one cell (same result).
+   CUBE_OPT_DEPOSIT_FINE=4 / CUBE_OPT_DEPOSIT_COARSE=5 pick the brick shape
+   of the fine / coarse density deposit (0-3; fine: 8x4x4, 4x4x4, 8x4x2,
+   4x4x2 coarse cells; coarse: 8x8x8, 16x8x8, 8x8x4, 4x4x4): a tile-size
+   choice for the autotuner, same exact sums for every shape. */
+enum cube_option {
+  CUBE_OPT_EXACT_KICKS = 1,
+  CUBE_OPT_PP_LEVEL = 2,
+  CUBE_OPT_RANK_WALK = 3,
+  CUBE_OPT_DEPOSIT_FINE = 4,
+  CUBE_OPT_DEPOSIT_COARSE = 5
+};
 int cube_set_option(cube_ctx* ctx, int option, int64_t value);
 
 /* Velocity-code self check: encodes n host doubles with sigma both by the
@@ -341,9 +351,12 @@ const char* cube_batch_last_error(const cube_batch* batch);
 /* dt and a_mid per box and step, host arrays [nbox][nsteps]; dt_old of the
    first step is 0 (timestep.f90:4) */
 int cube_batch_set_schedule(cube_batch* batch, int nsteps, const float* dt, const float* a_mid);
-/* per distinct box geometry, the PP start level (its staging tile shapes)
-   with the least device time; levels[nbox] receives the choice */
-int cube_batch_autotune(cube_batch* batch, int32_t* levels);
+/* per distinct box geometry, by device time on the box's initial state: the
+   fine and coarse deposits' brick shapes (CUBE_OPT_DEPOSIT_FINE / _COARSE)
+   and the PP start level (which staging tiles carry the pairs); choices
+   (3 x nbox int32, may be null) receives (PP level, fine shape, coarse
+   shape) per box.  Results do not depend on the choices. */
+int cube_batch_autotune(cube_batch* batch, int32_t* choices);
 /* advance every box nsteps steps of its schedule */
 int cube_batch_step(cube_batch* batch, int nsteps);
 int cube_batch_history(cube_batch* batch, int step, cube_batch_stats* out);  /* nbox entries */

@@ -38,7 +38,8 @@ def serial():
 def test_graph_matches_serial_bitwise(serial):
     hs, ss, _, _ = serial
     hg, sg, levels, t = run(0, [3, 2], tune=True)
-    assert all(0 <= l <= 4 for l in levels)
+    assert levels.shape == (4, 3)
+    assert all(0 <= l <= 4 for l in levels[:, 0]) and levels[:, 1:].min() >= 0 and levels[:, 1:].max() <= 3
     for k in range(5):
         for i in range(4):
             a, b = hs[k][i], hg[k][i]
