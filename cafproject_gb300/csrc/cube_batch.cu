@@ -37,7 +37,6 @@
 struct cube_batch {
   int device = 0, mode = 0, nbox = 0, nsteps = 0;
   std::vector<cube_ctx*> box;
-  std::vector<cube_batch_box> desc;
   std::vector<int> pp_level;
   std::vector<float> vz;         // serial mode: sim%vz_max per box (host)
   std::vector<cube_batch_stats> hhist;  // serial mode: per step and box
@@ -207,7 +206,6 @@ extern "C" int cube_batch_create(const cube_batch_box* boxes, int nbox, const fl
   b->device = device;
   b->mode = mode;
   b->nbox = nbox;
-  b->desc.assign(boxes, boxes + nbox);
   BCUDA(b, cudaSetDevice(device));
   BCUDA(b, cudaStreamCreateWithFlags(&b->s0, cudaStreamNonBlocking));
   BCUDA(b, cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));

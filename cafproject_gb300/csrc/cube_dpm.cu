@@ -57,7 +57,6 @@ struct cube_dpm {
   cube_ctx base;  // device, stream and error text
   Lattice lat_{};
   cube_dpm_params p{};
-  cube_cosmology cs{};
   int ng = 0, npd = 0, step = 0;
   int64_t np = 0;
   float mass = 0.f, vf = 0.f;
@@ -556,7 +555,6 @@ extern "C" int cube_dpm_create(const cube_dpm_params* p, const cube_cosmology* c
   if (!d) return CUBE_ERR_NOMEM;
   *out = d;
   d->p = *p;
-  d->cs = *cs;
   d->base.device = device;
   if (p->ng < 16 || p->ng % 2 || p->npd < 16 || p->npd % 2 || p->ng % p->npd)
     return dpm_fail(d, CUBE_ERR_ARG, "ng and npd must be even, at least 16, and npd must divide ng");
