@@ -38,6 +38,7 @@ struct DevStats {
   unsigned long long npairs, itest1;
   unsigned long long ndup_list;  // entries in the extra-copy list
   unsigned long long nexact;     // kick lanes evaluated on the exact FP64 chain
+  unsigned int vmax_est_bits[3]; // fine kick: max |v + vfield| in FP32, when the last vmax is unknown
   double testrhof, testrhoc;
   unsigned long long rhof_fix, rhoc_fix;  // deposited mass in 2^-32 fixed point
 };

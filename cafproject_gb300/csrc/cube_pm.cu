@@ -302,10 +302,15 @@ struct KickArgs {
   int exact_only;          // skip the certified fast path
   unsigned long long* nexact;
   const StepDev* sd;       // graph mode: a_mid, dt, tau from the device
+  unsigned int* vmax_est;        // fine kick: record max |v + vfield| (FP32) here when set
+  const unsigned int* tau_est;   // coarse kick: tau = 0.7 of this estimate when set
 };
 __device__ __forceinline__ float kick_amid(const KickArgs& a) { return a.sd ? __ldg(&a.sd->h.a_mid) : a.a_mid; }
 __device__ __forceinline__ float kick_dt(const KickArgs& a) { return a.sd ? __ldg(&a.sd->h.dt) : a.dt; }
-__device__ __forceinline__ float kick_tau(const KickArgs& a, int d) { return a.sd ? __ldg(&a.sd->h.tau[d]) : a.tau[d]; }
+__device__ __forceinline__ float kick_tau(const KickArgs& a, int d) {
+  if (a.sd) return __ldg(&a.sd->h.tau[d]);
+  return a.tau_est ? __fmul_rn(0.7f, __uint_as_float(__ldg(a.tau_est + d))) : a.tau[d];
+}
 
 // The kick velocity of the reference is the FP64 chain
 //   v = decode; v = v + t1; ...; v = v + t8       (pm.f90:145-153)
@@ -327,7 +332,7 @@ __global__ void __launch_bounds__(256, 4) k_kick(KickArgs a) {
     if (!need) return;
   }
   const Geo& g = a.g;
-  float vm[3] = {0.f, 0.f, 0.f};
+  float vm[3] = {0.f, 0.f, 0.f};  // coarse: exact vmax; fine: the FP32 estimate
   unsigned long long nex = 0;
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.np; p += (int64_t)gridDim.x * blockDim.x) {
     int64_t cell = a.pcell[p];
@@ -390,6 +395,8 @@ __global__ void __launch_bounds__(256, 4) k_kick(KickArgs a) {
         vfd = a.vfield[3 * cell + d];
         float ub = (fabsf(vf) + E + fabsf(vfd)) * 1.000001f;
         need_vmax = a.vmax_only || ub >= kick_tau(a, d);
+      } else if (a.vmax_est) {
+        vm[d] = fmaxf(vm[d], fabsf(__fadd_rn(vf, a.vfield[3 * cell + d])));
       }
       long long out;
       if (ok && !need_vmax) {
@@ -409,11 +416,11 @@ __global__ void __launch_bounds__(256, 4) k_kick(KickArgs a) {
       if (!a.vmax_only) store_code(a.vp_out, 3 * p + d, g.izipv, out);
     }
   }
-  if (!kFine) {
+  if (!kFine || a.vmax_est) {
     for (int d = 0; d < 3; d++) {
       float m = vm[d];
       for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-      if ((threadIdx.x & 31) == 0) atomic_max_pos(&a.vmax_bits[d], m);
+      if ((threadIdx.x & 31) == 0) atomic_max_pos(kFine ? &a.vmax_est[d] : &a.vmax_bits[d], m);
     }
   }
   for (int o = 16; o > 0; o >>= 1) nex += __shfl_xor_sync(0xffffffffu, nex, o);
@@ -645,6 +652,11 @@ int cube_fine_kick_impl(cube_ctx* c, float a_mid, float dt, bool pre) {
   k.vmax_bits = nullptr;
   k.nexact = &c->dstats->nexact;
   k.exact_only = c->opt_exact_kicks;
+  // after an upload or initial conditions the last vmax is unknown: the fine
+  // kick then records the velocities' maxima for the coarse kick's threshold
+  // (the fine density of this step zeroed the estimate)
+  if (!c->graph_mode && c->vmax_prev[0] == 0.f && c->vmax_prev[1] == 0.f && c->vmax_prev[2] == 0.f)
+    k.vmax_est = c->dstats->vmax_est_bits;
   cube_phase_begin(c, PH_F_KICK);
   if (pre)
     k_kick<true, true><<<cube_grid(c->np, 256), 256, 0, c->stream>>>(k);
@@ -751,6 +763,10 @@ int cube_coarse_kick_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st, bo
     // last vmax is evaluated exactly; if none does, the whole vmax is redone
     k.tau[d] = 0.7f * c->vmax_prev[d];
   }
+  // last vmax unknown: 0.7 of the fine kick's FP32 maxima instead (zero when
+  // no fine kick recorded them: every lane exact)
+  const bool est = !c->graph_mode && c->vmax_prev[0] == 0.f && c->vmax_prev[1] == 0.f && c->vmax_prev[2] == 0.f;
+  if (est) k.tau_est = c->dstats->vmax_est_bits;
   k.a_mid = a_mid;
   k.dt = dt;
   k.vmax_bits = c->dstats->vmax_bits;
@@ -785,7 +801,8 @@ int cube_coarse_kick_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st, bo
   bool rerun = false;
   for (int d = 0; d < 3; d++) {
     vm[d] = bits_float(c->hstats->vmax_bits[d]);
-    if (!(vm[d] >= k.tau[d])) rerun = true;
+    const float tau = est ? 0.7f * bits_float(c->hstats->vmax_est_bits[d]) : k.tau[d];
+    if (!(vm[d] >= tau)) rerun = true;
   }
   unsigned long long nex = c->hstats->nexact;
   if (rerun) {
