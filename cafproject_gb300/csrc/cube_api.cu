@@ -54,7 +54,7 @@ static void release(cube_ctx* c) {
   }
   void* bufs[] = {c->xp[0], c->xp[1], c->vp[0], c->vp[1], c->pid[0], c->pid[1], c->pcell[0], c->pcell[1],
                   c->rhoc[0], c->rhoc[1],
-                  c->vfield[0], c->vfield[1], c->cstart[0], c->cstart[1], c->dest, c->dframe, c->doff, c->lrank, c->offc, c->perm, c->rank, c->xtra,
+                  c->vfield[0], c->vfield[1], c->cstart[0], c->cstart[1], c->dest, c->dframe, c->doff, c->lrank, c->offc, c->perm, c->vdense, c->rank, c->xtra,
                   c->scan_tmp, c->red_tmp, c->tan_tab, c->codec[0].dec, c->codec[1].dec, c->codec[0].bnd, c->codec[1].bnd, c->codec[0].dech, c->codec[1].dech, c->rho_f, c->force_f[0],
                   c->force_f[1], c->force_f[2], c->kern_f, c->kern_f_raw, c->rho_c, c->force_c[0],
                   c->force_c[1], c->force_c[2], c->kern_c, c->fpp, c->pp_list[0], c->pp_list[1], c->pp_list[2], c->pp_list[3], c->pp_nlist, c->dstats,
@@ -163,6 +163,7 @@ static int create_impl(const cube_params* p, const float* fine_table, const floa
   ALLOC(c->lrank, 2 * np);
   ALLOC(c->offc, 2 * 27 * c->ncells);
   ALLOC(c->perm, 4 * np);
+  ALLOC(c->vdense, 4 * c->ncells);
   ALLOC(c->rank, 4 * np);
   c->xtra_cap = 1 << 20;
   ALLOC(c->xtra, sizeof(int4) * c->xtra_cap);

@@ -37,6 +37,7 @@ struct DevStats {
   unsigned int vmax_bits[3];
   unsigned long long npairs, itest1;
   unsigned long long ndup_list;  // entries in the extra-copy list
+  unsigned int ndense;           // destination cells left to the warp-per-cell vfield pass
   unsigned long long nexact;     // kick lanes evaluated on the exact FP64 chain
   unsigned int vmax_est_bits[3]; // fine kick: max |v + vfield| in FP32, when the last vmax is unknown
   double testrhof, testrhoc;
@@ -105,6 +106,7 @@ struct cube_ctx {
   uint16_t* lrank = nullptr;    // rank among the particles of one source cell bound for one destination
   uint16_t* offc = nullptr;     // 27 planes over the source cells: counts bound for each neighbour, then base ranks
   int32_t* perm = nullptr;      // new position -> old particle index
+  int32_t* vdense = nullptr;    // destination cells with many particles (vfield_new by a warp each)
   uint32_t* rank = nullptr;     // rank of the primary copy in its destination
   int4* xtra = nullptr;         // extra copies: (particle, dest cell, rank, -)
   int64_t xtra_cap = 0;

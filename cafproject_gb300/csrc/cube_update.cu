@@ -55,6 +55,7 @@ struct UpdArgs {
   int32_t* pid_new;
   int32_t* pcell_new;
   const StepDev* sd;  // graph mode: dt_mid and nlayer from the device
+  int32_t* vdense;    // destination cells over VF_DENSE particles, for k_vfield_dense
 };
 
 __device__ __forceinline__ float dtm(const UpdArgs& a) { return a.sd ? __ldg(&a.sd->h.dt_mid) : a.dt_mid; }
@@ -217,10 +218,7 @@ __global__ void k_dest(UpdArgs a) {
 // rounded to real(4), with vreal = decode + vfield(source) in real(8).  Fast
 // path: the exact sum acc + dec + vfield as float-float, certified to round to
 // the same float as the reference's two FP64 roundings followed by one FP32.
-__device__ __forceinline__ float accumulate_v(const UpdArgs& a, float acc, int64_t p, int d, int64_t S) {
-  int vcode = load_code(a.vp, 3 * p + d, a.g.izipv);
-  float2 dd = codec_decode_ff(a.cv, vcode);
-  float vfs = a.vfield[3 * S + d];
+__device__ __forceinline__ float accumulate_vals(const UpdArgs& a, float acc, int vcode, float2 dd, float vfs) {
   float s1, e1, s2, e2;
   two_sum(acc, dd.x, s1, e1);
   two_sum(s1, vfs, s2, e2);
@@ -230,6 +228,10 @@ __device__ __forceinline__ float accumulate_v(const UpdArgs& a, float acc, int64
   float r;
   if (!a.exact_only && round_certified(s2, lo, margin, &r)) return r;
   return accumulate_exact(a.cv, vcode, vfs, acc);
+}
+__device__ __forceinline__ float accumulate_v(const UpdArgs& a, float acc, int64_t p, int d, int64_t S) {
+  const int vcode = load_code(a.vp, 3 * p + d, a.g.izipv);
+  return accumulate_vals(a, acc, vcode, codec_decode_ff(a.cv, vcode), a.vfield[3 * S + d]);
 }
 
 // vfield_new/(rhoce+weight_v) (update_particle.f90:81-83): the denominator
@@ -372,14 +374,22 @@ __global__ void k_rank_place(UpdArgs a) {
   }
 }
 
+// a cell over VF_DENSE particles goes to k_vfield_dense: one thread summing
+// hundreds of particles in rank order, three dependent loads each, would set
+// the kernel's tail
+constexpr uint32_t VF_DENSE = 64;
 __global__ void k_vfield_new(UpdArgs a) {
   if (a.sd && counting_failed(a)) return;
   for (int64_t D = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; D < a.ncells;
        D += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t cnt = (uint32_t)a.cnt_new[D];
+    if (cnt > VF_DENSE) {
+      a.vdense[atomicAdd(&a.st->ndense, 1u)] = (int32_t)D;
+      continue;
+    }
     float acc[3];
 #pragma unroll
     for (int d = 0; d < 3; d++) acc[d] = __fmul_rn(a.vfield[3 * D + d], 0.1f);  // vfield*weight_v
-    const uint32_t cnt = (uint32_t)a.cnt_new[D];
     const int64_t i0 = a.cstart_new[D];
     for (uint32_t i = 0; i < cnt; i++) {
       int64_t p = a.perm[i0 + i];
@@ -389,6 +399,46 @@ __global__ void k_vfield_new(UpdArgs a) {
     }
 #pragma unroll
     for (int d = 0; d < 3; d++) a.vfield_new[3 * D + d] = vfield_quotient(acc[d], cnt, a.exact_only);
+  }
+}
+
+// vfield_new of the listed dense cells, one warp per cell: the lanes load 32
+// particles' codes, decoded values and source-cell means at a time (all
+// independent), then lanes 0-2 -- one per component -- run the reference's
+// sequential real(4) sum over them in rank order, the same arithmetic as
+// k_vfield_new's thread
+__global__ void __launch_bounds__(128) k_vfield_dense(UpdArgs a) {
+  if (a.sd && counting_failed(a)) return;
+  __shared__ float2 sdd[4][32][3];
+  __shared__ float svf[4][32][3];
+  __shared__ int scode[4][32][3];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+  const uint32_t n = *(volatile unsigned int*)&a.st->ndense;
+  for (int64_t it = blockIdx.x * (int64_t)(blockDim.x >> 5) + w; it < (int64_t)n; it += nw) {
+    const int64_t D = a.vdense[it];
+    const uint32_t cnt = (uint32_t)a.cnt_new[D];
+    const int64_t i0 = a.cstart_new[D];
+    float acc = lane < 3 ? __fmul_rn(a.vfield[3 * D + lane], 0.1f) : 0.f;  // vfield*weight_v
+    for (uint32_t j0 = 0; j0 < cnt; j0 += 32) {
+      const uint32_t m = min(32u, cnt - j0);
+      if ((uint32_t)lane < m) {
+        const int64_t p = a.perm[i0 + j0 + lane];
+        const int64_t S = a.pcell[p];
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          const int vcode = load_code(a.vp, 3 * p + d, a.g.izipv);
+          scode[w][lane][d] = vcode;
+          sdd[w][lane][d] = codec_decode_ff(a.cv, vcode);
+          svf[w][lane][d] = a.vfield[3 * S + d];
+        }
+      }
+      __syncwarp();
+      if (lane < 3)
+        for (uint32_t j = 0; j < m; j++) acc = accumulate_vals(a, acc, scode[w][j][lane], sdd[w][j][lane], svf[w][j][lane]);
+      __syncwarp();
+    }
+    if (lane < 3) a.vfield_new[3 * D + lane] = vfield_quotient(acc, cnt, a.exact_only);
   }
 }
 
@@ -654,6 +704,7 @@ static int update_x_graph(cube_ctx* c) {
   a.vp_new = c->vp[kn];
   a.pid_new = c->pid[kn];
   a.pcell_new = c->pcell[kn];
+  a.vdense = c->vdense;
   const int B = 256;
   cudaStream_t s = c->stream;
   CUBE_CUDA(c, cudaMemsetAsync(c->rank, 0xFF, 4 * (size_t)c->np, s));
@@ -667,6 +718,7 @@ static int update_x_graph(cube_ctx* c) {
   if (r) return r;
   k_rank_place<<<cube_grid(c->np, B), B, 0, s>>>(a);
   k_vfield_new<<<cube_grid(c->ncells, 128, 32), 128, 0, s>>>(a);
+  k_vfield_dense<<<cube_grid((int64_t)1 << 40, 1, 4), 128, 0, s>>>(a);
   k_scatter<<<cube_grid(c->np, B), B, 0, s>>>(a);
   k_scatter_xtra<<<cube_grid(c->xtra_cap, B, 2), B, 0, s>>>(a);
   const int nb = c->red_blocks;
@@ -728,6 +780,7 @@ int cube_update_x_impl(cube_ctx* c, float dt_old, float dt, float vz_max, cube_s
   a.vp_new = c->vp[kn];
   a.pid_new = c->pid[kn];
   a.pcell_new = c->pcell[kn];
+  a.vdense = c->vdense;
   const int B = 256;
   CUBE_CUDA(c, cudaMemsetAsync(c->rank, 0xFF, 4 * (size_t)c->np, c->stream));  // "no rank" sentinel
   cube_phase_begin(c, PH_UPD_DEST);
@@ -777,6 +830,7 @@ int cube_update_x_impl(cube_ctx* c, float dt_old, float dt, float vz_max, cube_s
     cube_phase_begin(c, PH_UPD_PLACE);
     k_rank_place<<<cube_grid(c->np, B), B, 0, c->stream>>>(a);
     k_vfield_new<<<cube_grid(c->ncells, 128, 32), 128, 0, c->stream>>>(a);
+    k_vfield_dense<<<cube_grid((int64_t)1 << 40, 1, 4), 128, 0, c->stream>>>(a);
     cube_phase_end(c, PH_UPD_PLACE);
     CUBE_CUDA(c, cudaGetLastError());
   }

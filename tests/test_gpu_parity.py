@@ -48,6 +48,10 @@ CASES = [
     ("nnt1_x1v2", dict(nc=32, nnt=1, izipx=1, izipv=2), dict(mean_per_cell=4, seed=2, vsig=0.02)),
     ("nnt2_x2v1", dict(nc=24, nnt=2, izipx=2, izipv=1), dict(mean_per_cell=5, seed=3, vsig=0.02)),
     ("nnt3_clump", dict(nc=36, nnt=3, izipx=1, izipv=2), dict(mean_per_cell=3, seed=4, vsig=0.03, clump=30)),
+    # three cells of ~600 particles: their new velocity means go through the
+    # warp-per-cell pass
+    ("nnt2_dense", dict(nc=24, nnt=2, izipx=1, izipv=2), dict(mean_per_cell=4, seed=5, vsig=0.02, clump=3,
+                                                             clump_mult=150)),
 ]
 
 
