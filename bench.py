@@ -218,11 +218,13 @@ def run_gb300(args, ws, rank, lrank):
     ts.dt_vmax = np.float32(np.float32(18.0) / np.float32(max(vm)))
     stream = torch.cuda.ExternalStream(g.stream())
 
-    def step(fused=True):
+    def step(fused=True, after_x=None):
         dt, a_mid = ts.timestep()
         g.update_x(ts.dt_old, dt, ts.vz_max)
         g.buffer_grid()
         g.buffer_x()
+        if after_x:
+            after_x()
         if p.pp_on and fused:  # ext_pp_force + particle_mesh, PP beside the PM force chain
             pps, pms = g.pp_particle_mesh(a_mid, dt)
         elif p.pp_on:
@@ -305,10 +307,11 @@ def run_gb300(args, ws, rank, lrank):
     barrier(ws)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    # xp, pid, rhoc and vfield travel to the host beside PP+PM, vp after the kicks
     for _ in range(ke):
         g.upload(hin["xp"], hin["vp"], hin["pid"], hin["rhoc"], hin["vfield"])
-        step()
-        g.download(out=out)
+        step(after_x=lambda: g.download_begin(out))
+        g.download_finish()
     torch.cuda.synchronize()
     te = time.perf_counter() - t0
     te = allreduce_max(te, ws, dev)

@@ -44,6 +44,12 @@ static int alloc(cube_ctx* c, void** p, size_t bytes) {
 static void release(cube_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
+  if (c->stream_copy) {
+    cudaStreamSynchronize(c->stream_copy);
+    cudaStreamDestroy(c->stream_copy);
+    cudaEventDestroy(c->ev_copy_start);
+    cudaEventDestroy(c->ev_copy);
+  }
   cube_timers_free(c);
   if (c->owner) {  // meshes, kernels, plans, work area and stream belong to the owner
     c->rho_f = c->kern_f = c->kern_f_raw = c->rho_c = c->kern_c = nullptr;
@@ -276,6 +282,21 @@ extern "C" int cube_download_state(cube_ctx* c, int64_t* nplocal, void* xp, void
   return cube_state_out(c, nplocal, xp, vp, pid, rhoc, vfield);
 }
 
+extern "C" int cube_download_begin(cube_ctx* c, int64_t* nplocal, void* xp, int32_t* pid, int32_t* rhoc,
+                                   float* vfield) {
+  if (!c) return CUBE_ERR_ARG;
+  if (!c->have_state) return cube_fail(c, CUBE_ERR_STATE, "no state uploaded");
+  CUBE_CUDA(c, cudaSetDevice(c->device));
+  return cube_state_out_begin(c, nplocal, xp, pid, rhoc, vfield);
+}
+
+extern "C" int cube_download_finish(cube_ctx* c, void* vp) {
+  if (!c) return CUBE_ERR_ARG;
+  if (!c->have_state) return cube_fail(c, CUBE_ERR_STATE, "no state uploaded");
+  CUBE_CUDA(c, cudaSetDevice(c->device));
+  return cube_state_out_finish(c, vp);
+}
+
 extern "C" int cube_set_sigma(cube_ctx* c, float s, float sn) {
   if (!c) return CUBE_ERR_ARG;
   c->sigma_vi = s;
@@ -299,6 +320,7 @@ static int check_ready(cube_ctx* c) {
 
 extern "C" int cube_update_x(cube_ctx* c, float dt_old, float dt, float vz_max, cube_stats* st) {
   int r = check_ready(c);
+  if (!r) r = cube_copy_join(c);
   if (r) return r;
   return cube_update_x_impl(c, dt_old, dt, vz_max, st);
 }

@@ -159,6 +159,12 @@ struct cube_ctx {
   cudaEvent_t ev_fork = nullptr, ev_pp = nullptr;
   DevStats* dstats_pp = nullptr;
   DevStats* hstats_pp = nullptr;  // pinned
+  // device-to-host copy of xp, pid, rhoc and vfield beside the force half of
+  // the step (cube_download_begin / cube_download_finish); calls that change
+  // the state are ordered after it on the device (cube_copy_join)
+  cudaStream_t stream_copy = nullptr;
+  cudaEvent_t ev_copy_start = nullptr, ev_copy = nullptr;
+  bool copy_pending = false;
   // per-phase timers (null when disabled)
   struct CubeTimers* timers = nullptr;
   // stats
@@ -658,6 +664,10 @@ double cube_ic_vfactor(double a, double om, double ol);
 int cube_state_in(cube_ctx* c, int64_t np, const void* xp, const void* vp, const int32_t* pid,
                   const int32_t* rhoc, const float* vfield);
 int cube_state_out(cube_ctx* c, int64_t* np, void* xp, void* vp, int32_t* pid, int32_t* rhoc, float* vfield);
+// orders the context stream after a pending cube_download_begin copy
+int cube_copy_join(cube_ctx* c);
+int cube_state_out_begin(cube_ctx* c, int64_t* np, void* xp, int32_t* pid, int32_t* rhoc, float* vfield);
+int cube_state_out_finish(cube_ctx* c, void* vp);
 int cube_stats_fetch(cube_ctx* c);
 
 // phase timers (cube_timing.cu); no-ops unless timing is enabled

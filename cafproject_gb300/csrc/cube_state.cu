@@ -118,6 +118,8 @@ int cube_state_in(cube_ctx* c, int64_t np, const void* xp, const void* vp, const
                   const float* vfield) {
   int k = c->cur;
   const cube_params& p = c->p;
+  int r = cube_copy_join(c);
+  if (r) return r;
   // the counts are checked on the device, after the copies (a failed check
   // leaves the context without a state)
   c->have_state = false;
@@ -129,7 +131,7 @@ int cube_state_in(cube_ctx* c, int64_t np, const void* xp, const void* vp, const
     CUBE_CUDA(c, cudaMemsetAsync(c->pid[k], 0, (size_t)4 * np, c->stream));
   CUBE_CUDA(c, cudaMemcpyAsync(c->rhoc[k], rhoc, (size_t)4 * c->ncells, cudaMemcpyHostToDevice, c->stream));
   CUBE_CUDA(c, cudaMemcpyAsync(c->vfield[k], vfield, (size_t)12 * c->ncells, cudaMemcpyHostToDevice, c->stream));
-  int r = cube_scan_counts(c, c->rhoc[k], c->cstart[k], c->ncells);
+  r = cube_scan_counts(c, c->rhoc[k], c->cstart[k], c->ncells);
   if (r) return r;
   CUBE_CUDA(c, cudaMemsetAsync(&c->dstats->flags, 0, sizeof(int), c->stream));
   k_fill_pcell<<<cube_grid(c->ncells, 256), 256, 0, c->stream>>>(c->rhoc[k], c->cstart[k], c->ncells, c->pcell[k],
@@ -160,6 +162,46 @@ int cube_state_out(cube_ctx* c, int64_t* np, void* xp, void* vp, int32_t* pid, i
   if (vfield)
     CUBE_CUDA(c, cudaMemcpyAsync(vfield, c->vfield[k], (size_t)12 * c->ncells, cudaMemcpyDeviceToHost, c->stream));
   CUBE_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CUBE_OK;
+}
+
+int cube_copy_join(cube_ctx* c) {
+  if (c->copy_pending) CUBE_CUDA(c, cudaStreamWaitEvent(c->stream, c->ev_copy, 0));
+  return CUBE_OK;
+}
+
+// The force half of a step (PP and PM) reads xp, pid, rhoc and vfield and
+// writes only vp, so those four can travel to the host while it runs: the
+// copies go on their own stream after an event on the context stream.
+int cube_state_out_begin(cube_ctx* c, int64_t* np, void* xp, int32_t* pid, int32_t* rhoc, float* vfield) {
+  int k = c->cur;
+  const cube_params& p = c->p;
+  if (!c->stream_copy) {
+    CUBE_CUDA(c, cudaStreamCreateWithFlags(&c->stream_copy, cudaStreamNonBlocking));
+    CUBE_CUDA(c, cudaEventCreateWithFlags(&c->ev_copy_start, cudaEventDisableTiming));
+    CUBE_CUDA(c, cudaEventCreateWithFlags(&c->ev_copy, cudaEventDisableTiming));
+  }
+  if (np) *np = c->np;
+  cudaStream_t s = c->stream_copy;
+  CUBE_CUDA(c, cudaEventRecord(c->ev_copy_start, c->stream));
+  CUBE_CUDA(c, cudaStreamWaitEvent(s, c->ev_copy_start, 0));
+  if (xp) CUBE_CUDA(c, cudaMemcpyAsync(xp, c->xp[k], (size_t)3 * c->np * p.izipx, cudaMemcpyDeviceToHost, s));
+  if (pid) CUBE_CUDA(c, cudaMemcpyAsync(pid, c->pid[k], (size_t)4 * c->np, cudaMemcpyDeviceToHost, s));
+  if (rhoc) CUBE_CUDA(c, cudaMemcpyAsync(rhoc, c->rhoc[k], (size_t)4 * c->ncells, cudaMemcpyDeviceToHost, s));
+  if (vfield) CUBE_CUDA(c, cudaMemcpyAsync(vfield, c->vfield[k], (size_t)12 * c->ncells, cudaMemcpyDeviceToHost, s));
+  CUBE_CUDA(c, cudaEventRecord(c->ev_copy, s));
+  c->copy_pending = true;
+  return CUBE_OK;
+}
+
+int cube_state_out_finish(cube_ctx* c, void* vp) {
+  if (vp)
+    CUBE_CUDA(c, cudaMemcpyAsync(vp, c->vp[c->cur], (size_t)3 * c->np * c->p.izipv, cudaMemcpyDeviceToHost, c->stream));
+  CUBE_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (c->copy_pending) {
+    CUBE_CUDA(c, cudaEventSynchronize(c->ev_copy));
+    c->copy_pending = false;
+  }
   return CUBE_OK;
 }
 

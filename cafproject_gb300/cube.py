@@ -26,6 +26,7 @@ STATUS = {0: "CUBE_OK", 1: "CUBE_ERR_ARG", 2: "CUBE_ERR_CUDA", 3: "CUBE_ERR_TILE
 
 # every symbol include/cube_gpu.h declares
 EXPORTS = ["cube_create", "cube_destroy", "cube_last_error", "cube_upload_state", "cube_download_state",
+           "cube_download_begin", "cube_download_finish",
            "cube_set_sigma", "cube_get_sigma", "cube_update_x", "cube_buffer_grid", "cube_buffer_x",
            "cube_buffer_v", "cube_pp_force", "cube_particle_mesh", "cube_pp_particle_mesh", "cube_pm_fine_density", "cube_pm_coarse_density",
            "cube_pm_fine_forces", "cube_pm_fine_kick",
@@ -119,6 +120,8 @@ def load_library(path=None):
     L.cube_last_error.restype = ctypes.c_char_p
     L.cube_upload_state.argtypes = [P, I64, P, P, P, P, P]
     L.cube_download_state.argtypes = [P, ctypes.POINTER(I64), P, P, P, P, P]
+    L.cube_download_begin.argtypes = [P, ctypes.POINTER(I64), P, P, P, P]
+    L.cube_download_finish.argtypes = [P, P]
     L.cube_set_sigma.argtypes = [P, F, F]
     L.cube_get_sigma.argtypes = [P, ctypes.POINTER(F), ctypes.POINTER(F)]
     L.cube_update_x.argtypes = [P, F, F, F, P]
@@ -249,6 +252,22 @@ class CubeGPU:
         self._check(self.L.cube_download_state(self.h, ctypes.byref(nn), _ptr(xp), _ptr(vp), _ptr(pid), _ptr(rhoc),
                                                _ptr(vf)))
         return dict(xp=xp, vp=vp, pid=pid, rhoc=rhoc, vfield=vf)
+
+    def download_begin(self, out):
+        """Start copying xp, pid, rhoc and vfield into the (pinned) arrays of
+        ``out`` beside the rest of the step; ``download_finish`` adds vp and
+        waits.  Call it after update_x and the buffer calls."""
+        n = self.nplocal()
+        nn = ctypes.c_int64()
+        self._pending = (n, out)
+        self._check(self.L.cube_download_begin(self.h, ctypes.byref(nn), _ptr(out["xp"][:n]), _ptr(out["pid"][:n]),
+                                               _ptr(out["rhoc"]), _ptr(out["vfield"])))
+
+    def download_finish(self):
+        n, out = self._pending
+        self._pending = None
+        self._check(self.L.cube_download_finish(self.h, _ptr(out["vp"][:n])))
+        return dict(xp=out["xp"][:n], vp=out["vp"][:n], pid=out["pid"][:n], rhoc=out["rhoc"], vfield=out["vfield"])
 
     def set_sigma(self, sigma_vi, sigma_vi_new=None):
         sn = sigma_vi if sigma_vi_new is None else sigma_vi_new

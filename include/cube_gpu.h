@@ -158,6 +158,18 @@ int cube_upload_state(cube_ctx* ctx, int64_t nplocal, const void* xp, const void
 int cube_download_state(cube_ctx* ctx, int64_t* nplocal, void* xp, void* vp, int32_t* pid, int32_t* rhoc,
                         float* vfield);
 
+/* The same download in two halves, so that the host copy overlaps the force
+   half of the step.  After cube_update_x and the buffer calls the arrays xp,
+   pid, rhoc and vfield are final for the step (PP and PM read them and write
+   only vp): cube_download_begin starts copying them on a side stream and
+   returns; cube_download_finish copies vp (may be NULL) and returns when all
+   of them are in host memory.  Host memory should be pinned for the copies
+   to run asynchronously; any of the four may be NULL.  A call that changes
+   the state before the finish (cube_update_x, an upload, a checkpoint read,
+   initial conditions) is ordered after the copies on the device. */
+int cube_download_begin(cube_ctx* ctx, int64_t* nplocal, void* xp, int32_t* pid, int32_t* rhoc, float* vfield);
+int cube_download_finish(cube_ctx* ctx, void* vp);
+
 /* Checkpoint files in the reference's format (checkpoint.f90:10-50; read back
    as particle_initialization.f90:34-64 does): in dir, <z>_info_<image>.bin,
    _xp_, _vp_, _np_, _vc_ and (with particle ids) _id_, <z> = z printed as

@@ -69,3 +69,39 @@ def test_upload_rejects_inconsistent_counts():
         assert np.array_equal(g.download()["rhoc"], st["rhoc"])
     finally:
         g.close()
+
+
+def test_split_download_matches_download():
+    # xp, pid, rhoc and vfield copied beside PP+PM (cube_download_begin right
+    # after update_x), vp after the kicks: the same arrays as a download at the
+    # end of the step; an update_x issued before the finish is ordered after
+    # the copies, so the arrays hold the state of the step that began them
+    import torch
+    from cafproject_gb300 import cube as C
+    from cafproject_gb300 import params as P
+    from cafproject_gb300 import synth
+    p = P.small(nc=24, nnt=2, pp_on=True)
+    st = synth.random_state(p, mean_per_cell=8, seed=12, vsig=0.03, clump=4)
+    g = C.CubeGPU(p)
+    try:
+        g.upload(st["xp"], st["vp"], st["pid"], st["rhoc"], st["vfield"])
+        s = np.float32(st["sigma_vi"])
+        g.set_sigma(s, s)
+        out = {k: torch.from_numpy(np.empty_like(st[k])).pin_memory().numpy()
+               for k in ("xp", "vp", "pid", "rhoc", "vfield")}
+        for _ in range(2):
+            g.update_x(np.float32(20.0), np.float32(30.0), st["vz_max"])
+            g.download_begin(out)
+            g.pp_particle_mesh(np.float32(0.4), np.float32(0.02))
+            got = {k: v.copy() for k, v in g.download_finish().items()}
+            ref = g.download()
+            for key in ("xp", "vp", "pid", "rhoc", "vfield"):
+                assert np.array_equal(got[key], ref[key]), key
+        ref = g.download()
+        g.download_begin(out)
+        g.update_x(np.float32(20.0), np.float32(30.0), st["vz_max"])
+        got = g.download_finish()
+        for key in ("xp", "pid", "rhoc", "vfield"):
+            assert np.array_equal(got[key], ref[key]), key
+    finally:
+        g.close()
