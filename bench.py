@@ -307,9 +307,10 @@ def run_gb300(args, ws, rank, lrank):
     barrier(ws)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    # xp, pid, rhoc and vfield travel to the host beside PP+PM, vp after the kicks
+    # pid travels to the device beside the re-sort's first passes; xp, pid,
+    # rhoc and vfield to the host beside PP+PM, vp behind the coarse kick
     for _ in range(ke):
-        g.upload(hin["xp"], hin["vp"], hin["pid"], hin["rhoc"], hin["vfield"])
+        g.upload_begin(hin["xp"], hin["vp"], hin["pid"], hin["rhoc"], hin["vfield"])
         step(after_x=lambda: g.download_begin(out))
         g.download_finish()
     torch.cuda.synchronize()

@@ -49,6 +49,7 @@ static void release(cube_ctx* c) {
     cudaStreamDestroy(c->stream_copy);
     cudaEventDestroy(c->ev_copy_start);
     cudaEventDestroy(c->ev_copy);
+    cudaEventDestroy(c->ev_pid);
   }
   cube_timers_free(c);
   if (c->owner) {  // meshes, kernels, plans, work area and stream belong to the owner
@@ -282,19 +283,27 @@ extern "C" int cube_download_state(cube_ctx* c, int64_t* nplocal, void* xp, void
   return cube_state_out(c, nplocal, xp, vp, pid, rhoc, vfield);
 }
 
-extern "C" int cube_download_begin(cube_ctx* c, int64_t* nplocal, void* xp, int32_t* pid, int32_t* rhoc,
+extern "C" int cube_upload_begin(cube_ctx* c, int64_t nplocal, const void* xp, const void* vp, const int32_t* pid,
+                                 const int32_t* rhoc, const float* vfield) {
+  if (!c || !xp || !vp || !rhoc || !vfield || nplocal < 0) return CUBE_ERR_ARG;
+  if (nplocal > c->p.np_max) return cube_fail(c, CUBE_ERR_IMAGE_OVERFLOW, "nplocal exceeds np_max");
+  CUBE_CUDA(c, cudaSetDevice(c->device));
+  return cube_state_in(c, nplocal, xp, vp, pid, rhoc, vfield, true);
+}
+
+extern "C" int cube_download_begin(cube_ctx* c, int64_t* nplocal, void* xp, void* vp, int32_t* pid, int32_t* rhoc,
                                    float* vfield) {
   if (!c) return CUBE_ERR_ARG;
   if (!c->have_state) return cube_fail(c, CUBE_ERR_STATE, "no state uploaded");
+  if (c->copy_pending) return cube_fail(c, CUBE_ERR_STATE, "a download is already in flight");
   CUBE_CUDA(c, cudaSetDevice(c->device));
-  return cube_state_out_begin(c, nplocal, xp, pid, rhoc, vfield);
+  return cube_state_out_begin(c, nplocal, xp, vp, pid, rhoc, vfield);
 }
 
-extern "C" int cube_download_finish(cube_ctx* c, void* vp) {
+extern "C" int cube_download_finish(cube_ctx* c) {
   if (!c) return CUBE_ERR_ARG;
-  if (!c->have_state) return cube_fail(c, CUBE_ERR_STATE, "no state uploaded");
   CUBE_CUDA(c, cudaSetDevice(c->device));
-  return cube_state_out_finish(c, vp);
+  return cube_state_out_finish(c);
 }
 
 extern "C" int cube_set_sigma(cube_ctx* c, float s, float sn) {
@@ -476,6 +485,7 @@ extern "C" int cube_synchronize(cube_ctx* c) {
   if (!c) return CUBE_ERR_ARG;
   CUBE_CUDA(c, cudaSetDevice(c->device));
   CUBE_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (c->stream_copy) CUBE_CUDA(c, cudaStreamSynchronize(c->stream_copy));
   return CUBE_OK;
 }
 

@@ -405,6 +405,11 @@ extern "C" int cube_batch_step(cube_batch* b, int nsteps) {
   if (b->steps_done + nsteps > b->nsteps) return bfail(b, CUBE_ERR_ARG, "steps beyond the schedule");
   if (nsteps == 0) return CUBE_OK;
   if (b->hhist.size() != (size_t)b->nsteps * b->nbox) b->hhist.assign((size_t)b->nsteps * b->nbox, cube_batch_stats{});
+  for (cube_ctx* c : b->box)  // host copies of a box's state started through its context end first
+    if (c->stream_copy) {
+      BCUDA(b, cudaStreamSynchronize(c->stream_copy));
+      c->copy_pending = c->pid_pending = false;
+    }
   return b->mode == CUBE_BATCH_GRAPH ? graph_steps(b, nsteps) : serial_steps(b, nsteps);
 }
 

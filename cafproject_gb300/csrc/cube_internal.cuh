@@ -159,12 +159,16 @@ struct cube_ctx {
   cudaEvent_t ev_fork = nullptr, ev_pp = nullptr;
   DevStats* dstats_pp = nullptr;
   DevStats* hstats_pp = nullptr;  // pinned
-  // device-to-host copy of xp, pid, rhoc and vfield beside the force half of
-  // the step (cube_download_begin / cube_download_finish); calls that change
-  // the state are ordered after it on the device (cube_copy_join)
+  // host copies beside the step on their own stream: a download of xp, pid,
+  // rhoc and vfield beside PP and PM, of vp beside the coarse kick
+  // (cube_download_begin / _finish; calls that change the state are ordered
+  // after it on the device by cube_copy_join), and the upload of pid beside
+  // the re-sort up to the scatter (cube_upload_begin; cube_pid_join)
   cudaStream_t stream_copy = nullptr;
-  cudaEvent_t ev_copy_start = nullptr, ev_copy = nullptr;
+  cudaEvent_t ev_copy_start = nullptr, ev_copy = nullptr, ev_pid = nullptr;
   bool copy_pending = false;
+  void* vp_host = nullptr;  // vp destination of a pending download
+  bool pid_pending = false;
   // per-phase timers (null when disabled)
   struct CubeTimers* timers = nullptr;
   // stats
@@ -662,12 +666,15 @@ int cube_ic_filter(cube_ctx* c, const cube_cosmology& cs, double a, int n, cufft
 void cube_ic_noise(float* r, int n, int pitch, uint32_t seed, cudaStream_t s);
 double cube_ic_vfactor(double a, double om, double ol);
 int cube_state_in(cube_ctx* c, int64_t np, const void* xp, const void* vp, const int32_t* pid,
-                  const int32_t* rhoc, const float* vfield);
+                  const int32_t* rhoc, const float* vfield, bool defer_pid = false);
 int cube_state_out(cube_ctx* c, int64_t* np, void* xp, void* vp, int32_t* pid, int32_t* rhoc, float* vfield);
 // orders the context stream after a pending cube_download_begin copy
 int cube_copy_join(cube_ctx* c);
-int cube_state_out_begin(cube_ctx* c, int64_t* np, void* xp, int32_t* pid, int32_t* rhoc, float* vfield);
-int cube_state_out_finish(cube_ctx* c, void* vp);
+// orders the context stream after a deferred pid upload
+int cube_pid_join(cube_ctx* c);
+int cube_copy_stream(cube_ctx* c);
+int cube_state_out_begin(cube_ctx* c, int64_t* np, void* xp, void* vp, int32_t* pid, int32_t* rhoc, float* vfield);
+int cube_state_out_finish(cube_ctx* c);
 int cube_stats_fetch(cube_ctx* c);
 
 // phase timers (cube_timing.cu); no-ops unless timing is enabled

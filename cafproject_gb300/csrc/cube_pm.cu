@@ -774,7 +774,32 @@ int cube_coarse_kick_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st, bo
   k.vmax_only = 0;
   k.exact_only = c->opt_exact_kicks;
   cube_phase_begin(c, PH_C_KICK);
-  if (pre)
+  if (c->vp_host && !c->graph_mode) {
+    // a download is waiting for vp: kick in four pieces of particles, each
+    // piece's codes going to the host while the next is kicked
+    const size_t bx = 3 * (size_t)c->p.izipx, bv = 3 * (size_t)c->p.izipv;
+    for (int i = 0; i < 4; i++) {
+      const int64_t p0 = c->np * i / 4, p1 = c->np * (i + 1) / 4;
+      if (p1 <= p0) continue;
+      KickArgs kp = k;
+      kp.np = p1 - p0;
+      kp.xp = (const char*)k.xp + bx * p0;
+      kp.vp_in = (const char*)k.vp_in + bv * p0;
+      kp.vp_out = (char*)k.vp_out + bv * p0;
+      kp.pcell = k.pcell + p0;
+      if (pre)
+        k_kick<false, true><<<cube_grid(kp.np, 256), 256, 0, c->stream>>>(kp);
+      else
+        k_kick<false, false><<<cube_grid(kp.np, 256), 256, 0, c->stream>>>(kp);
+      CUBE_CUDA(c, cudaEventRecord(c->ev_copy_start, c->stream));
+      CUBE_CUDA(c, cudaStreamWaitEvent(c->stream_copy, c->ev_copy_start, 0));
+      CUBE_CUDA(c, cudaMemcpyAsync((char*)c->vp_host + bv * p0, kp.vp_out, bv * (p1 - p0), cudaMemcpyDeviceToHost,
+                                   c->stream_copy));
+    }
+    CUBE_CUDA(c, cudaEventRecord(c->ev_copy, c->stream_copy));
+    c->copy_pending = true;
+    c->vp_host = nullptr;
+  } else if (pre)
     k_kick<false, true><<<cube_grid(c->np, 256), 256, 0, c->stream>>>(k);
   else
     k_kick<false, false><<<cube_grid(c->np, 256), 256, 0, c->stream>>>(k);

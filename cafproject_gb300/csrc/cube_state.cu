@@ -115,17 +115,27 @@ __global__ void k_fill_pcell(const int32_t* __restrict__ rhoc, const int64_t* __
 }
 
 int cube_state_in(cube_ctx* c, int64_t np, const void* xp, const void* vp, const int32_t* pid, const int32_t* rhoc,
-                  const float* vfield) {
+                  const float* vfield, bool defer_pid) {
   int k = c->cur;
   const cube_params& p = c->p;
   int r = cube_copy_join(c);
+  if (!r) r = cube_pid_join(c);
   if (r) return r;
   // the counts are checked on the device, after the copies (a failed check
   // leaves the context without a state)
   c->have_state = false;
+  if (pid && defer_pid) {  // the re-sort reads pid only in its scatter
+    if ((r = cube_copy_stream(c))) return r;
+    CUBE_CUDA(c, cudaEventRecord(c->ev_copy_start, c->stream));
+    CUBE_CUDA(c, cudaStreamWaitEvent(c->stream_copy, c->ev_copy_start, 0));
+    CUBE_CUDA(c, cudaMemcpyAsync(c->pid[k], pid, (size_t)4 * np, cudaMemcpyHostToDevice, c->stream_copy));
+    CUBE_CUDA(c, cudaEventRecord(c->ev_pid, c->stream_copy));
+    c->pid_pending = true;
+  }
   CUBE_CUDA(c, cudaMemcpyAsync(c->xp[k], xp, (size_t)3 * np * p.izipx, cudaMemcpyHostToDevice, c->stream));
   CUBE_CUDA(c, cudaMemcpyAsync(c->vp[k], vp, (size_t)3 * np * p.izipv, cudaMemcpyHostToDevice, c->stream));
-  if (pid)
+  if (pid && defer_pid) {
+  } else if (pid)
     CUBE_CUDA(c, cudaMemcpyAsync(c->pid[k], pid, (size_t)4 * np, cudaMemcpyHostToDevice, c->stream));
   else
     CUBE_CUDA(c, cudaMemsetAsync(c->pid[k], 0, (size_t)4 * np, c->stream));
@@ -154,6 +164,7 @@ int cube_state_in(cube_ctx* c, int64_t np, const void* xp, const void* vp, const
 int cube_state_out(cube_ctx* c, int64_t* np, void* xp, void* vp, int32_t* pid, int32_t* rhoc, float* vfield) {
   int k = c->cur;
   const cube_params& p = c->p;
+  if (int r = cube_pid_join(c)) return r;
   if (np) *np = c->np;
   if (xp) CUBE_CUDA(c, cudaMemcpyAsync(xp, c->xp[k], (size_t)3 * c->np * p.izipx, cudaMemcpyDeviceToHost, c->stream));
   if (vp) CUBE_CUDA(c, cudaMemcpyAsync(vp, c->vp[k], (size_t)3 * c->np * p.izipv, cudaMemcpyDeviceToHost, c->stream));
@@ -165,24 +176,39 @@ int cube_state_out(cube_ctx* c, int64_t* np, void* xp, void* vp, int32_t* pid, i
   return CUBE_OK;
 }
 
+int cube_copy_stream(cube_ctx* c) {
+  if (c->stream_copy) return CUBE_OK;
+  CUBE_CUDA(c, cudaStreamCreateWithFlags(&c->stream_copy, cudaStreamNonBlocking));
+  CUBE_CUDA(c, cudaEventCreateWithFlags(&c->ev_copy_start, cudaEventDisableTiming));
+  CUBE_CUDA(c, cudaEventCreateWithFlags(&c->ev_copy, cudaEventDisableTiming));
+  CUBE_CUDA(c, cudaEventCreateWithFlags(&c->ev_pid, cudaEventDisableTiming));
+  return CUBE_OK;
+}
+
 int cube_copy_join(cube_ctx* c) {
   if (c->copy_pending) CUBE_CUDA(c, cudaStreamWaitEvent(c->stream, c->ev_copy, 0));
   return CUBE_OK;
 }
 
+int cube_pid_join(cube_ctx* c) {
+  if (c->pid_pending) {
+    CUBE_CUDA(c, cudaStreamWaitEvent(c->stream, c->ev_pid, 0));
+    c->pid_pending = false;
+  }
+  return CUBE_OK;
+}
+
 // The force half of a step (PP and PM) reads xp, pid, rhoc and vfield and
 // writes only vp, so those four can travel to the host while it runs: the
-// copies go on their own stream after an event on the context stream.
-int cube_state_out_begin(cube_ctx* c, int64_t* np, void* xp, int32_t* pid, int32_t* rhoc, float* vfield) {
+// copies go on their own stream after an event on the context stream.  vp
+// follows the next coarse kick, piece by piece (cube_pm_coarse_kick), or the
+// finish when no kick comes first.
+int cube_state_out_begin(cube_ctx* c, int64_t* np, void* xp, void* vp, int32_t* pid, int32_t* rhoc, float* vfield) {
   int k = c->cur;
   const cube_params& p = c->p;
-  if (!c->stream_copy) {
-    CUBE_CUDA(c, cudaStreamCreateWithFlags(&c->stream_copy, cudaStreamNonBlocking));
-    CUBE_CUDA(c, cudaEventCreateWithFlags(&c->ev_copy_start, cudaEventDisableTiming));
-    CUBE_CUDA(c, cudaEventCreateWithFlags(&c->ev_copy, cudaEventDisableTiming));
-  }
+  if (int r = cube_copy_stream(c)) return r;
   if (np) *np = c->np;
-  cudaStream_t s = c->stream_copy;
+  cudaStream_t s = c->stream_copy;  // a deferred pid upload is earlier on this stream
   CUBE_CUDA(c, cudaEventRecord(c->ev_copy_start, c->stream));
   CUBE_CUDA(c, cudaStreamWaitEvent(s, c->ev_copy_start, 0));
   if (xp) CUBE_CUDA(c, cudaMemcpyAsync(xp, c->xp[k], (size_t)3 * c->np * p.izipx, cudaMemcpyDeviceToHost, s));
@@ -191,12 +217,16 @@ int cube_state_out_begin(cube_ctx* c, int64_t* np, void* xp, int32_t* pid, int32
   if (vfield) CUBE_CUDA(c, cudaMemcpyAsync(vfield, c->vfield[k], (size_t)12 * c->ncells, cudaMemcpyDeviceToHost, s));
   CUBE_CUDA(c, cudaEventRecord(c->ev_copy, s));
   c->copy_pending = true;
+  c->vp_host = vp;
   return CUBE_OK;
 }
 
-int cube_state_out_finish(cube_ctx* c, void* vp) {
-  if (vp)
-    CUBE_CUDA(c, cudaMemcpyAsync(vp, c->vp[c->cur], (size_t)3 * c->np * c->p.izipv, cudaMemcpyDeviceToHost, c->stream));
+int cube_state_out_finish(cube_ctx* c) {
+  if (c->vp_host) {
+    CUBE_CUDA(c, cudaMemcpyAsync(c->vp_host, c->vp[c->cur], (size_t)3 * c->np * c->p.izipv, cudaMemcpyDeviceToHost,
+                                 c->stream));
+    c->vp_host = nullptr;
+  }
   CUBE_CUDA(c, cudaStreamSynchronize(c->stream));
   if (c->copy_pending) {
     CUBE_CUDA(c, cudaEventSynchronize(c->ev_copy));

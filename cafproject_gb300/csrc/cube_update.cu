@@ -834,6 +834,8 @@ int cube_update_x_impl(cube_ctx* c, float dt_old, float dt, float vz_max, cube_s
     cube_phase_end(c, PH_UPD_PLACE);
     CUBE_CUDA(c, cudaGetLastError());
   }
+  r = cube_pid_join(c);  // a deferred pid upload lands before the scatter reads it
+  if (r) return r;
   cube_phase_begin(c, PH_UPD_SCATTER);
   k_scatter<<<cube_grid(c->np, B), B, 0, c->stream>>>(a);
   if (hs.ndup_list) k_scatter_xtra<<<cube_grid((int64_t)hs.ndup_list, B), B, 0, c->stream>>>(a);

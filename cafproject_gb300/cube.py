@@ -26,7 +26,7 @@ STATUS = {0: "CUBE_OK", 1: "CUBE_ERR_ARG", 2: "CUBE_ERR_CUDA", 3: "CUBE_ERR_TILE
 
 # every symbol include/cube_gpu.h declares
 EXPORTS = ["cube_create", "cube_destroy", "cube_last_error", "cube_upload_state", "cube_download_state",
-           "cube_download_begin", "cube_download_finish",
+           "cube_upload_begin", "cube_download_begin", "cube_download_finish",
            "cube_set_sigma", "cube_get_sigma", "cube_update_x", "cube_buffer_grid", "cube_buffer_x",
            "cube_buffer_v", "cube_pp_force", "cube_particle_mesh", "cube_pp_particle_mesh", "cube_pm_fine_density", "cube_pm_coarse_density",
            "cube_pm_fine_forces", "cube_pm_fine_kick",
@@ -120,8 +120,9 @@ def load_library(path=None):
     L.cube_last_error.restype = ctypes.c_char_p
     L.cube_upload_state.argtypes = [P, I64, P, P, P, P, P]
     L.cube_download_state.argtypes = [P, ctypes.POINTER(I64), P, P, P, P, P]
-    L.cube_download_begin.argtypes = [P, ctypes.POINTER(I64), P, P, P, P]
-    L.cube_download_finish.argtypes = [P, P]
+    L.cube_upload_begin.argtypes = L.cube_upload_state.argtypes
+    L.cube_download_begin.argtypes = [P, ctypes.POINTER(I64), P, P, P, P, P]
+    L.cube_download_finish.argtypes = [P]
     L.cube_set_sigma.argtypes = [P, F, F]
     L.cube_get_sigma.argtypes = [P, ctypes.POINTER(F), ctypes.POINTER(F)]
     L.cube_update_x.argtypes = [P, F, F, F, P]
@@ -253,20 +254,30 @@ class CubeGPU:
                                                _ptr(vf)))
         return dict(xp=xp, vp=vp, pid=pid, rhoc=rhoc, vfield=vf)
 
+    def upload_begin(self, xp, vp, pid, rhoc, vfield):
+        """``upload`` with pid copied beside the next update_x's first passes;
+        the arrays must be contiguous, of the state's dtypes, and pinned for
+        the overlap, and pid unchanged until that update_x returns."""
+        for a in (xp, vp, pid, rhoc, vfield):
+            assert a is None or a.flags.c_contiguous
+        self._check(self.L.cube_upload_begin(self.h, xp.shape[0], _ptr(xp), _ptr(vp), _ptr(pid), _ptr(rhoc),
+                                             _ptr(vfield)))
+
     def download_begin(self, out):
-        """Start copying xp, pid, rhoc and vfield into the (pinned) arrays of
-        ``out`` beside the rest of the step; ``download_finish`` adds vp and
-        waits.  Call it after update_x and the buffer calls."""
+        """Start the download into the (pinned) arrays of ``out``: xp, pid,
+        rhoc and vfield now, beside the rest of the step, vp behind the next
+        coarse kick.  Call it after update_x and the buffer calls;
+        ``download_finish`` waits."""
         n = self.nplocal()
         nn = ctypes.c_int64()
         self._pending = (n, out)
-        self._check(self.L.cube_download_begin(self.h, ctypes.byref(nn), _ptr(out["xp"][:n]), _ptr(out["pid"][:n]),
-                                               _ptr(out["rhoc"]), _ptr(out["vfield"])))
+        self._check(self.L.cube_download_begin(self.h, ctypes.byref(nn), _ptr(out["xp"][:n]), _ptr(out["vp"][:n]),
+                                               _ptr(out["pid"][:n]), _ptr(out["rhoc"]), _ptr(out["vfield"])))
 
     def download_finish(self):
         n, out = self._pending
         self._pending = None
-        self._check(self.L.cube_download_finish(self.h, _ptr(out["vp"][:n])))
+        self._check(self.L.cube_download_finish(self.h))
         return dict(xp=out["xp"][:n], vp=out["vp"][:n], pid=out["pid"][:n], rhoc=out["rhoc"], vfield=out["vfield"])
 
     def set_sigma(self, sigma_vi, sigma_vi_new=None):

@@ -158,17 +158,29 @@ int cube_upload_state(cube_ctx* ctx, int64_t nplocal, const void* xp, const void
 int cube_download_state(cube_ctx* ctx, int64_t* nplocal, void* xp, void* vp, int32_t* pid, int32_t* rhoc,
                         float* vfield);
 
-/* The same download in two halves, so that the host copy overlaps the force
-   half of the step.  After cube_update_x and the buffer calls the arrays xp,
-   pid, rhoc and vfield are final for the step (PP and PM read them and write
-   only vp): cube_download_begin starts copying them on a side stream and
-   returns; cube_download_finish copies vp (may be NULL) and returns when all
-   of them are in host memory.  Host memory should be pinned for the copies
-   to run asynchronously; any of the four may be NULL.  A call that changes
-   the state before the finish (cube_update_x, an upload, a checkpoint read,
-   initial conditions) is ordered after the copies on the device. */
-int cube_download_begin(cube_ctx* ctx, int64_t* nplocal, void* xp, int32_t* pid, int32_t* rhoc, float* vfield);
-int cube_download_finish(cube_ctx* ctx, void* vp);
+/* Upload and download overlapped with the step, for a driver that keeps the
+   state in host memory and moves it every step.  Host memory should be
+   page-locked for the copies to run asynchronously.
+
+   cube_upload_begin is cube_upload_state with pid copied on a side stream:
+   the re-sort reads pid only in its scatter, so the copy runs beside the
+   re-sort's first passes.  The host pid array must stay unchanged until the
+   next cube_update_x (or cube_synchronize) returns.
+
+   cube_download_begin, called after cube_update_x and the buffer calls,
+   starts copying xp, pid, rhoc and vfield, which are final for the step (PP
+   and PM read them and write only vp), on a side stream and returns.  vp is
+   copied behind the next coarse kick, piece by piece as the kick finishes
+   each quarter of the particles, or by cube_download_finish when no kick
+   comes first.  cube_download_finish returns when all of them are in host
+   memory.  Any array may be NULL.  A call that changes the state before the
+   finish (cube_update_x, an upload, a checkpoint read, initial conditions)
+   is ordered after the copies on the device. */
+int cube_upload_begin(cube_ctx* ctx, int64_t nplocal, const void* xp, const void* vp, const int32_t* pid,
+                      const int32_t* rhoc, const float* vfield);
+int cube_download_begin(cube_ctx* ctx, int64_t* nplocal, void* xp, void* vp, int32_t* pid, int32_t* rhoc,
+                        float* vfield);
+int cube_download_finish(cube_ctx* ctx);
 
 /* Checkpoint files in the reference's format (checkpoint.f90:10-50; read back
    as particle_initialization.f90:34-64 does): in dir, <z>_info_<image>.bin,

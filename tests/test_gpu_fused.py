@@ -73,9 +73,10 @@ def test_upload_rejects_inconsistent_counts():
 
 def test_split_download_matches_download():
     # xp, pid, rhoc and vfield copied beside PP+PM (cube_download_begin right
-    # after update_x), vp after the kicks: the same arrays as a download at the
-    # end of the step; an update_x issued before the finish is ordered after
-    # the copies, so the arrays hold the state of the step that began them
+    # after update_x), vp behind the coarse kick's pieces: the same arrays as a
+    # download at the end of the step; an update_x issued before the finish is
+    # ordered after the copies, so the arrays hold the state of the step that
+    # began them; with no kick before the finish, the finish copies vp
     import torch
     from cafproject_gb300 import cube as C
     from cafproject_gb300 import params as P
@@ -103,5 +104,37 @@ def test_split_download_matches_download():
         got = g.download_finish()
         for key in ("xp", "pid", "rhoc", "vfield"):
             assert np.array_equal(got[key], ref[key]), key
+        assert np.array_equal(got["vp"], g.download()["vp"])
     finally:
         g.close()
+
+
+def test_overlapped_upload_matches_upload():
+    # pid copied beside the re-sort's first passes (cube_upload_begin): the
+    # steps give bit for bit the state of a plain upload, and the host pid
+    # array may change once update_x has returned
+    import torch
+    from cafproject_gb300 import cube as C
+    from cafproject_gb300 import params as P
+    from cafproject_gb300 import synth
+    p = P.small(nc=24, nnt=2, pp_on=True)
+    st = synth.random_state(p, mean_per_cell=8, seed=13, vsig=0.03, clump=4)
+    outs = []
+    for overlap in (False, True):
+        g = C.CubeGPU(p)
+        try:
+            pin = {k: torch.from_numpy(np.ascontiguousarray(st[k])).pin_memory().numpy()
+                   for k in ("xp", "vp", "pid", "rhoc", "vfield")}
+            (g.upload_begin if overlap else g.upload)(pin["xp"], pin["vp"], pin["pid"], pin["rhoc"], pin["vfield"])
+            s = np.float32(st["sigma_vi"])
+            g.set_sigma(s, s)
+            for _ in range(2):
+                g.update_x(np.float32(20.0), np.float32(30.0), st["vz_max"])
+                pin["pid"][:] = -7
+                g.pp_particle_mesh(np.float32(0.4), np.float32(0.02))
+            outs.append(g.download())
+        finally:
+            g.close()
+    for key in ("xp", "vp", "pid", "rhoc", "vfield"):
+        assert np.array_equal(outs[0][key], outs[1][key]), key
+    assert (outs[1]["pid"] != -7).all()
