@@ -68,6 +68,11 @@ static void release(cube_ctx* c) {
                   c->cufft_work};
   for (void* b : bufs)
     if (b) cudaFree(b);
+  for (int i = 0; i < 2; i++) {
+    if (c->skey[i]) cudaFree(c->skey[i]);
+    if (c->sval[i]) cudaFree(c->sval[i]);
+  }
+  if (c->sort_tmp) cudaFree(c->sort_tmp);
   if (c->hstats) cudaFreeHost(c->hstats);
   if (c->hstats_pp) cudaFreeHost(c->hstats_pp);
   if (c->dstats_pp) cudaFree(c->dstats_pp);
@@ -465,7 +470,8 @@ extern "C" int cube_set_option(cube_ctx* c, int option, int64_t value) {
       c->opt_exact_kicks = value ? 1 : 0;
       return CUBE_OK;
     case CUBE_OPT_RANK_WALK:
-      c->opt_rank_walk = value ? 1 : 0;
+      if (value < 0 || value > 2) return cube_fail(c, CUBE_ERR_ARG, "rank path is 0, 1 or 2");
+      c->opt_rank_walk = (int)value;
       return CUBE_OK;
     case CUBE_OPT_PP_LEVEL:
       if (value < 0 || value > 4) return cube_fail(c, CUBE_ERR_ARG, "PP level must be 0 to 4");

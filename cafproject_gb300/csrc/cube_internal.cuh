@@ -109,6 +109,12 @@ struct cube_ctx {
   int32_t* vdense = nullptr;    // destination cells with many particles (vfield_new by a warp each)
   uint32_t* rank = nullptr;     // rank of the primary copy in its destination
   int4* xtra = nullptr;         // extra copies: (particle, dest cell, rank, -)
+  // general rank path: sort keys and entries (two buffers each, np_max +
+  // xtra_cap) and the sort's scratch, allocated on first use
+  uint64_t* skey[2] = {nullptr, nullptr};
+  int32_t* sval[2] = {nullptr, nullptr};
+  void* sort_tmp = nullptr;
+  size_t sort_tmp_bytes = 0;
   int64_t xtra_cap = 0;
   void* scan_tmp = nullptr;
   size_t scan_tmp_bytes = 0;
@@ -132,7 +138,7 @@ struct cube_ctx {
   StepOut* sout = nullptr;  // device (owned by the batch)
   unsigned long long kick_exact_lanes = 0;
   int opt_exact_kicks = 0;
-  int opt_rank_walk = 0;   // force the general visit-order rank walker
+  int opt_rank_walk = 0;   // ranks: 0 counting path (sort when it does not apply), 1 walker, 2 sort
   int rank_walked = 0;     // the last update used the walker
   int opt_pp_level = 0;  // first PP level (0-4)
   int opt_dep_fine = 0, opt_dep_coarse = 0;  // deposit brick shapes (0-3)
@@ -670,6 +676,9 @@ int cube_state_in(cube_ctx* c, int64_t np, const void* xp, const void* vp, const
 int cube_state_out(cube_ctx* c, int64_t* np, void* xp, void* vp, int32_t* pid, int32_t* rhoc, float* vfield);
 // orders the context stream after a pending cube_download_begin copy
 int cube_copy_join(cube_ctx* c);
+// stable radix sort of n (key, entry) pairs over key bits [begin_bit, end_bit)
+// from skey[0]/sval[0]; *keys, *vals receive the buffers holding the result
+int cube_sort_pairs(cube_ctx* c, int64_t n, int begin_bit, int end_bit, uint64_t** keys, int32_t** vals);
 // orders the context stream after a deferred pid upload
 int cube_pid_join(cube_ctx* c);
 int cube_copy_stream(cube_ctx* c);

@@ -566,6 +566,99 @@ __device__ __forceinline__ void write_particle(const UpdArgs& a, int64_t p, int3
   a.pcell_new[idx] = D;
 }
 
+// U2, general path: the rank of a landing (a particle's primary destination,
+// or an extra copy's) is its position among the landings in its destination
+// cell ordered by the reference's visit order, and the new disjoint order is
+// the cells in storage order with their particles by rank.  So one sort of
+// all landings by
+//   (destination cell, layer of the source's z in the destination tile's
+//    frame, source offsets z, y, x from the destination, index in the
+//    source cell)
+// yields the new order itself: position = cstart_new[D] + rank.  Offsets fit
+// 5 bits (|offset| <= 2 ncb) and the layer 5 bits (nlayer <= 31); the index
+// in the source cell takes the bits left below the destination's.  Without
+// extra copies the sort skips the index bits: the radix sort is stable and
+// the primaries enter in storage order, which within a source cell is the
+// index order.
+constexpr int SORT_VISIT_BITS = 20;
+__host__ __device__ inline int sort_dest_bits(int64_t ncells) {
+  int b = 1;
+  while (((int64_t)1 << b) < ncells) b++;
+  return b;
+}
+
+__global__ void k_sort_keys(UpdArgs a, uint64_t* __restrict__ keys, int32_t* __restrict__ vals, int64_t nx, int lb) {
+  const Geo& g = a.g;
+  const int64_t n = a.np + nx;
+  const uint64_t lmax = (uint64_t)1 << lb;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t p;
+    int32_t D;
+    int fr;
+    if (i < a.np) {
+      p = i;
+      D = a.dest[p];
+      fr = a.dframe[p];
+    } else {
+      const int4 x = a.xtra[i - a.np];
+      p = x.x;
+      D = x.y;
+      fr = x.w;
+    }
+    vals[i] = (int32_t)i;
+    if (D < 0 || (int64_t)D >= a.ncells) {  // lost: after every landing
+      keys[i] = ~0ull;
+      continue;
+    }
+    const int64_t S = a.pcell[p];
+    const uint64_t l = (uint64_t)(p - a.cstart[S]);
+    int sg[3], dg[3];
+    cell_coords(g, S, sg[0], sg[1], sg[2]);
+    cell_coords(g, D, dg[0], dg[1], dg[2]);
+    uint32_t visit = 0;
+    int layer = 0;
+    bool bad = l >= lmax;
+    for (int d = 2; d >= 0; d--) {
+      int T, L, TD, DL;
+      tile_local(g, sg[d], T, L);
+      tile_local(g, dg[d], TD, DL);
+      const int digit = d == 2 ? fr / 9 : (d == 1 ? (fr / 3) % 3 : fr % 3);
+      const int Ls = L + (digit - 1) * g.nt;  // the source in the destination tile's frame
+      const int off = Ls - DL;
+      bad = bad || off < -15 || off > 15;
+      if (d == 2) layer = (Ls + g.ncb - 1) % nlay(a);
+      visit = (visit << 5) | (uint32_t)(off + 15);
+    }
+    bad = bad || layer > 31;
+    if (bad) atomicOr(&a.st->flags, 64);  // does not fit the key: the walker takes over
+    visit |= (uint32_t)layer << 15;
+    keys[i] = ((uint64_t)D << (SORT_VISIT_BITS + lb)) | ((uint64_t)visit << lb) | (l & (lmax - 1));
+    atomicAdd(&a.cnt_new[D], 1);
+  }
+}
+
+// ranks, extra copies' ranks and the inverse permutation from the sorted landings
+__global__ void k_sort_place(UpdArgs a, const uint64_t* __restrict__ keys, const int32_t* __restrict__ vals,
+                             int64_t n_new, int shift) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_new; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t D = (int64_t)(keys[i] >> shift);
+    const int64_t id = vals[i];
+    if (D >= a.ncells) {
+      atomicOr(&a.st->flags, 2);
+      continue;
+    }
+    const uint32_t r = (uint32_t)(i - a.cstart_new[D]);
+    int64_t p = id;
+    if (id < a.np) {
+      a.rank[p] = r;
+    } else {
+      p = a.xtra[id - a.np].x;
+      a.xtra[id - a.np].z = (int)r;
+    }
+    a.perm[i] = (int32_t)p;
+  }
+}
+
 // U3: scatter every primary copy to its place in the new disjoint order.
 __global__ void k_scatter(UpdArgs a) {
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -786,49 +879,77 @@ int cube_update_x_impl(cube_ctx* c, float dt_old, float dt, float vz_max, cube_s
   cube_phase_begin(c, PH_UPD_DEST);
   k_dest<<<cube_grid(c->np, B), B, 0, c->stream>>>(a);
   cube_phase_end(c, PH_UPD_DEST);
-  // ranks: the counting path (kernels check their own eligibility on the
-  // device and flag it), else the general visit-order walker
-  bool walker = c->opt_rank_walk != 0;
-  cube_phase_begin(c, PH_UPD_RANK);
-  if (walker) {
-    k_rank<<<cube_grid(c->ncells, 128, 32), 128, 0, c->stream>>>(a);
-  } else {
-    CUBE_CUDA(c, cudaMemsetAsync(c->offc, 0, sizeof(uint16_t) * NOFF * (size_t)c->ncells, c->stream));
-    k_rank_local<<<cube_grid(c->np, 256), 256, 0, c->stream>>>(a);
-    k_rank_base<<<cube_grid(c->ncells, 256), 256, 0, c->stream>>>(a);
-  }
-  cube_phase_end(c, PH_UPD_RANK);
-  CUBE_CUDA(c, cudaGetLastError());
-  cube_phase_begin(c, PH_UPD_SCAN);
-  r = cube_scan_counts(c, c->rhoc[kn], c->cstart[kn], c->ncells);
-  cube_phase_end(c, PH_UPD_SCAN);
-  if (r) return r;
+  // ranks: the counting path (its kernels check their own eligibility on the
+  // device and flag it), else the sort of all landings; the visit-order
+  // walker on request, or when a landing does not fit the sort key
+  enum { COUNT = 0, WALK = 1, SORT = 2 };
+  int path = c->opt_rank_walk;
   int64_t np_new = 0;
-  CUBE_CUDA(c, cudaMemcpyAsync(&np_new, c->cstart[kn] + c->ncells, 8, cudaMemcpyDeviceToHost, c->stream));
-  r = cube_stats_fetch(c);
-  if (r) return r;
-  if (c->hstats->flags & 1) return cube_fail(c, CUBE_ERR_DISPLACEMENT, "a particle left the double-buffer tile");
-  if (!walker && (c->hstats->flags & 12)) {  // counting path not applicable: walk
-    walker = true;
-    CUBE_CUDA(c, cudaMemsetAsync(&c->dstats->flags, 0, sizeof(int), c->stream));
+  auto walk = [&]() -> int {
     cube_phase_begin(c, PH_UPD_RANK);
     k_rank<<<cube_grid(c->ncells, 128, 32), 128, 0, c->stream>>>(a);
     cube_phase_end(c, PH_UPD_RANK);
     CUBE_CUDA(c, cudaGetLastError());
-    r = cube_scan_counts(c, c->rhoc[kn], c->cstart[kn], c->ncells);
-    if (r) return r;
+    return CUBE_OK;
+  };
+  auto scan = [&]() -> int {
+    cube_phase_begin(c, PH_UPD_SCAN);
+    int rr = cube_scan_counts(c, c->rhoc[kn], c->cstart[kn], c->ncells);
+    cube_phase_end(c, PH_UPD_SCAN);
+    if (rr) return rr;
     CUBE_CUDA(c, cudaMemcpyAsync(&np_new, c->cstart[kn] + c->ncells, 8, cudaMemcpyDeviceToHost, c->stream));
-    r = cube_stats_fetch(c);
-    if (r) return r;
+    return cube_stats_fetch(c);
+  };
+  if (path == COUNT) {
+    cube_phase_begin(c, PH_UPD_RANK);
+    CUBE_CUDA(c, cudaMemsetAsync(c->offc, 0, sizeof(uint16_t) * NOFF * (size_t)c->ncells, c->stream));
+    k_rank_local<<<cube_grid(c->np, 256), 256, 0, c->stream>>>(a);
+    k_rank_base<<<cube_grid(c->ncells, 256), 256, 0, c->stream>>>(a);
+    cube_phase_end(c, PH_UPD_RANK);
+    CUBE_CUDA(c, cudaGetLastError());
+    if ((r = scan())) return r;
+    if (c->hstats->flags & 12) path = SORT;  // counting path not applicable
+  } else if (path == WALK) {
+    if ((r = walk()) || (r = scan())) return r;
+  } else {
+    if ((r = cube_stats_fetch(c))) return r;
   }
-  c->rank_walked = walker ? 1 : 0;
+  if (c->hstats->flags & 1) return cube_fail(c, CUBE_ERR_DISPLACEMENT, "a particle left the double-buffer tile");
+  if ((int64_t)c->hstats->ndup_list > c->xtra_cap)
+    return cube_fail(c, CUBE_ERR_TILE_OVERFLOW, "extra-copy list overflow");
+  if (path == SORT) {
+    const int64_t nx = (int64_t)c->hstats->ndup_list;
+    const int db = sort_dest_bits(c->ncells), lb = 64 - SORT_VISIT_BITS - db;
+    if (lb < 8) return cube_fail(c, CUBE_ERR_ARG, "too many cells for the re-sort key");
+    CUBE_CUDA(c, cudaMemsetAsync(&c->dstats->flags, 0, sizeof(int), c->stream));
+    cube_phase_begin(c, PH_UPD_RANK);
+    CUBE_CUDA(c, cudaMemsetAsync(c->rhoc[kn], 0, 4 * (size_t)c->ncells, c->stream));
+    uint64_t* keys = c->skey[0];
+    int32_t* vals = c->sval[0];
+    if ((r = cube_sort_pairs(c, 0, 0, 64, &keys, &vals))) return r;  // buffers
+    k_sort_keys<<<cube_grid(c->np + nx, 256), 256, 0, c->stream>>>(a, keys, vals, nx, lb);
+    CUBE_CUDA(c, cudaGetLastError());
+    if ((r = cube_sort_pairs(c, c->np + nx, nx ? 0 : lb, 64, &keys, &vals))) return r;
+    cube_phase_end(c, PH_UPD_RANK);
+    if ((r = scan())) return r;
+    if (c->hstats->flags & 64) {  // a landing did not fit the key
+      CUBE_CUDA(c, cudaMemsetAsync(&c->dstats->flags, 0, sizeof(int), c->stream));
+      path = WALK;
+      if ((r = walk()) || (r = scan())) return r;
+    } else {
+      cube_phase_begin(c, PH_UPD_PLACE);
+      k_sort_place<<<cube_grid(np_new, 256), 256, 0, c->stream>>>(a, keys, vals, np_new, 64 - db);
+      cube_phase_end(c, PH_UPD_PLACE);
+      CUBE_CUDA(c, cudaGetLastError());
+    }
+  }
+  c->rank_walked = path;
   DevStats hs = *c->hstats;
-  if ((int64_t)hs.ndup_list > c->xtra_cap) return cube_fail(c, CUBE_ERR_TILE_OVERFLOW, "extra-copy list overflow");
   if (np_new > c->p.np_max)
     return cube_fail(c, CUBE_ERR_IMAGE_OVERFLOW, "new particle count exceeds np_max");
-  if (!walker) {
+  if (path != WALK) {
     cube_phase_begin(c, PH_UPD_PLACE);
-    k_rank_place<<<cube_grid(c->np, B), B, 0, c->stream>>>(a);
+    if (path == COUNT) k_rank_place<<<cube_grid(c->np, B), B, 0, c->stream>>>(a);
     k_vfield_new<<<cube_grid(c->ncells, 128, 32), 128, 0, c->stream>>>(a);
     k_vfield_dense<<<cube_grid((int64_t)1 << 40, 1, 4), 128, 0, c->stream>>>(a);
     cube_phase_end(c, PH_UPD_PLACE);

@@ -75,7 +75,7 @@ typedef struct cube_stats {
   float sigma_vi_new;     /* std_vsim_res/sqrt(3.) */
   int32_t nlayer;         /* layer count used for the visit order */
   int32_t max_disp;       /* largest cell displacement seen */
-  int32_t rank_walked;    /* 1: ranks came from the general walker, 0: counting path */
+  int32_t rank_walked;    /* ranks came from 0: the counting path, 1: the walker, 2: the sort */
   /* cube_pp_force (ext_pp_force.f90:10-162) */
   float f2_max_pp;
   int32_t pp_dense_bricks; /* bricks redone cell by cell (too dense to stage) */
@@ -302,9 +302,14 @@ void* cube_stream(cube_ctx* ctx);
    block; 4: global memory, one block per cell), which otherwise serve only
    regions too dense for the level before.  The pair sums
    are order-independent, so every level gives bitwise the same result; used
-   to test the dense-region paths.  CUBE_OPT_RANK_WALK=3 makes cube_update_x
-   use its general visit-order walker for the ranks instead of the counting
-   path it takes when every particle moved at most one cell (same result).
+   to test the dense-region paths.  CUBE_OPT_RANK_WALK=3 picks how
+   cube_update_x finds each particle's rank in its destination cell (the
+   reference's visit order): 0 (default) the counting path when every
+   particle moved at most one cell and landed in one frame, else a radix
+   sort on (destination, place of the source cell in the destination's visit
+   order, index in the source cell); 1 the visit-order walker (one thread per
+   destination walking its source cells); 2 the sort always.  Same result
+   for all.
    CUBE_OPT_DEPOSIT_FINE=4 / CUBE_OPT_DEPOSIT_COARSE=5 pick the brick shape
    of the fine / coarse density deposit (0-3; fine: 8x4x4, 4x4x4, 8x4x2,
    4x4x2 coarse cells; coarse: 8x8x8, 16x8x8, 8x8x4, 4x4x4): a tile-size

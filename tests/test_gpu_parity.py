@@ -83,29 +83,34 @@ def test_update_x_bitexact(name, pk, sk, dt):
 
 
 @pytest.mark.parametrize("name,pk,sk", CASES, ids=[c[0] for c in CASES])
-@pytest.mark.parametrize("dt", [20.0, 40.0])
+@pytest.mark.parametrize("dt", [20.0, 40.0, 90.0, 150.0])
 def test_update_rank_paths_agree_bitwise(name, pk, sk, dt):
-    # counting path (every particle moved at most one cell) against the
-    # general visit-order walker: identical state and statistics
+    # the three rank paths -- counting (every particle moved at most one cell,
+    # one frame), the visit-order walker, the sort of all landings -- give the
+    # same state and statistics; the default takes the sort when counting does
+    # not apply
     p = _params(pk)
     st = synth.random_state(p, **sk)
     outs = []
-    for walk in (0, 1):
+    for path in (0, 1, 2):
         g = C.CubeGPU(p)
         g.upload(st["xp"], st["vp"], st["pid"], st["rhoc"], st["vfield"])
         g.set_sigma(st["sigma_vi"], st["sigma_vi"])
-        g.set_option(C.OPT_RANK_WALK, walk)
+        g.set_option(C.OPT_RANK_WALK, path)
         s = g.update_x(np.float32(dt * 0.7), np.float32(dt), st["vz_max"])
         outs.append((s, g.download()))
         g.close()
-    (sa, da), (sb, db) = outs
-    assert sb["rank_walked"] == 1
+    (sa, da) = outs[0]
+    assert outs[1][0]["rank_walked"] == 1 and outs[2][0]["rank_walked"] == 2
     if sa["max_disp"] <= 1 and sa["ndup"] == 0:
         assert sa["rank_walked"] == 0
-    for k in ("xp", "vp", "pid", "rhoc"):
-        np.testing.assert_array_equal(da[k], db[k])
-    np.testing.assert_array_equal(da["vfield"].view(np.uint32), db["vfield"].view(np.uint32))
-    assert sa["sum_r"] == sb["sum_r"] and sa["nplocal"] == sb["nplocal"]
+    else:
+        assert sa["rank_walked"] == 2
+    for sb, db in outs[1:]:
+        for k in ("xp", "vp", "pid", "rhoc"):
+            np.testing.assert_array_equal(da[k], db[k])
+        np.testing.assert_array_equal(da["vfield"].view(np.uint32), db["vfield"].view(np.uint32))
+        assert sa["sum_r"] == sb["sum_r"] and sa["nplocal"] == sb["nplocal"] and sa["ndup"] == sb["ndup"]
 
 
 def test_upload_download_roundtrip():
