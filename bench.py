@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--adjoint-only", action="store_true", help="run only the differentiable-form measurement")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-ensemble line")
     ap.add_argument("--batched-only", action="store_true", help="run only the batched-ensemble measurement")
+    ap.add_argument("--no-two-species", action="store_true", help="skip the two-species line")
+    ap.add_argument("--two-species-only", action="store_true", help="run only the two-species measurement")
     ap.add_argument("--boxes", type=int, default=256, help="batched ensemble size")
     return ap.parse_args()
 
@@ -380,6 +382,95 @@ def run_adjoint(args, lrank, reps=3):
         sim.close()
 
 
+def run_two_species(args, lrank, m_nu=0.05, z_init=10.0):
+    """The two-species workload: 512^3 CDM (np_nc 2, PP on) plus 1024^3
+    thermal neutrinos (np_nc 4, m_nu 0.05 eV, Fermi-Dirac speeds) in a
+    1 Gpc/h box, nc 256 over 4^3 tiles, the neutrinos sharing the meshes
+    (cube_create_linked); initial conditions on the device at z = 10, then
+    steps under the reference's dt constraints with both species' vmax.  The
+    neutrinos move several coarse cells a step, so their re-sort takes the
+    sort of all landings."""
+    import torch
+
+    from cafproject_gb300 import cube as C
+    from cafproject_gb300 import params as P
+    from cafproject_gb300.cosmology import TimeState
+
+    torch.cuda.set_device(lrank)
+    h0, om = 0.7, 0.3
+    # mean density one per fine cell, split by Omega_nu h^2 = m_nu / 93.14 eV
+    f_nu = m_nu / 93.14 / h0 ** 2 / om
+    pc = P.CubeParams(nc=256, nnt=4, pp_on=True, rsoft=0.1, box=1000.0, np_nc=2, mass_p=8.0 * (1 - f_nu))
+    pn = P.CubeParams(nc=256, nnt=4, pp_on=False, box=1000.0, np_nc=4, mass_p=1.0 * f_nu)
+    t0 = time.perf_counter()
+    g = C.CubeGPU(pc, device=lrank)
+    nu = C.CubeGPU(pn, owner=g)
+    try:
+        sc, vc = g.ic_zeldovich(z_init, args.seed)
+        sn, vn = nu.ic_zeldovich_nu(z_init, args.seed, m_nu, args.seed + 7)
+        g.synchronize()
+        t_ic = time.perf_counter() - t0
+        ts = TimeState(a=np.float32(1.0 / (1.0 + z_init)), omega_m=om, omega_l=1 - om)
+        ts.vz_max = np.float32(max(vc[2], vn[2]))
+        ts.dt_vmax = np.float32(np.float32(18.0) / np.float32(max(max(vc), max(vn))))
+        stream = torch.cuda.ExternalStream(g.stream())
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+        parts = []
+        info = {}
+
+        def step(timed):
+            dt, a_mid = ts.timestep()
+            if timed:
+                ev[0].record(stream)
+            uc = g.update_x(ts.dt_old, dt, ts.vz_max)
+            if timed:
+                ev[1].record(stream)
+            un = nu.update_x(ts.dt_old, dt, ts.vz_max)
+            if timed:
+                ev[2].record(stream)
+            pp = g.ext_pp_force(a_mid, dt)
+            if timed:
+                ev[3].record(stream)
+            st, stn = g.particle_mesh2(nu, a_mid, dt)
+            if timed:
+                ev[4].record(stream)
+                torch.cuda.synchronize()
+                parts.append([ev[i].elapsed_time(ev[i + 1]) for i in range(4)])
+            ts.constrain({"f2_max_fine": st["f2_max_fine"], "f2_max_coarse": st["f2_max_coarse"],
+                          "vmax": [max(st["vmax"][d], stn["vmax"][d]) for d in range(3)]}, pp, pc.ncell)
+            info.update(nu_rank_path=int(un["rank_walked"]), nu_max_disp=int(un["max_disp"]),
+                        nu_nlayer=int(un["nlayer"]), cdm_rank_path=int(uc["rank_walked"]),
+                        nu_ndup=int(un["ndup"]))
+
+        for _ in range(max(1, args.warmup - 1)):
+            step(False)
+        for _ in range(args.steps):
+            step(True)
+        n = g.nplocal() + nu.nplocal()
+        # per-phase device time of one more step, timers on (not in the value)
+        g.timing(True)
+        nu.timing(True)
+        step(False)
+        phases = {"cdm": {k: round(v[0], 2) for k, v in g.timing_read().items() if v[1]},
+                  "nu": {k: round(v[0], 2) for k, v in nu.timing_read().items() if v[1]}}
+        g.timing(False)
+        nu.timing(False)
+        ms = [sum(x) for x in parts]
+        med = statistics.median(ms)
+        brk = {k: round(statistics.median(x[i] for x in parts), 2)
+               for i, k in enumerate(("update_cdm", "update_nu", "pp_cdm", "pm_both"))}
+        return {"metric": "particle-steps/s, 512^3 CDM + 1024^3 neutrinos", "value": n / (med / 1000.0),
+                "unit": UNIT, "ms_per_step": round(med, 2), "steps": args.steps, "ms_breakdown": brk,
+                "particles": {"cdm": int(g.nplocal()), "nu": int(nu.nplocal())}, "ic_s": round(t_ic, 1),
+                "z_init": z_init, "m_nu_ev": m_nu, "timing": "CUDA events on the library stream, per step",
+                "phases_ms": phases,
+                "config": {"workload": "two-species 1 Gpc/h", "nc": 256, "nf": 1024, "nnt": 4, "pp": "cdm",
+                           "np_nc": {"cdm": 2, "nu": 4}}, **info}
+    finally:
+        nu.close()
+        g.close()
+
+
 def run_batched(args, lrank, nsteps=50):
     """Boxes/s of the batched ensemble against the plain form run serially:
     256 boxes, each 32^3..128^3 particles (uniform choice), fine mesh twice the
@@ -512,9 +603,14 @@ def main():
         if rank == 0:
             print(json.dumps({"batched": run_batched(args, lrank)}), flush=True)
         return
+    if args.two_species_only:
+        if rank == 0:
+            print(json.dumps({"two_species": run_two_species(args, lrank)}), flush=True)
+        return
     r = run_gb300(args, ws, rank, lrank)
     adj = run_adjoint(args, lrank) if (rank == 0 and ws == 1 and not args.no_adjoint) else None
     bat = run_batched(args, lrank) if (rank == 0 and ws == 1 and not args.no_batched) else None
+    two = run_two_species(args, lrank) if (rank == 0 and ws == 1 and not args.no_two_species) else None
     if rank == 0:
         p = r["p"]
         line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -533,6 +629,8 @@ def main():
             line["adjoint"] = adj
         if bat:
             line["batched"] = bat
+        if two:
+            line["two_species"] = two
         print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist

@@ -521,13 +521,9 @@ __global__ void k_rank(UpdArgs a) {
   }
 }
 
-__device__ __forceinline__ void write_particle(const UpdArgs& a, int64_t p, int32_t D, uint32_t r) {
+// particle p, landed in cell D, written at index idx of the new arrays
+__device__ __forceinline__ void write_particle_at(const UpdArgs& a, int64_t p, int32_t D, int64_t idx) {
   const Geo& g = a.g;
-  if (D < 0 || (int64_t)D >= a.ncells || r >= (uint32_t)a.cnt_new[D]) {
-    atomicOr(&a.st->flags, 2);  // rank not assigned: never write outside the new arrays
-    return;
-  }
-  int64_t idx = a.cstart_new[D] + r;
   int64_t cell = a.pcell[p];
   // nint(dt_mid*vreal/(x_resolution*ncell)): the divisor is a power of two
   float scale = g.izipx == 1 ? 64.0f : 16384.0f;
@@ -566,6 +562,14 @@ __device__ __forceinline__ void write_particle(const UpdArgs& a, int64_t p, int3
   a.pcell_new[idx] = D;
 }
 
+__device__ __forceinline__ void write_particle(const UpdArgs& a, int64_t p, int32_t D, uint32_t r) {
+  if (D < 0 || (int64_t)D >= a.ncells || r >= (uint32_t)a.cnt_new[D]) {
+    atomicOr(&a.st->flags, 2);  // rank not assigned: never write outside the new arrays
+    return;
+  }
+  write_particle_at(a, p, D, a.cstart_new[D] + r);
+}
+
 // U2, general path: the rank of a landing (a particle's primary destination,
 // or an extra copy's) is its position among the landings in its destination
 // cell ordered by the reference's visit order, and the new disjoint order is
@@ -574,20 +578,21 @@ __device__ __forceinline__ void write_particle(const UpdArgs& a, int64_t p, int3
 //   (destination cell, layer of the source's z in the destination tile's
 //    frame, source offsets z, y, x from the destination, index in the
 //    source cell)
-// yields the new order itself: position = cstart_new[D] + rank.  Offsets fit
-// 5 bits (|offset| <= 2 ncb) and the layer 5 bits (nlayer <= 31); the index
-// in the source cell takes the bits left below the destination's.  Without
-// extra copies the sort skips the index bits: the radix sort is stable and
-// the primaries enter in storage order, which within a source cell is the
-// index order.
-constexpr int SORT_VISIT_BITS = 20;
-__host__ __device__ inline int sort_dest_bits(int64_t ncells) {
-  int b = 1;
-  while (((int64_t)1 << b) < ncells) b++;
+// yields the new order itself: position = cstart_new[D] + rank.  The fields
+// are as wide as this step needs: offsets + R in ob bits (|offset| <= R, the
+// largest displacement), the layer in bits(nlayer), the index in the source
+// cell in the lb bits left below (a landing that does not fit flags itself
+// and the walker takes over).  Without extra copies the sort skips the index
+// bits: the radix sort is stable and the primaries enter in storage order,
+// which within a source cell is the index order.
+inline int bits_for(int64_t n) {  // smallest b with 2^b >= n
+  int b = 0;
+  while (((int64_t)1 << b) < n) b++;
   return b;
 }
 
-__global__ void k_sort_keys(UpdArgs a, uint64_t* __restrict__ keys, int32_t* __restrict__ vals, int64_t nx, int lb) {
+__global__ void k_sort_keys(UpdArgs a, uint64_t* __restrict__ keys, int32_t* __restrict__ vals, int64_t nx, int lb,
+                            int ob, int R, int vb) {
   const Geo& g = a.g;
   const int64_t n = a.np + nx;
   const uint64_t lmax = (uint64_t)1 << lb;
@@ -615,7 +620,7 @@ __global__ void k_sort_keys(UpdArgs a, uint64_t* __restrict__ keys, int32_t* __r
     int sg[3], dg[3];
     cell_coords(g, S, sg[0], sg[1], sg[2]);
     cell_coords(g, D, dg[0], dg[1], dg[2]);
-    uint32_t visit = 0;
+    uint64_t visit = 0;
     int layer = 0;
     bool bad = l >= lmax;
     for (int d = 2; d >= 0; d--) {
@@ -625,37 +630,36 @@ __global__ void k_sort_keys(UpdArgs a, uint64_t* __restrict__ keys, int32_t* __r
       const int digit = d == 2 ? fr / 9 : (d == 1 ? (fr / 3) % 3 : fr % 3);
       const int Ls = L + (digit - 1) * g.nt;  // the source in the destination tile's frame
       const int off = Ls - DL;
-      bad = bad || off < -15 || off > 15;
+      bad = bad || off < -R || off > R;
       if (d == 2) layer = (Ls + g.ncb - 1) % nlay(a);
-      visit = (visit << 5) | (uint32_t)(off + 15);
+      visit = (visit << ob) | (uint64_t)((off + R) & ((1 << ob) - 1));
     }
-    bad = bad || layer > 31;
     if (bad) atomicOr(&a.st->flags, 64);  // does not fit the key: the walker takes over
-    visit |= (uint32_t)layer << 15;
-    keys[i] = ((uint64_t)D << (SORT_VISIT_BITS + lb)) | ((uint64_t)visit << lb) | (l & (lmax - 1));
+    visit |= (uint64_t)layer << (3 * ob);
+    keys[i] = ((uint64_t)D << (vb + lb)) | (visit << lb) | (l & (lmax - 1));
     atomicAdd(&a.cnt_new[D], 1);
   }
 }
 
-// ranks, extra copies' ranks and the inverse permutation from the sorted landings
-__global__ void k_sort_place(UpdArgs a, const uint64_t* __restrict__ keys, const int32_t* __restrict__ vals,
-                             int64_t n_new, int shift) {
+// the inverse permutation (new index -> particle) from the sorted landings
+__global__ void k_sort_place(UpdArgs a, const int32_t* __restrict__ vals, int64_t n_new) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_new; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t id = vals[i];
+    a.perm[i] = id < a.np ? (int32_t)id : a.xtra[id - a.np].x;
+  }
+}
+
+// U3 on the sort path: one thread per new index writes the particle that
+// lands there (coalesced writes; the reads stay within a few cells of the
+// destination, which L2 holds)
+__global__ void k_sort_gather(UpdArgs a, const uint64_t* __restrict__ keys, int64_t n_new, int shift) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_new; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t D = (int64_t)(keys[i] >> shift);
-    const int64_t id = vals[i];
-    if (D >= a.ncells) {
+    if (D >= a.ncells || i < a.cstart_new[D] || i >= a.cstart_new[D + 1]) {
       atomicOr(&a.st->flags, 2);
       continue;
     }
-    const uint32_t r = (uint32_t)(i - a.cstart_new[D]);
-    int64_t p = id;
-    if (id < a.np) {
-      a.rank[p] = r;
-    } else {
-      p = a.xtra[id - a.np].x;
-      a.xtra[id - a.np].z = (int)r;
-    }
-    a.perm[i] = (int32_t)p;
+    write_particle_at(a, a.perm[i], (int32_t)D, i);
   }
 }
 
@@ -811,7 +815,7 @@ static int update_x_graph(cube_ctx* c) {
   if (r) return r;
   k_rank_place<<<cube_grid(c->np, B), B, 0, s>>>(a);
   k_vfield_new<<<cube_grid(c->ncells, 128, 32), 128, 0, s>>>(a);
-  k_vfield_dense<<<cube_grid((int64_t)1 << 40, 1, 4), 128, 0, s>>>(a);
+  k_vfield_dense<<<cube_grid((int64_t)1 << 40, 1, 16), 128, 0, s>>>(a);
   k_scatter<<<cube_grid(c->np, B), B, 0, s>>>(a);
   k_scatter_xtra<<<cube_grid(c->xtra_cap, B, 2), B, 0, s>>>(a);
   const int nb = c->red_blocks;
@@ -917,9 +921,14 @@ int cube_update_x_impl(cube_ctx* c, float dt_old, float dt, float vz_max, cube_s
   if (c->hstats->flags & 1) return cube_fail(c, CUBE_ERR_DISPLACEMENT, "a particle left the double-buffer tile");
   if ((int64_t)c->hstats->ndup_list > c->xtra_cap)
     return cube_fail(c, CUBE_ERR_TILE_OVERFLOW, "extra-copy list overflow");
+  int db = 0;
+  uint64_t* skeys = nullptr;
   if (path == SORT) {
     const int64_t nx = (int64_t)c->hstats->ndup_list;
-    const int db = sort_dest_bits(c->ncells), lb = 64 - SORT_VISIT_BITS - db;
+    const int R = std::max(c->hstats->max_disp, 1);
+    const int ob = bits_for(2 * R + 1), vb = bits_for(nlayer) + 3 * ob;
+    db = bits_for(c->ncells);
+    const int lb = 64 - db - vb;
     if (lb < 8) return cube_fail(c, CUBE_ERR_ARG, "too many cells for the re-sort key");
     CUBE_CUDA(c, cudaMemsetAsync(&c->dstats->flags, 0, sizeof(int), c->stream));
     cube_phase_begin(c, PH_UPD_RANK);
@@ -927,7 +936,7 @@ int cube_update_x_impl(cube_ctx* c, float dt_old, float dt, float vz_max, cube_s
     uint64_t* keys = c->skey[0];
     int32_t* vals = c->sval[0];
     if ((r = cube_sort_pairs(c, 0, 0, 64, &keys, &vals))) return r;  // buffers
-    k_sort_keys<<<cube_grid(c->np + nx, 256), 256, 0, c->stream>>>(a, keys, vals, nx, lb);
+    k_sort_keys<<<cube_grid(c->np + nx, 256), 256, 0, c->stream>>>(a, keys, vals, nx, lb, ob, R, vb);
     CUBE_CUDA(c, cudaGetLastError());
     if ((r = cube_sort_pairs(c, c->np + nx, nx ? 0 : lb, 64, &keys, &vals))) return r;
     cube_phase_end(c, PH_UPD_RANK);
@@ -938,9 +947,10 @@ int cube_update_x_impl(cube_ctx* c, float dt_old, float dt, float vz_max, cube_s
       if ((r = walk()) || (r = scan())) return r;
     } else {
       cube_phase_begin(c, PH_UPD_PLACE);
-      k_sort_place<<<cube_grid(np_new, 256), 256, 0, c->stream>>>(a, keys, vals, np_new, 64 - db);
+      k_sort_place<<<cube_grid(np_new, 256), 256, 0, c->stream>>>(a, vals, np_new);
       cube_phase_end(c, PH_UPD_PLACE);
       CUBE_CUDA(c, cudaGetLastError());
+      skeys = keys;
     }
   }
   c->rank_walked = path;
@@ -951,15 +961,19 @@ int cube_update_x_impl(cube_ctx* c, float dt_old, float dt, float vz_max, cube_s
     cube_phase_begin(c, PH_UPD_PLACE);
     if (path == COUNT) k_rank_place<<<cube_grid(c->np, B), B, 0, c->stream>>>(a);
     k_vfield_new<<<cube_grid(c->ncells, 128, 32), 128, 0, c->stream>>>(a);
-    k_vfield_dense<<<cube_grid((int64_t)1 << 40, 1, 4), 128, 0, c->stream>>>(a);
+    k_vfield_dense<<<cube_grid((int64_t)1 << 40, 1, 16), 128, 0, c->stream>>>(a);
     cube_phase_end(c, PH_UPD_PLACE);
     CUBE_CUDA(c, cudaGetLastError());
   }
   r = cube_pid_join(c);  // a deferred pid upload lands before the scatter reads it
   if (r) return r;
   cube_phase_begin(c, PH_UPD_SCATTER);
-  k_scatter<<<cube_grid(c->np, B), B, 0, c->stream>>>(a);
-  if (hs.ndup_list) k_scatter_xtra<<<cube_grid((int64_t)hs.ndup_list, B), B, 0, c->stream>>>(a);
+  if (skeys) {
+    k_sort_gather<<<cube_grid(np_new, B), B, 0, c->stream>>>(a, skeys, np_new, 64 - db);
+  } else {
+    k_scatter<<<cube_grid(c->np, B), B, 0, c->stream>>>(a);
+    if (hs.ndup_list) k_scatter_xtra<<<cube_grid((int64_t)hs.ndup_list, B), B, 0, c->stream>>>(a);
+  }
   cube_phase_end(c, PH_UPD_SCATTER);
   CUBE_CUDA(c, cudaGetLastError());
   // sigma statistics of the new state (decoded with sigma_vi)
