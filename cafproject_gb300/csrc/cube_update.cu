@@ -375,9 +375,11 @@ __global__ void k_rank_place(UpdArgs a) {
 }
 
 // a cell over VF_DENSE particles goes to k_vfield_dense: one thread summing
-// hundreds of particles in rank order, three dependent loads each, would set
-// the kernel's tail
-constexpr uint32_t VF_DENSE = 64;
+// hundreds of particles in rank order would set the kernel's tail.  The
+// thread path loads VF_BATCH particles' codes, decoded values and source
+// means ahead of their (sequential) sums, so the loads of a batch overlap.
+constexpr uint32_t VF_DENSE = 256;
+constexpr uint32_t VF_BATCH = 4;
 __global__ void k_vfield_new(UpdArgs a) {
   if (a.sd && counting_failed(a)) return;
   for (int64_t D = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; D < a.ncells;
@@ -391,11 +393,31 @@ __global__ void k_vfield_new(UpdArgs a) {
 #pragma unroll
     for (int d = 0; d < 3; d++) acc[d] = __fmul_rn(a.vfield[3 * D + d], 0.1f);  // vfield*weight_v
     const int64_t i0 = a.cstart_new[D];
-    for (uint32_t i = 0; i < cnt; i++) {
-      int64_t p = a.perm[i0 + i];
-      int64_t S = a.pcell[p];
+    for (uint32_t i = 0; i < cnt; i += VF_BATCH) {
+      int64_t pb[VF_BATCH], Sb[VF_BATCH];
+      int code[VF_BATCH][3];
+      float vfs[VF_BATCH][3];
+      float2 dd[VF_BATCH][3];
 #pragma unroll
-      for (int d = 0; d < 3; d++) acc[d] = accumulate_v(a, acc[d], p, d, S);
+      for (uint32_t j = 0; j < VF_BATCH; j++) pb[j] = i + j < cnt ? a.perm[i0 + i + j] : a.perm[i0 + i];
+#pragma unroll
+      for (uint32_t j = 0; j < VF_BATCH; j++) {
+        Sb[j] = a.pcell[pb[j]];
+#pragma unroll
+        for (int d = 0; d < 3; d++) code[j][d] = load_code(a.vp, 3 * pb[j] + d, a.g.izipv);
+      }
+#pragma unroll
+      for (uint32_t j = 0; j < VF_BATCH; j++)
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          vfs[j][d] = a.vfield[3 * Sb[j] + d];
+          dd[j][d] = codec_decode_ff(a.cv, code[j][d]);
+        }
+#pragma unroll
+      for (uint32_t j = 0; j < VF_BATCH; j++)
+        if (i + j < cnt)
+#pragma unroll
+          for (int d = 0; d < 3; d++) acc[d] = accumulate_vals(a, acc[d], code[j][d], dd[j][d], vfs[j][d]);
     }
 #pragma unroll
     for (int d = 0; d < 3; d++) a.vfield_new[3 * D + d] = vfield_quotient(acc[d], cnt, a.exact_only);
