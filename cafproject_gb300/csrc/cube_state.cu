@@ -393,7 +393,13 @@ __global__ void k_codec_check(const double* __restrict__ v, int64_t n, double c,
                               int32_t* __restrict__ direct, int32_t* __restrict__ table) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     direct[i] = (int32_t)v_encode(v[i], c, nvbin);
-    table[i] = (int32_t)codec_encode(k, v[i]);
+    int32_t t = (int32_t)codec_encode(k, v[i]);
+    // the kernels' certified encode (its table-free test first): when it
+    // certifies a code, that code must be the table's; INT32_MIN marks a miss
+    const long long bits = __double_as_longlong(v[i]);
+    long long nq;
+    if (certify_abs(bits & 0x7fffffffffffffffLL, 0.f, k, &nq) && (bits < 0 ? -nq : nq) != (long long)t) t = INT32_MIN;
+    table[i] = t;
   }
 }
 
