@@ -325,15 +325,17 @@ extern "C" int cube_get_sigma(const cube_ctx* c, float* s, float* sn) {
   return CUBE_OK;
 }
 
-static int check_ready(cube_ctx* c) {
+// join: order the context stream after a pending cube_upload_begin first
+// (cube_update_x takes the pieces as they land instead)
+static int check_ready(cube_ctx* c, bool join = true) {
   if (!c) return CUBE_ERR_ARG;
   if (!c->have_state) return cube_fail(c, CUBE_ERR_STATE, "no state uploaded");
   CUBE_CUDA(c, cudaSetDevice(c->device));
-  return CUBE_OK;
+  return join ? cube_upload_join(c) : CUBE_OK;
 }
 
 extern "C" int cube_update_x(cube_ctx* c, float dt_old, float dt, float vz_max, cube_stats* st) {
-  int r = check_ready(c);
+  int r = check_ready(c, false);
   if (!r) r = cube_copy_join(c);
   if (r) return r;
   return cube_update_x_impl(c, dt_old, dt, vz_max, st);
@@ -445,6 +447,7 @@ extern "C" int cube_particle_mesh2(cube_ctx* c, cube_ctx* nu, float a_mid, float
   if (r) return r;
   if (!nu || nu->owner != c) return cube_fail(c, CUBE_ERR_ARG, "the second species must be linked to this context");
   if (!nu->have_state) return cube_fail(c, CUBE_ERR_STATE, "no state uploaded for the linked species");
+  if ((r = cube_upload_join(nu))) return cube_fail(c, r, nu->err);
   const float pre[2] = {a_mid, dt};
   if ((r = cube_fine_density_impl(c, nullptr, false))) return r;
   if ((r = cube_fine_density_impl(nu, nullptr, true))) return cube_fail(c, r, nu->err);

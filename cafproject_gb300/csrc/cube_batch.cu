@@ -408,7 +408,7 @@ extern "C" int cube_batch_step(cube_batch* b, int nsteps) {
   for (cube_ctx* c : b->box)  // host copies of a box's state started through its context end first
     if (c->stream_copy) {
       BCUDA(b, cudaStreamSynchronize(c->stream_copy));
-      c->copy_pending = c->pid_pending = false;
+      c->copy_pending = c->pid_pending = c->xv_pending = false;
     }
   return b->mode == CUBE_BATCH_GRAPH ? graph_steps(b, nsteps) : serial_steps(b, nsteps);
 }

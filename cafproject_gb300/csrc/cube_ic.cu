@@ -493,7 +493,7 @@ static int ic_impl(cube_ctx* c, const cube_cosmology* cs, float z_init, uint32_t
   }
   CUBE_CUDA(c, cudaSetDevice(c->device));
   if (int r = cube_copy_join(c)) return r;
-  if (int r = cube_pid_join(c)) return r;
+  if (int r = cube_upload_join(c)) return r;
   cudaStream_t s = c->stream;
   const double a = 1.0 / (1.0 + z_init);
   const int64_t nspec = (int64_t)(nf / 2 + 1) * nf * nf;

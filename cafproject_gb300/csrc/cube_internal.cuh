@@ -168,13 +168,18 @@ struct cube_ctx {
   // host copies beside the step on their own stream: a download of xp, pid,
   // rhoc and vfield beside PP and PM, of vp beside the coarse kick
   // (cube_download_begin / _finish; calls that change the state are ordered
-  // after it on the device by cube_copy_join), and the upload of pid beside
-  // the re-sort up to the scatter (cube_upload_begin; cube_pid_join)
+  // after it on the device by cube_copy_join), and an upload whose xp and vp
+  // arrive in UP_PIECES pieces beside the re-sort's first pass and pid beside
+  // the rest of the re-sort up to the scatter (cube_upload_begin; any other
+  // call that reads the state first waits for all of it, cube_upload_join)
+  static constexpr int UP_PIECES = 4;
   cudaStream_t stream_copy = nullptr;
   cudaEvent_t ev_copy_start = nullptr, ev_copy = nullptr, ev_pid = nullptr;
+  cudaEvent_t ev_xv[UP_PIECES] = {};
   bool copy_pending = false;
   void* vp_host = nullptr;  // vp destination of a pending download
-  bool pid_pending = false;
+  bool pid_pending = false, xv_pending = false;
+  int64_t up_np = 0;        // particle count of the pending upload's pieces
   // per-phase timers (null when disabled)
   struct CubeTimers* timers = nullptr;
   // stats
@@ -681,6 +686,8 @@ int cube_copy_join(cube_ctx* c);
 int cube_sort_pairs(cube_ctx* c, int64_t n, int begin_bit, int end_bit, uint64_t** keys, int32_t** vals);
 // orders the context stream after a deferred pid upload
 int cube_pid_join(cube_ctx* c);
+// ... after every piece of a pending cube_upload_begin (xp, vp and pid)
+int cube_upload_join(cube_ctx* c);
 int cube_copy_stream(cube_ctx* c);
 int cube_state_out_begin(cube_ctx* c, int64_t* np, void* xp, void* vp, int32_t* pid, int32_t* rhoc, float* vfield);
 int cube_state_out_finish(cube_ctx* c);

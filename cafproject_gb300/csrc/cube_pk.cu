@@ -108,6 +108,7 @@ extern "C" int cube_power_spectrum(cube_ctx* c, int ng, float box, const float* 
   const int need = cube_pk_nbin(ng);
   if (nbin < need) return cube_fail(c, CUBE_ERR_ARG, "xi needs nint(ng/2*sqrt(3)) bins");
   CUBE_CUDA(c, cudaSetDevice(c->device));
+  if (int r = cube_upload_join(c)) return r;
   cudaStream_t s = c->stream;
   float* m1 = c->force_f[0];
   float* m2 = c->force_f[1];

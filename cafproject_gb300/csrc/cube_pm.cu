@@ -775,11 +775,11 @@ int cube_coarse_kick_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st, bo
   k.exact_only = c->opt_exact_kicks;
   cube_phase_begin(c, PH_C_KICK);
   if (c->vp_host && !c->graph_mode) {
-    // a download is waiting for vp: kick in four pieces of particles, each
+    // a download is waiting for vp: kick in eight pieces of particles, each
     // piece's codes going to the host while the next is kicked
     const size_t bx = 3 * (size_t)c->p.izipx, bv = 3 * (size_t)c->p.izipv;
-    for (int i = 0; i < 4; i++) {
-      const int64_t p0 = c->np * i / 4, p1 = c->np * (i + 1) / 4;
+    for (int i = 0; i < 8; i++) {
+      const int64_t p0 = c->np * i / 8, p1 = c->np * (i + 1) / 8;
       if (p1 <= p0) continue;
       KickArgs kp = k;
       kp.np = p1 - p0;

@@ -115,32 +115,50 @@ __global__ void k_fill_pcell(const int32_t* __restrict__ rhoc, const int64_t* __
 }
 
 int cube_state_in(cube_ctx* c, int64_t np, const void* xp, const void* vp, const int32_t* pid, const int32_t* rhoc,
-                  const float* vfield, bool defer_pid) {
+                  const float* vfield, bool defer) {
   int k = c->cur;
   const cube_params& p = c->p;
   int r = cube_copy_join(c);
-  if (!r) r = cube_pid_join(c);
+  if (!r) r = cube_upload_join(c);
   if (r) return r;
   // the counts are checked on the device, after the copies (a failed check
   // leaves the context without a state)
   c->have_state = false;
-  if (pid && defer_pid) {  // the re-sort reads pid only in its scatter
-    if ((r = cube_copy_stream(c))) return r;
-    CUBE_CUDA(c, cudaEventRecord(c->ev_copy_start, c->stream));
-    CUBE_CUDA(c, cudaStreamWaitEvent(c->stream_copy, c->ev_copy_start, 0));
-    CUBE_CUDA(c, cudaMemcpyAsync(c->pid[k], pid, (size_t)4 * np, cudaMemcpyHostToDevice, c->stream_copy));
-    CUBE_CUDA(c, cudaEventRecord(c->ev_pid, c->stream_copy));
-    c->pid_pending = true;
-  }
-  CUBE_CUDA(c, cudaMemcpyAsync(c->xp[k], xp, (size_t)3 * np * p.izipx, cudaMemcpyHostToDevice, c->stream));
-  CUBE_CUDA(c, cudaMemcpyAsync(c->vp[k], vp, (size_t)3 * np * p.izipv, cudaMemcpyHostToDevice, c->stream));
-  if (pid && defer_pid) {
-  } else if (pid)
-    CUBE_CUDA(c, cudaMemcpyAsync(c->pid[k], pid, (size_t)4 * np, cudaMemcpyHostToDevice, c->stream));
-  else
-    CUBE_CUDA(c, cudaMemsetAsync(c->pid[k], 0, (size_t)4 * np, c->stream));
   CUBE_CUDA(c, cudaMemcpyAsync(c->rhoc[k], rhoc, (size_t)4 * c->ncells, cudaMemcpyHostToDevice, c->stream));
-  CUBE_CUDA(c, cudaMemcpyAsync(c->vfield[k], vfield, (size_t)12 * c->ncells, cudaMemcpyHostToDevice, c->stream));
+  if (defer) {
+    // vfield, then xp and vp piece by piece, then pid on the copy stream: the
+    // re-sort's first pass takes each piece as it lands (cube_update_x); the
+    // count check below needs only rhoc
+    if ((r = cube_copy_stream(c))) return r;
+    cudaStream_t s = c->stream_copy;
+    CUBE_CUDA(c, cudaEventRecord(c->ev_copy_start, c->stream));
+    CUBE_CUDA(c, cudaStreamWaitEvent(s, c->ev_copy_start, 0));
+    CUBE_CUDA(c, cudaMemcpyAsync(c->vfield[k], vfield, (size_t)12 * c->ncells, cudaMemcpyHostToDevice, s));
+    const size_t bx = 3 * (size_t)p.izipx, bv = 3 * (size_t)p.izipv;
+    for (int i = 0; i < cube_ctx::UP_PIECES; i++) {
+      const int64_t p0 = np * i / cube_ctx::UP_PIECES, p1 = np * (i + 1) / cube_ctx::UP_PIECES;
+      CUBE_CUDA(c, cudaMemcpyAsync((char*)c->xp[k] + bx * p0, (const char*)xp + bx * p0, bx * (p1 - p0),
+                                   cudaMemcpyHostToDevice, s));
+      CUBE_CUDA(c, cudaMemcpyAsync((char*)c->vp[k] + bv * p0, (const char*)vp + bv * p0, bv * (p1 - p0),
+                                   cudaMemcpyHostToDevice, s));
+      CUBE_CUDA(c, cudaEventRecord(c->ev_xv[i], s));
+    }
+    if (pid)
+      CUBE_CUDA(c, cudaMemcpyAsync(c->pid[k], pid, (size_t)4 * np, cudaMemcpyHostToDevice, s));
+    else
+      CUBE_CUDA(c, cudaMemsetAsync(c->pid[k], 0, (size_t)4 * np, s));
+    CUBE_CUDA(c, cudaEventRecord(c->ev_pid, s));
+    c->xv_pending = c->pid_pending = true;
+    c->up_np = np;
+  } else {
+    CUBE_CUDA(c, cudaMemcpyAsync(c->xp[k], xp, (size_t)3 * np * p.izipx, cudaMemcpyHostToDevice, c->stream));
+    CUBE_CUDA(c, cudaMemcpyAsync(c->vp[k], vp, (size_t)3 * np * p.izipv, cudaMemcpyHostToDevice, c->stream));
+    if (pid)
+      CUBE_CUDA(c, cudaMemcpyAsync(c->pid[k], pid, (size_t)4 * np, cudaMemcpyHostToDevice, c->stream));
+    else
+      CUBE_CUDA(c, cudaMemsetAsync(c->pid[k], 0, (size_t)4 * np, c->stream));
+    CUBE_CUDA(c, cudaMemcpyAsync(c->vfield[k], vfield, (size_t)12 * c->ncells, cudaMemcpyHostToDevice, c->stream));
+  }
   r = cube_scan_counts(c, c->rhoc[k], c->cstart[k], c->ncells);
   if (r) return r;
   CUBE_CUDA(c, cudaMemsetAsync(&c->dstats->flags, 0, sizeof(int), c->stream));
@@ -152,8 +170,14 @@ int cube_state_in(cube_ctx* c, int64_t np, const void* xp, const void* vp, const
   CUBE_CUDA(c, cudaMemcpyAsync(&tot, c->cstart[k] + c->ncells, 8, cudaMemcpyDeviceToHost, c->stream));
   CUBE_CUDA(c, cudaMemcpyAsync(&fl, &c->dstats->flags, 4, cudaMemcpyDeviceToHost, c->stream));
   CUBE_CUDA(c, cudaStreamSynchronize(c->stream));
-  if (fl & (1 << 16)) return cube_fail(c, CUBE_ERR_ARG, "negative rhoc");
-  if (tot != np) return cube_fail(c, CUBE_ERR_COUNT_MISMATCH, "sum(rhoc) != nplocal");
+  if ((fl & (1 << 16)) || tot != np) {
+    if (defer) {  // no state: the pieces still in flight end before the call does
+      CUBE_CUDA(c, cudaStreamSynchronize(c->stream_copy));
+      c->xv_pending = c->pid_pending = false;
+    }
+    if (fl & (1 << 16)) return cube_fail(c, CUBE_ERR_ARG, "negative rhoc");
+    return cube_fail(c, CUBE_ERR_COUNT_MISMATCH, "sum(rhoc) != nplocal");
+  }
   c->np = np;
   c->npglobal = np;
   c->have_state = true;
@@ -164,7 +188,7 @@ int cube_state_in(cube_ctx* c, int64_t np, const void* xp, const void* vp, const
 int cube_state_out(cube_ctx* c, int64_t* np, void* xp, void* vp, int32_t* pid, int32_t* rhoc, float* vfield) {
   int k = c->cur;
   const cube_params& p = c->p;
-  if (int r = cube_pid_join(c)) return r;
+  if (int r = cube_upload_join(c)) return r;
   if (np) *np = c->np;
   if (xp) CUBE_CUDA(c, cudaMemcpyAsync(xp, c->xp[k], (size_t)3 * c->np * p.izipx, cudaMemcpyDeviceToHost, c->stream));
   if (vp) CUBE_CUDA(c, cudaMemcpyAsync(vp, c->vp[k], (size_t)3 * c->np * p.izipv, cudaMemcpyDeviceToHost, c->stream));
@@ -182,6 +206,8 @@ int cube_copy_stream(cube_ctx* c) {
   CUBE_CUDA(c, cudaEventCreateWithFlags(&c->ev_copy_start, cudaEventDisableTiming));
   CUBE_CUDA(c, cudaEventCreateWithFlags(&c->ev_copy, cudaEventDisableTiming));
   CUBE_CUDA(c, cudaEventCreateWithFlags(&c->ev_pid, cudaEventDisableTiming));
+  for (int i = 0; i < cube_ctx::UP_PIECES; i++)
+    CUBE_CUDA(c, cudaEventCreateWithFlags(&c->ev_xv[i], cudaEventDisableTiming));
   return CUBE_OK;
 }
 
@@ -196,6 +222,12 @@ int cube_pid_join(cube_ctx* c) {
     c->pid_pending = false;
   }
   return CUBE_OK;
+}
+
+int cube_upload_join(cube_ctx* c) {
+  if (c->xv_pending) c->pid_pending = true;  // pid is the last piece on the copy stream
+  c->xv_pending = false;
+  return cube_pid_join(c);
 }
 
 // The force half of a step (PP and PM) reads xp, pid, rhoc and vfield and

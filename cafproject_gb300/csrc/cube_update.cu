@@ -56,6 +56,7 @@ struct UpdArgs {
   int32_t* pcell_new;
   const StepDev* sd;  // graph mode: dt_mid and nlayer from the device
   int32_t* vdense;    // destination cells over VF_DENSE particles, for k_vfield_dense
+  int64_t p_lo;       // k_dest: first particle of this launch (particles [p_lo, np))
 };
 
 __device__ __forceinline__ float dtm(const UpdArgs& a) { return a.sd ? __ldg(&a.sd->h.dt_mid) : a.dt_mid; }
@@ -104,7 +105,7 @@ __global__ void k_dest(UpdArgs a) {
   const Geo& g = a.g;
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int local_max = 0;
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.np; p += stride) {
+  for (int64_t p = a.p_lo + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.np; p += stride) {
     int64_t cell = a.pcell[p];
     int gc[3];
     cell_coords(g, cell, gc[0], gc[1], gc[2]);
@@ -903,7 +904,20 @@ int cube_update_x_impl(cube_ctx* c, float dt_old, float dt, float vz_max, cube_s
   const int B = 256;
   CUBE_CUDA(c, cudaMemsetAsync(c->rank, 0xFF, 4 * (size_t)c->np, c->stream));  // "no rank" sentinel
   cube_phase_begin(c, PH_UPD_DEST);
-  k_dest<<<cube_grid(c->np, B), B, 0, c->stream>>>(a);
+  if (c->xv_pending && c->up_np == c->np) {
+    // a pending cube_upload_begin: take xp and vp piece by piece as they land
+    for (int i = 0; i < cube_ctx::UP_PIECES; i++) {
+      UpdArgs ap = a;
+      ap.p_lo = c->np * i / cube_ctx::UP_PIECES;
+      ap.np = c->np * (i + 1) / cube_ctx::UP_PIECES;
+      CUBE_CUDA(c, cudaStreamWaitEvent(c->stream, c->ev_xv[i], 0));
+      if (ap.np > ap.p_lo) k_dest<<<cube_grid(ap.np - ap.p_lo, B), B, 0, c->stream>>>(ap);
+    }
+    c->xv_pending = false;  // pid (the last piece) is joined before the scatter
+  } else {
+    if ((r = cube_upload_join(c))) return r;
+    k_dest<<<cube_grid(c->np, B), B, 0, c->stream>>>(a);
+  }
   cube_phase_end(c, PH_UPD_DEST);
   // ranks: the counting path (its kernels check their own eligibility on the
   // device and flag it), else the sort of all landings; the visit-order

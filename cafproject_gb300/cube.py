@@ -255,9 +255,10 @@ class CubeGPU:
         return dict(xp=xp, vp=vp, pid=pid, rhoc=rhoc, vfield=vf)
 
     def upload_begin(self, xp, vp, pid, rhoc, vfield):
-        """``upload`` with pid copied beside the next update_x's first passes;
-        the arrays must be contiguous, of the state's dtypes, and pinned for
-        the overlap, and pid unchanged until that update_x returns."""
+        """``upload`` with xp and vp copied in pieces beside the next
+        update_x's first pass and pid beside the rest of it; the arrays must
+        be contiguous, of the state's dtypes, and pinned for the overlap, and
+        xp, vp and pid unchanged until that update_x returns."""
         for a in (xp, vp, pid, rhoc, vfield):
             assert a is None or a.flags.c_contiguous
         self._check(self.L.cube_upload_begin(self.h, xp.shape[0], _ptr(xp), _ptr(vp), _ptr(pid), _ptr(rhoc),

@@ -162,16 +162,19 @@ int cube_download_state(cube_ctx* ctx, int64_t* nplocal, void* xp, void* vp, int
    state in host memory and moves it every step.  Host memory should be
    page-locked for the copies to run asynchronously.
 
-   cube_upload_begin is cube_upload_state with pid copied on a side stream:
-   the re-sort reads pid only in its scatter, so the copy runs beside the
-   re-sort's first passes.  The host pid array must stay unchanged until the
-   next cube_update_x (or cube_synchronize) returns.
+   cube_upload_begin is cube_upload_state with vfield, xp, vp and pid copied
+   on a side stream, xp and vp in four pieces: the counts are checked before
+   it returns (they need only rhoc), the re-sort's first pass takes each
+   piece of xp and vp as it lands, and the re-sort reads pid only in its
+   scatter.  The host xp, vp and pid arrays must stay unchanged until the
+   next cube_update_x (or cube_synchronize) returns; any other call that
+   reads the state first waits for the whole upload.
 
    cube_download_begin, called after cube_update_x and the buffer calls,
    starts copying xp, pid, rhoc and vfield, which are final for the step (PP
    and PM read them and write only vp), on a side stream and returns.  vp is
    copied behind the next coarse kick, piece by piece as the kick finishes
-   each quarter of the particles, or by cube_download_finish when no kick
+   each eighth of the particles, or by cube_download_finish when no kick
    comes first.  cube_download_finish returns when all of them are in host
    memory.  Any array may be NULL.  A call that changes the state before the
    finish (cube_update_x, an upload, a checkpoint read, initial conditions)

@@ -109,10 +109,12 @@ def test_split_download_matches_download():
         g.close()
 
 
-def test_overlapped_upload_matches_upload():
-    # pid copied beside the re-sort's first passes (cube_upload_begin): the
-    # steps give bit for bit the state of a plain upload, and the host pid
-    # array may change once update_x has returned
+@pytest.mark.parametrize("first", ["update_x", "particle_mesh"])
+def test_overlapped_upload_matches_upload(first):
+    # xp and vp in pieces beside the re-sort's first pass, pid beside the rest
+    # (cube_upload_begin): the steps give bit for bit the state of a plain
+    # upload, and the host arrays may change once update_x has returned; a
+    # call other than update_x first waits for the whole upload
     import torch
     from cafproject_gb300 import cube as C
     from cafproject_gb300 import params as P
@@ -128,9 +130,12 @@ def test_overlapped_upload_matches_upload():
             (g.upload_begin if overlap else g.upload)(pin["xp"], pin["vp"], pin["pid"], pin["rhoc"], pin["vfield"])
             s = np.float32(st["sigma_vi"])
             g.set_sigma(s, s)
+            if first == "particle_mesh":
+                g.pp_particle_mesh(np.float32(0.4), np.float32(0.02))
             for _ in range(2):
                 g.update_x(np.float32(20.0), np.float32(30.0), st["vz_max"])
-                pin["pid"][:] = -7
+                for k in ("pid", "xp", "vp"):
+                    pin[k][:] = -7
                 g.pp_particle_mesh(np.float32(0.4), np.float32(0.02))
             outs.append(g.download())
         finally:
