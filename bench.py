@@ -306,15 +306,21 @@ def run_gb300(args, ws, rank, lrank):
     outt = {k: torch.empty_like(v).pin_memory() for k, v in pin.items()}
     out = {k: v.numpy() for k, v in outt.items()}
     h2d = sum(v.nbytes for v in hin.values())
-    barrier(ws)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    # pid travels to the device beside the re-sort's first passes; xp, pid,
-    # rhoc and vfield to the host beside PP+PM, vp behind the coarse kick
-    for _ in range(ke):
+
+    # xp and vp travel to the device in pieces beside the re-sort's first
+    # pass, pid beside the rest of it; xp, pid, rhoc and vfield to the host
+    # beside PP+PM, vp behind the coarse kick
+    def e2e_step():
         g.upload_begin(hin["xp"], hin["vp"], hin["pid"], hin["rhoc"], hin["vfield"])
         step(after_x=lambda: g.download_begin(out))
         g.download_finish()
+
+    e2e_step()  # untimed: the copy stream's first use and the fresh pinned buffers' first transfers
+    barrier(ws)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        e2e_step()
     torch.cuda.synchronize()
     te = time.perf_counter() - t0
     te = allreduce_max(te, ws, dev)
