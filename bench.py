@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-ensemble line")
     ap.add_argument("--batched-only", action="store_true", help="run only the batched-ensemble measurement")
     ap.add_argument("--no-two-species", action="store_true", help="skip the two-species line")
+    ap.add_argument("--no-redshifts", action="store_true", help="skip the later-redshift steps")
     ap.add_argument("--two-species-only", action="store_true", help="run only the two-species measurement")
     ap.add_argument("--boxes", type=int, default=256, help="batched ensemble size")
     return ap.parse_args()
@@ -197,6 +198,55 @@ def algorithmic_bytes(p, n):
         "coarse_fft": (4 * nc3 + 8 * hc) + (8 * hc + 12 * hc + 24 * hc) + 3 * (8 * hc + 4 * nc3) + 24 * nc3,
         "coarse_kick": n * (3 * p.izipx + 2 * 3 * p.izipv + 4 + 12) + 12 * nc3,
     }
+
+
+def run_redshifts(args, lrank, zs=(5.0, 0.0)):
+    """The same 512^3 step from Zel'dovich states at later redshifts, where
+    clustering makes PP and the re-sort dearer: per z, device time per step
+    (CUDA events on the library stream) over args.steps steps after
+    args.warmup, with the step's PP and PM as one call as in the headline."""
+    import torch
+
+    from cafproject_gb300 import cube as C
+    from cafproject_gb300 import params as P
+    from cafproject_gb300.cosmology import TimeState
+
+    torch.cuda.set_device(lrank)
+    p = P.WORKLOADS[args.workload]()
+    out = {}
+    for z in zs:
+        g = C.CubeGPU(p, device=lrank)
+        try:
+            sigma, vm = g.ic_zeldovich(z, args.seed)
+            ts = TimeState(a=np.float32(1.0 / (1.0 + z)), omega_m=p.omega_m, omega_l=p.omega_l)
+            ts.vz_max = np.float32(vm[2])
+            ts.dt_vmax = np.float32(np.float32(18.0) / np.float32(max(vm)))
+            stream = torch.cuda.ExternalStream(g.stream())
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            pp_pairs = 0
+
+            def step():
+                nonlocal pp_pairs
+                dt, a_mid = ts.timestep()
+                g.update_x(ts.dt_old, dt, ts.vz_max)
+                pps, pms = g.pp_particle_mesh(a_mid, dt)
+                ts.constrain(pms, pps, p.ncell)
+                pp_pairs = int(pps["npairs"])
+
+            for _ in range(args.warmup):
+                step()
+            g.synchronize()
+            e0.record(stream)
+            for _ in range(args.steps):
+                step()
+            e1.record(stream)
+            g.synchronize()
+            ms = e0.elapsed_time(e1) / args.steps
+            out["%g" % z] = {"ms_per_step": round(ms, 2), "value": g.nplocal() / (ms / 1000.0),
+                             "pp_pairs_per_step": pp_pairs}
+        finally:
+            g.close()
+    return out
 
 
 def run_gb300(args, ws, rank, lrank):
@@ -617,6 +667,7 @@ def main():
     adj = run_adjoint(args, lrank) if (rank == 0 and ws == 1 and not args.no_adjoint) else None
     bat = run_batched(args, lrank) if (rank == 0 and ws == 1 and not args.no_batched) else None
     two = run_two_species(args, lrank) if (rank == 0 and ws == 1 and not args.no_two_species) else None
+    zs = run_redshifts(args, lrank) if (rank == 0 and ws == 1 and not args.no_redshifts) else None
     if rank == 0:
         p = r["p"]
         line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -637,6 +688,9 @@ def main():
             line["batched"] = bat
         if two:
             line["two_species"] = two
+        if zs:
+            zs = {"%g" % args.z: {"ms_per_step": round(r["ms"], 2), "value": r["value"]}, **zs}
+            line["redshifts"] = zs
         print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist
