@@ -574,7 +574,7 @@ def run_batched(args, lrank, nsteps=50):
 
 def gpu_launches(p, steps):
     """Launches of this library's kernels per step (cuFFT kernels not counted)."""
-    upd = 1 + 2 + 3 + 2 + 1 + 1  # dest, counting ranks (2), scan (3), place + vfield, scatter, sigma
+    upd = 1 + 2 + 3 + 3 + 1 + 1  # dest, counting ranks (2), scan (3), place + two vfield passes, scatter, sigma
     pp = 6 if p.pp_on else 0     # five pair levels (bricks, large bricks, cells, large cells, global), kick
     fine = 4                     # deposit, green, maxima + kick factors, kick
     coarse = 4
