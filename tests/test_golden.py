@@ -76,3 +76,38 @@ def test_gpu_step_matches_golden_fixtures():
         assert abs(pm["f2_max_coarse"] - g["pm_f2_max_coarse"]) <= 1e-5 * g["pm_f2_max_coarse"]
     finally:
         c.close()
+
+
+def test_oracle_reproduces_resort_fixture():
+    # a step that moves particles several cells over 2^3 tiles: the layered
+    # visit order beyond neighbouring cells, pinned (velocity codes within one
+    # off x86, as above)
+    pytest.importorskip("oracle.cube_oracle")
+    g = dict(np.load(os.path.join(HERE, "golden", "oracle_resort_nc24.npz")))
+    m = _mk()
+    new = m.make_resort()
+    assert set(new) == set(g)
+    import platform
+    same_libm = platform.machine() == "x86_64"
+    for k, v in g.items():
+        if k.endswith("_vp") and not same_libm:
+            d = np.abs(np.asarray(new[k]).astype(np.int64) - v.astype(np.int64))
+            assert d.max() <= 1 and (d > 0).mean() < 1e-3, k
+        else:
+            np.testing.assert_array_equal(np.asarray(new[k]), v, err_msg=k)
+    # the fixture does exercise multi-cell moves: some particle's new cell is
+    # more than one cell from its old one
+    p = m.resort_params()
+    nt, nnt = p.nt, p.nnt
+
+    def coords(cid):
+        ix, iy, iz = cid % nt, (cid // nt) % nt, (cid // nt ** 2) % nt
+        t = cid // nt ** 3
+        return np.stack([(t % nnt) * nt + ix, ((t // nnt) % nnt) * nt + iy, (t // nnt ** 2) * nt + iz], 1)
+
+    ncells = p.nc ** 3
+    old = np.repeat(np.arange(ncells), g["in_rhoc"])
+    new_cell = np.repeat(np.arange(ncells), g["upd_rhoc"])
+    src = g["upd_pid"].astype(np.int64) - 1
+    off = (coords(old[src]) - coords(new_cell) + p.nc // 2) % p.nc - p.nc // 2
+    assert np.abs(off).max() > 1
