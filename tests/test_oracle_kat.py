@@ -206,6 +206,39 @@ def test_update_x_rank_follows_layer_order():
     assert orders[5] == (k6, k4)
 
 
+def test_update_x_rank_follows_layer_order_beyond_neighbours():
+    # Particles from local k=2 and k=8 move three cells (+3 and -3) into k=5,
+    # beyond the counting path's reach.  Layer = (k+ncb-1) mod nlayer with
+    # ncb=6: nlayer=7 gives k=2 -> 0 and k=8 -> 6 (k=2 first); nlayer=9 gives
+    # 7 and 4 (k=8 first); nlayer=1 is the plain k order (k=2 first).
+    p = P.CubeParams(nc=24, nnt=1, pp_on=False, mass_p=8.0)
+    sigma = np.float32(0.01)
+    cells = [(3, 3, 1), (3, 3, 7)]  # 0-based z: local k=2 and k=8
+    v = 0.5
+    code = int(synth.encode(np.array([v]), sigma, 2)[0])
+    st = state_from(p, cells, [[0, 0, 0], [0, 0, 0]], [[0, 0, code], [0, 0, -code]])
+    t = np.float32(np.tan(np.float64(np.float32(np.float32(PI_F * np.float32(code)) / np.float32(65535)))))
+    vv = float(t) / synth.vcoef(sigma)
+    dt = np.float32(12.0 / vv)  # dt_mid*v/ncell = 3 cells
+    orders = {}
+    for ceil_q, label in ((0, 1), (3, 7), (4, 9)):
+        img = O.OracleImage(p)
+        img.load(**st)
+        img.sigma_vi = sigma
+        out = img.update_x(dt, dt, np.float32(ceil_q) / dt * np.float32(4.0) * np.float32(0.999))
+        s = img.state()
+        assert out["nlayer"] == label
+        cell = 3 + 24 * (3 + 24 * 4)  # 0-based (x,y,z)=(3,3,4)
+        start = int(np.sum(s["rhoc"][:cell]))
+        assert s["rhoc"][cell] == 2
+        orders[label] = tuple(s["pid"][start:start + 2])
+    k2 = int(st["pid"][np.nonzero(np.asarray(st["vp"])[:, 2] > 0)[0][0]])
+    k8 = int(st["pid"][np.nonzero(np.asarray(st["vp"])[:, 2] < 0)[0][0]])
+    assert orders[1] == (k2, k8)
+    assert orders[7] == (k2, k8)
+    assert orders[9] == (k8, k2)
+
+
 def test_mass_conservation():
     p = P.small(nc=24, nnt=2)
     st = synth.random_state(p, seed=4, clump=5)
