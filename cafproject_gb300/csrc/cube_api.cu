@@ -53,6 +53,7 @@ static void release(cube_ctx* c) {
   }
   cube_timers_free(c);
   if (c->owner) {  // meshes, kernels, plans, work area and stream belong to the owner
+    if (c->owner->linked == c) c->owner->linked = nullptr;
     c->rho_f = c->kern_f = c->kern_f_raw = c->rho_c = c->kern_c = nullptr;
     for (int d = 0; d < 3; d++) c->force_f[d] = c->force_c[d] = nullptr;
     c->cufft_work = nullptr;
@@ -155,6 +156,7 @@ static int create_impl(const cube_params* p, const float* fine_table, const floa
   CUBE_CUDA(c, cudaSetDevice(device));
   if (owner) {
     c->owner = owner;
+    owner->linked = c;
     c->stream = owner->stream;
   } else {
     CUBE_CUDA(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
@@ -461,7 +463,37 @@ extern "C" int cube_particle_mesh2(cube_ctx* c, cube_ctx* nu, float a_mid, float
   if ((r = cube_coarse_spectral_impl(c, st, pre))) return r;
   if ((r = cube_coarse_kick_impl(c, a_mid, dt, st, true))) return r;
   if ((r = cube_coarse_kick_impl(nu, a_mid, dt, st_nu, true))) return cube_fail(c, r, nu->err);
+  // testrhof / testrhoc sum both species' mass (pm.f90:108, 258); the coarse
+  // kick left the second species' deposited masses in its host stats
+  if (st) {
+    st->testrhof += std::ldexp((double)nu->hstats->rhof_fix, -dep_shift(nu->p.mass_p));
+    st->testrhoc += std::ldexp((double)nu->hstats->rhoc_fix, -dep_shift(nu->p.mass_p));
+  }
   return CUBE_OK;
+}
+
+// Density stages of cube_particle_mesh2, for parity tests: both species'
+// CIC deposits into the shared fine (coarse) mesh, testrhof (testrhoc) the
+// total mass.
+static int density2(cube_ctx* c, cube_ctx* nu, cube_stats* st, bool fine) {
+  int r = check_ready(c);
+  if (r) return r;
+  if (!nu || nu->owner != c) return cube_fail(c, CUBE_ERR_ARG, "the second species must be linked to this context");
+  if (!nu->have_state) return cube_fail(c, CUBE_ERR_STATE, "no state uploaded for the linked species");
+  if ((r = cube_upload_join(nu))) return cube_fail(c, r, nu->err);
+  cube_stats a{}, b{};
+  if ((r = fine ? cube_fine_density_impl(c, &a, false) : cube_coarse_density_impl(c, &a, false))) return r;
+  if ((r = fine ? cube_fine_density_impl(nu, &b, true) : cube_coarse_density_impl(nu, &b, true)))
+    return cube_fail(c, r, nu->err);
+  if (st) {
+    st->testrhof = a.testrhof + b.testrhof;
+    st->testrhoc = a.testrhoc + b.testrhoc;
+  }
+  return CUBE_OK;
+}
+extern "C" int cube_pm_fine_density2(cube_ctx* c, cube_ctx* nu, cube_stats* st) { return density2(c, nu, st, true); }
+extern "C" int cube_pm_coarse_density2(cube_ctx* c, cube_ctx* nu, cube_stats* st) {
+  return density2(c, nu, st, false);
 }
 
 extern "C" int64_t cube_nplocal(const cube_ctx* c) { return c ? c->np : -1; }
@@ -484,6 +516,10 @@ extern "C" int cube_set_option(cube_ctx* c, int option, int64_t value) {
     case CUBE_OPT_DEPOSIT_COARSE:
       if (value < 0 || value > 3) return cube_fail(c, CUBE_ERR_ARG, "deposit brick shape must be 0 to 3");
       (option == CUBE_OPT_DEPOSIT_FINE ? c->opt_dep_fine : c->opt_dep_coarse) = (int)value;
+      return CUBE_OK;
+    case CUBE_OPT_FAIL_ALLOC:
+      if (value < 0 || value > 64) return cube_fail(c, CUBE_ERR_ARG, "allocation fault index must be 0 to 64");
+      c->fail_alloc = (int)value;
       return CUBE_OK;
     default:
       return cube_fail(c, CUBE_ERR_ARG, "unknown option");
@@ -544,6 +580,14 @@ static int field_io(cube_ctx* c, int field, void* host, bool to_host) {
       double s = (double)n * n * n;
       float* h = (float*)host;
       for (size_t i = 0; i < cnt; i++) h[i] = (float)((double)h[i] * s);
+      return CUBE_OK;
+    }
+    case CUBE_FIELD_FORCE_PP: {
+      if (!to_host) return cube_fail(c, CUBE_ERR_ARG, "the PP force is read-only");
+      if (!c->fpp) return cube_fail(c, CUBE_ERR_ARG, "PP is off for this context (pp_on = 0)");
+      if (!c->have_state) return cube_fail(c, CUBE_ERR_STATE, "no state uploaded");
+      CUBE_CUDA(c, cudaMemcpyAsync(host, c->fpp, 12 * (size_t)c->np, cudaMemcpyDeviceToHost, c->stream));
+      CUBE_CUDA(c, cudaStreamSynchronize(c->stream));
       return CUBE_OK;
     }
     default:

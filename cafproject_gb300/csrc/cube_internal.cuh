@@ -142,6 +142,8 @@ struct cube_ctx {
   int rank_walked = 0;     // the last update used the walker
   int opt_pp_level = 0;  // first PP level (0-4)
   int opt_dep_fine = 0, opt_dep_coarse = 0;  // deposit brick shapes (0-3)
+  int fail_alloc = 0;    // host fault injection: the n-th lazy allocation fails (0: off)
+  cube_ctx* linked = nullptr;  // the second species linked to this context, if any
   // fine PM
   cufftHandle plan_f_r2c = 0, plan_f_c2r = 0;
   float* rho_f = nullptr;       // padded real / complex in place

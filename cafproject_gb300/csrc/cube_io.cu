@@ -96,6 +96,16 @@ extern "C" int cube_checkpoint_write(cube_ctx* c, const char* dir, float z, int 
   s.ncb = c->p.ncb;
   s.image = image;
   s.sigma_vi = c->sigma_vi;  // checkpoint.f90:31
+  // the second species' fields of the header come from its live state, as
+  // the reference writes sigma_vi_nu (CUBEnu checkpoint.f90:32), so the info
+  // file always matches the *_nu files written beside it
+  if (c->linked && c->linked->have_state) {
+    const cube_ctx* nu = c->linked;
+    s.nplocal_nu = nu->np;
+    s.izipx_nu = nu->p.izipx;
+    s.izipv_nu = nu->p.izipv;
+    s.sigma_vi_nu = nu->sigma_vi;
+  }
   // the linked species writes xp_nu, vp_nu, np_nu, vc_nu, id_nu (checkpoint.f90:19-23, 55-70);
   // its counts travel in the owner's header (nplocal_nu)
   const bool nu = c->owner != nullptr;

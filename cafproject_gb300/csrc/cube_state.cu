@@ -499,18 +499,26 @@ extern "C" int cube_arith_check(cube_ctx* c, int64_t* mismatches) {
 }
 
 // ------------------------------------------------- codec check, static scratch
-// cube_codec_check_static: the same check with its device scratch in a
+// cube_codec_check_static: the same check with all of its device scratch in a
 // file-scope array instead of per-call cudaMalloc/cudaFree.  It serves callers
 // that must not allocate device memory: a production run sizes np_max to fill
 // most of HBM, so a mid-run cudaMalloc can fail or fragment the pool, and
-// cudaFree synchronises the whole device, which stalls a monitoring thread's
-// caller and every other stream.  The array is CUBE_CODEC_STATIC_MAX doubles of
-// input followed by two CUBE_CODEC_STATIC_MAX int32 outputs (256 KiB); nothing
-// in it needs to start at zero (the kernel writes every output it reads back).
+// cudaFree synchronises the whole device, which stalls every other stream.
+// The array holds CUBE_CODEC_STATIC_MAX doubles of input, two
+// CUBE_CODEC_STATIC_MAX int32 outputs and one set of codec tables for the
+// largest velocity format (izipv = 2: 65536 decode values as double and as a
+// float pair, 32769 encode bounds), 1.25 MiB + 256 KiB in all.  The tables
+// are rebuilt by every call for its sigma, so the context's own two codec
+// slots (the step's sigma_vi and sigma_vi_new) are never touched.  Nothing in
+// the array needs to start at zero: each call writes every value it reads.
 // All contexts on one device share the array, so two calls whose device work
 // overlapped would race; each call holds a per-device host lock from its
-// first copy until its stream has drained.
-constexpr int64_t kCodecStaticBytes = CUBE_CODEC_STATIC_MAX * (8 + 4 + 4);
+// first launch until its stream has drained.
+constexpr int64_t kStaticNvbin = 65536;  // 2^(8*izipv) for izipv <= 2
+constexpr int64_t kStaticIoBytes = CUBE_CODEC_STATIC_MAX * (8 + 4 + 4);
+constexpr int64_t kStaticTabBytes = kStaticNvbin * 8 + kStaticNvbin * 8 + (kStaticNvbin / 2 + 1) * 8;
+constexpr int64_t kCodecStaticBytes = kStaticIoBytes + kStaticTabBytes;
+static_assert(kStaticIoBytes % 256 == 0, "the tables start 256-byte aligned");
 static __device__ __align__(256) unsigned char g_codec_scratch[kCodecStaticBytes];
 
 namespace {
@@ -540,22 +548,36 @@ extern "C" int cube_codec_check_static(cube_ctx* c, float sigma, const double* v
   if (n > CUBE_CODEC_STATIC_MAX)
     return cube_fail(c, CUBE_ERR_ARG, "n = " + std::to_string(n) + " exceeds the static scratch maximum of " +
                                           std::to_string((long long)CUBE_CODEC_STATIC_MAX) + " values");
-  CUBE_CUDA(c, cudaSetDevice(c->device));
+  if (!(sigma > 0.f)) return cube_fail(c, CUBE_ERR_ARG, "sigma_vi must be positive");
   if (c->device < 0 || c->device >= kMaxDevices) return cube_fail(c, CUBE_ERR_ARG, "device ordinal out of range");
+  if (c->nvbin > kStaticNvbin) return cube_fail(c, CUBE_ERR_ARG, "velocity format wider than the static tables");
+  CUBE_CUDA(c, cudaSetDevice(c->device));
   std::lock_guard<std::mutex> lock(g_codec_scratch_mu[c->device]);
   unsigned char* base = nullptr;
   int r = codec_scratch_address(c, &base);
-  if (r) return r;
-  CodecView k;
-  r = cube_codec_pair(c, sigma, sigma, &k, nullptr);
   if (r) return r;
   if (n == 0) return CUBE_OK;
   double* dv = reinterpret_cast<double*>(base);
   int32_t* dd = reinterpret_cast<int32_t*>(base + 8 * CUBE_CODEC_STATIC_MAX);
   int32_t* dt = reinterpret_cast<int32_t*>(base + 12 * CUBE_CODEC_STATIC_MAX);
+  cube_ctx::Codec tab;
+  tab.sigma = sigma;
+  tab.dec = reinterpret_cast<double*>(base + kStaticIoBytes);
+  tab.dech = reinterpret_cast<float2*>(base + kStaticIoBytes + 8 * kStaticNvbin);
+  tab.bnd = reinterpret_cast<long long*>(base + kStaticIoBytes + 16 * kStaticNvbin);
+  CodecView k;
+  view_of(c, tab, &k);
   // every early return below first drains the stream, so the lock is never
   // released with work on the shared array still in flight
-  cudaError_t e = cudaMemcpyAsync(dv, v, 8 * (size_t)n, cudaMemcpyHostToDevice, c->stream);
+  const int nmax = c->nvbin / 2 - 1;
+  k_decode_table<<<(c->nvbin + 255) / 256, 256, 0, c->stream>>>(c->tan_tab, c->nvbin, sigma, nullptr, tab.dec,
+                                                                  tab.dech);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) {
+    k_encode_bounds<<<(nmax + 127) / 128, 128, 0, c->stream>>>(sigma, nullptr, c->nvbin, tab.bnd);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dv, v, 8 * (size_t)n, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess) {
     k_codec_check<<<cube_grid(n, 256), 256, 0, c->stream>>>(dv, n, vcoef_host(sigma), c->nvbin, k, dd, dt);
     e = cudaGetLastError();

@@ -19,6 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIBPATH = os.path.join(HERE, "_build", "libcube_gb300.so")
 
 FIELD_RHO_F, FIELD_FORCE_F, FIELD_RHO_C, FIELD_FORCE_C, FIELD_KERN_F, FIELD_KERN_C = 1, 2, 3, 4, 5, 6
+FIELD_FORCE_PP = 7
 
 STATUS = {0: "CUBE_OK", 1: "CUBE_ERR_ARG", 2: "CUBE_ERR_CUDA", 3: "CUBE_ERR_TILE_OVERFLOW",
           4: "CUBE_ERR_IMAGE_OVERFLOW", 5: "CUBE_ERR_PP_OVERFLOW", 6: "CUBE_ERR_COUNT_MISMATCH",
@@ -33,7 +34,7 @@ EXPORTS = ["cube_create", "cube_destroy", "cube_last_error", "cube_upload_state"
            "cube_pm_coarse_forces", "cube_pm_coarse_kick", "cube_get_field", "cube_set_field", "cube_nplocal",
            "cube_synchronize", "cube_timing", "cube_timing_read", "cube_phase_name", "cube_stream",
            "cube_codec_check", "cube_codec_check_static", "cube_arith_check", "cube_pk_nbin",
-           "cube_power_spectrum", "cube_checkpoint_write", "cube_checkpoint_read", "cube_ic_zeldovich", "cube_ic_zeldovich_nu", "cube_create_linked", "cube_particle_mesh2", "cube_set_option",
+           "cube_power_spectrum", "cube_checkpoint_write", "cube_checkpoint_read", "cube_ic_zeldovich", "cube_ic_zeldovich_nu", "cube_create_linked", "cube_particle_mesh2", "cube_pm_fine_density2", "cube_pm_coarse_density2", "cube_set_option",
            "cube_dpm_create", "cube_dpm_destroy", "cube_dpm_last_error", "cube_dpm_stream", "cube_dpm_nparticles",
            "cube_dpm_set_schedule", "cube_dpm_noise", "cube_dpm_forward", "cube_dpm_backward", "cube_dpm_density",
            "cube_dpm_density_adjoint", "cube_dpm_tables", "cube_dpm_info",
@@ -46,6 +47,7 @@ OPT_PP_LEVEL = 2
 OPT_RANK_WALK = 3
 OPT_DEPOSIT_FINE = 4
 OPT_DEPOSIT_COARSE = 5
+OPT_FAIL_ALLOC = 6
 NPHASE = 16
 
 
@@ -158,6 +160,8 @@ def load_library(path=None):
     L.cube_ic_zeldovich_nu.argtypes = [P, P, F, ctypes.c_uint32, F, ctypes.c_uint32, P, P]
     L.cube_create_linked.argtypes = [P, P, P]
     L.cube_particle_mesh2.argtypes = [P, P, F, F, P, P]
+    L.cube_pm_fine_density2.argtypes = [P, P, P]
+    L.cube_pm_coarse_density2.argtypes = [P, P, P]
     L.cube_set_option.argtypes = [P, ctypes.c_int, I64]
     _lib = L
     return L
@@ -341,6 +345,17 @@ class CubeGPU:
         self._check(self.L.cube_pm_coarse_density(self.h, ctypes.byref(st)))
         return st.as_dict()
 
+    def fine_density2(self, nu):
+        """Fine density of this species and the linked species nu together."""
+        st = CubeStats()
+        self._check(self.L.cube_pm_fine_density2(self.h, nu.h, ctypes.byref(st)))
+        return st.as_dict()
+
+    def coarse_density2(self, nu):
+        st = CubeStats()
+        self._check(self.L.cube_pm_coarse_density2(self.h, nu.h, ctypes.byref(st)))
+        return st.as_dict()
+
     def fine_forces(self):
         st = CubeStats()
         self._check(self.L.cube_pm_fine_forces(self.h, ctypes.byref(st)))
@@ -462,7 +477,7 @@ class CubeGPU:
         nf, nc = self.p.nf, self.p.nc
         return {FIELD_RHO_F: (nf, nf, nf), FIELD_FORCE_F: (3, nf, nf, nf), FIELD_RHO_C: (nc, nc, nc),
                 FIELD_FORCE_C: (3, nc, nc, nc), FIELD_KERN_F: (3, nf, nf, nf // 2 + 1),
-                FIELD_KERN_C: (3, nc, nc, nc // 2 + 1)}[which]
+                FIELD_KERN_C: (3, nc, nc, nc // 2 + 1), FIELD_FORCE_PP: (self.nplocal(), 3)}[which]
 
     def get_field(self, which):
         """Fields as numpy arrays indexed [.., z, y, x] (Fortran order of the reference)."""

@@ -128,7 +128,9 @@ enum cube_field {
   CUBE_FIELD_RHO_C = 3,    /* coarse density nc^3 float */
   CUBE_FIELD_FORCE_C = 4,  /* coarse force, 3 planes of nc^3 float */
   CUBE_FIELD_KERN_F = 5,   /* fine kernel Im part, 3 planes of (nf/2+1)*nf*nf float (unscaled) */
-  CUBE_FIELD_KERN_C = 6    /* coarse kernel, 3 planes of (nc/2+1)*nc*nc float (unscaled) */
+  CUBE_FIELD_KERN_C = 6,   /* coarse kernel, 3 planes of (nc/2+1)*nc*nc float (unscaled) */
+  CUBE_FIELD_FORCE_PP = 7  /* PP pair force of the last cube_pp_force, f_tot(3,nplocal) float in
+                              storage order (ext_pp_force.f90:94-112); read-only */
 };
 
 /* Build a context on `device`: allocates every device buffer for the given
@@ -189,8 +191,10 @@ int cube_download_finish(cube_ctx* ctx);
    as particle_initialization.f90:34-64 does): in dir, <z>_info_<image>.bin,
    _xp_, _vp_, _np_, _vc_ and (with particle ids) _id_, <z> = z printed as
    Fortran f7.3 without blanks.  Write fills nplocal, izipx/v, nnt, nt, ncell,
-   ncb, image and sigma_vi from the context and takes the other header fields
-   from hdr; read checks the zip format and tile geometry, uploads the state,
+   ncb, image and sigma_vi from the context -- and, when a second species is
+   linked to the context and holds a state, nplocal_nu, izipx_nu, izipv_nu
+   and sigma_vi_nu from that species (checkpoint.f90:31-32) -- and takes the
+   other header fields from hdr; read checks the zip format and tile geometry, uploads the state,
    sets sigma_vi and returns the header in hdr (may be NULL).  On a linked
    context (the second species) they use the _xp_nu_, _vp_nu_, _np_nu_,
    _vc_nu_, _id_nu_ files, write no info file, and read nplocal_nu, izipx_nu,
@@ -254,6 +258,11 @@ int cube_pp_particle_mesh(cube_ctx* ctx, float a_mid, float dt, cube_stats* st_p
    are kicked by the same forces with their own velocity codes, sigma_vi and
    vmax (st_nu). */
 int cube_particle_mesh2(cube_ctx* ctx, cube_ctx* nu, float a_mid, float dt, cube_stats* st, cube_stats* st_nu);
+/* Its density stages, for parity tests: both species deposited into the
+   shared fine (coarse) mesh, each cell's second-species particles after the
+   first's (pm.f90:52-107 / 205-267); st->testrhof (testrhoc) is the total. */
+int cube_pm_fine_density2(cube_ctx* ctx, cube_ctx* nu, cube_stats* st);
+int cube_pm_coarse_density2(cube_ctx* ctx, cube_ctx* nu, cube_stats* st);
 
 /* Stages of particle_mesh, for parity tests that inspect or inject fields:
    density only (CIC deposit, pm.f90:52-107 / 205-267), forces (deposit +
@@ -316,13 +325,17 @@ void* cube_stream(cube_ctx* ctx);
    CUBE_OPT_DEPOSIT_FINE=4 / CUBE_OPT_DEPOSIT_COARSE=5 pick the brick shape
    of the fine / coarse density deposit (0-3; fine: 8x4x4, 4x4x4, 8x4x2,
    4x4x2 coarse cells; coarse: 8x8x8, 16x8x8, 8x8x4, 4x4x4): a tile-size
-   choice for the autotuner, same exact sums for every shape. */
+   choice for the autotuner, same exact sums for every shape.
+   CUBE_OPT_FAIL_ALLOC=6 is host-side fault injection for tests: value n > 0
+   makes the n-th device allocation the library makes lazily (the general
+   re-sort's key buffers, on first use) report failure, 0 turns it off. */
 enum cube_option {
   CUBE_OPT_EXACT_KICKS = 1,
   CUBE_OPT_PP_LEVEL = 2,
   CUBE_OPT_RANK_WALK = 3,
   CUBE_OPT_DEPOSIT_FINE = 4,
-  CUBE_OPT_DEPOSIT_COARSE = 5
+  CUBE_OPT_DEPOSIT_COARSE = 5,
+  CUBE_OPT_FAIL_ALLOC = 6
 };
 int cube_set_option(cube_ctx* ctx, int option, int64_t value);
 
@@ -338,14 +351,20 @@ int cube_codec_check(cube_ctx* ctx, float sigma, const double* v, int64_t n, int
 int cube_arith_check(cube_ctx* ctx, int64_t* mismatches);
 
 /* cube_codec_check without any device allocation (no counterpart in the
-   reference): the device scratch is a fixed file-scope array of
-   CUBE_CODEC_STATIC_MAX input values, shared by every call on a device, for
-   callers that must not allocate (a run whose particle arrays fill HBM; a
-   monitoring thread that must not trigger cudaFree's device-wide
-   synchronisation).  n > CUBE_CODEC_STATIC_MAX returns CUBE_ERR_ARG.  The
-   first call on each device resolves the array's address and should come
-   before any stream capture.  Calls are serialised per device by a host lock;
-   each returns after its stream has drained. */
+   reference): all of its device scratch -- CUBE_CODEC_STATIC_MAX input
+   values, their two outputs and one set of codec tables (1.5 MiB in all) --
+   is a fixed file-scope array that every GPU loading the library holds until
+   exit.  It is for callers that must not allocate: a run whose particle
+   arrays fill HBM (a mid-run cudaMalloc can fail there), or a monitor that
+   must not trigger cudaFree's device-wide synchronisation.  n >
+   CUBE_CODEC_STATIC_MAX returns CUBE_ERR_ARG.  The call builds its own codec
+   tables for sigma in the array, so the context's tables for the step's
+   sigma_vi / sigma_vi_new stay as they were.  The first call on each device
+   resolves the array's address and should come before any stream capture.
+   Calls on one device share the array and are serialised by a host lock that
+   covers only that array; each returns after the context's stream has
+   drained.  The call runs on the context's stream, so a monitoring thread
+   uses a context of its own (calls on one context must not overlap). */
 #define CUBE_CODEC_STATIC_MAX 16384
 int cube_codec_check_static(cube_ctx* ctx, float sigma, const double* v, int64_t n, int32_t* direct,
                             int32_t* table);

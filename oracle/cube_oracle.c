@@ -399,14 +399,45 @@ void orc_sigma_sums(const orc_params* p, float sigma_vi, const void* vp, const i
 
 /* ------------------------------------------------------------- fine PM */
 
+/* CIC of one particle at fine position cidx (tile-local coarse cell, 1-based)
+   into rho(nfe,nfe,nfe) with the reference's real(4) weights (pm.f90:62-78). */
+static inline void fine_cic(int64_t ncell, int64_t nfb, int64_t nfe, const int64_t cidx[3], const void* bxp,
+                            int64_t ip, int64_t izipx, float mass, float* rho) {
+  int64_t i1[3], i2[3];
+  float d1[3], d2[3];
+  for (int d = 0; d < 3; d++) {
+    double tx = fine_pos(ncell, cidx[d], ld_i(bxp, 3 * ip + d, izipx), izipx);
+    float tempx = (float)tx;
+    i1[d] = (int64_t)floorf(tempx) + 1;
+    i2[d] = i1[d] + 1;
+    d1[d] = (float)i1[d] - tempx;
+    d2[d] = 1.0f - d1[d];
+    i1[d] += nfb;
+    i2[d] += nfb;
+  }
+#define RF(a, b, c) rho[((a)-1) + nfe * (((b)-1) + nfe * ((c)-1))]
+  RF(i1[0], i1[1], i1[2]) += ((d1[0] * d1[1]) * d1[2]) * mass;
+  RF(i2[0], i1[1], i1[2]) += ((d2[0] * d1[1]) * d1[2]) * mass;
+  RF(i1[0], i2[1], i1[2]) += ((d1[0] * d2[1]) * d1[2]) * mass;
+  RF(i1[0], i1[1], i2[2]) += ((d1[0] * d1[1]) * d2[2]) * mass;
+  RF(i1[0], i2[1], i2[2]) += ((d1[0] * d2[1]) * d2[2]) * mass;
+  RF(i2[0], i1[1], i2[2]) += ((d2[0] * d1[1]) * d2[2]) * mass;
+  RF(i2[0], i2[1], i1[2]) += ((d2[0] * d2[1]) * d1[2]) * mass;
+  RF(i2[0], i2[1], i2[2]) += ((d2[0] * d2[1]) * d2[2]) * mass;
+#undef RF
+}
+
 /* Fine CIC deposit of tile t into rho(nfe,nfe,nfe) (pm.f90:50-107); rho is
-   zeroed here. OpenMP over k slabs 3 apart, as the reference layers them. */
+   zeroed here. OpenMP over k slabs 3 apart, as the reference layers them.
+   q (may be NULL) is a second species (CUBEnu's neutrinos) with its own
+   buffered state: each cell's particles of the second species follow the
+   cell's first-species particles into the same mesh (pm.f90:79-103). */
 void orc_fine_deposit(const orc_params* p, int64_t t, const int32_t* brhoc, const int64_t* bstart,
-                      const void* bxp, float* rho) {
+                      const void* bxp, float* rho, const orc_params* q, const int32_t* brhoc2,
+                      const int64_t* bstart2, const void* bxp2) {
   int64_t nt = p->nt, ncb = p->ncb, ncell = p->ncell;
   int64_t nfb = ncb * ncell, nft = nt * ncell, nfe = nft + 2 * nfb;
   const int64_t nlayer = 3;
-  float mass = p->mass_p;
   memset(rho, 0, sizeof(float) * nfe * nfe * nfe);
   set_threads(p);
   for (int64_t ilayer = 0; ilayer < nlayer; ilayer++) {
@@ -416,31 +447,11 @@ void orc_fine_deposit(const orc_params* p, int64_t t, const int32_t* brhoc, cons
         for (int64_t i = 2 - ncb; i <= nt + ncb - 1; i++) {
           int64_t e = ext_index(p, i, j, k, t);
           int64_t cidx[3] = {i, j, k};
-          for (int64_t l = 0; l < brhoc[e]; l++) {
-            int64_t ip = bstart[e] + l;
-            int64_t i1[3], i2[3];
-            float d1[3], d2[3];
-            for (int d = 0; d < 3; d++) {
-              double tx = fine_pos(ncell, cidx[d], ld_i(bxp, 3 * ip + d, p->izipx), p->izipx);
-              float tempx = (float)tx;
-              i1[d] = (int64_t)floorf(tempx) + 1;
-              i2[d] = i1[d] + 1;
-              d1[d] = (float)i1[d] - tempx;
-              d2[d] = 1.0f - d1[d];
-              i1[d] += nfb;
-              i2[d] += nfb;
-            }
-#define RF(a, b, c) rho[((a)-1) + nfe * (((b)-1) + nfe * ((c)-1))]
-            RF(i1[0], i1[1], i1[2]) += ((d1[0] * d1[1]) * d1[2]) * mass;
-            RF(i2[0], i1[1], i1[2]) += ((d2[0] * d1[1]) * d1[2]) * mass;
-            RF(i1[0], i2[1], i1[2]) += ((d1[0] * d2[1]) * d1[2]) * mass;
-            RF(i1[0], i1[1], i2[2]) += ((d1[0] * d1[1]) * d2[2]) * mass;
-            RF(i1[0], i2[1], i2[2]) += ((d1[0] * d2[1]) * d2[2]) * mass;
-            RF(i2[0], i1[1], i2[2]) += ((d2[0] * d1[1]) * d2[2]) * mass;
-            RF(i2[0], i2[1], i1[2]) += ((d2[0] * d2[1]) * d1[2]) * mass;
-            RF(i2[0], i2[1], i2[2]) += ((d2[0] * d2[1]) * d2[2]) * mass;
-#undef RF
-          }
+          for (int64_t l = 0; l < brhoc[e]; l++)
+            fine_cic(ncell, nfb, nfe, cidx, bxp, bstart[e] + l, p->izipx, p->mass_p, rho);
+          if (q)
+            for (int64_t l = 0; l < brhoc2[e]; l++)
+              fine_cic(ncell, nfb, nfe, cidx, bxp2, bstart2[e] + l, q->izipx, q->mass_p, rho);
         }
   }
 }
@@ -508,12 +519,40 @@ void orc_fine_kick(const orc_params* p, int64_t t, float a_mid, float dt, float 
 
 /* ----------------------------------------------------------- coarse PM */
 
-/* Coarse CIC deposit of the whole image into r3(nc,nc,nc) (pm.f90:205-267). */
+/* CIC of one particle into r3t(-1:nt+2)^3 at the coarse position of
+   tile-local cell cidx, -0.5 shift (pm.f90:219-233). */
+static inline void coarse_cic(int64_t n4, const int64_t cidx[3], const void* bxp, int64_t ip, int64_t izipx,
+                              float mass, float* r3t) {
+  int64_t i1[3], i2[3];
+  float d1[3], d2[3];
+  for (int d = 0; d < 3; d++) {
+    double tx2 = coarse_pos(cidx[d], ld_i(bxp, 3 * ip + d, izipx), izipx);
+    float tempx = (float)tx2;
+    i1[d] = (int64_t)floorf(tempx) + 1;
+    i2[d] = i1[d] + 1;
+    d1[d] = (float)i1[d] - tempx;
+    d2[d] = 1.0f - d1[d];
+  }
+#define RT(a, b, c) r3t[((a) + 1) + n4 * (((b) + 1) + n4 * ((c) + 1))]
+  RT(i1[0], i1[1], i1[2]) += ((d1[0] * d1[1]) * d1[2]) * mass;
+  RT(i2[0], i1[1], i1[2]) += ((d2[0] * d1[1]) * d1[2]) * mass;
+  RT(i1[0], i2[1], i1[2]) += ((d1[0] * d2[1]) * d1[2]) * mass;
+  RT(i1[0], i1[1], i2[2]) += ((d1[0] * d1[1]) * d2[2]) * mass;
+  RT(i1[0], i2[1], i2[2]) += ((d1[0] * d2[1]) * d2[2]) * mass;
+  RT(i2[0], i1[1], i2[2]) += ((d2[0] * d1[1]) * d2[2]) * mass;
+  RT(i2[0], i2[1], i1[2]) += ((d2[0] * d2[1]) * d1[2]) * mass;
+  RT(i2[0], i2[1], i2[2]) += ((d2[0] * d2[1]) * d2[2]) * mass;
+#undef RT
+}
+
+/* Coarse CIC deposit of the whole image into r3(nc,nc,nc) (pm.f90:205-267);
+   q (may be NULL) is a second species deposited after each cell's
+   first-species particles (pm.f90:234-250). */
 void orc_coarse_deposit(const orc_params* p, const int32_t* brhoc, const int64_t* bstart,
-                        const void* bxp, float* r3) {
+                        const void* bxp, float* r3, const orc_params* q, const int32_t* brhoc2,
+                        const int64_t* bstart2, const void* bxp2) {
   int64_t nt = p->nt, nnt = p->nnt, nc = p->nc;
   int64_t n4 = nt + 4; /* r3t(-1:nt+2)^3 */
-  float mass = p->mass_p;
   float* r3t = (float*)malloc(sizeof(float) * n4 * n4 * n4);
   memset(r3, 0, sizeof(float) * nc * nc * nc);
   set_threads(p);
@@ -527,30 +566,13 @@ void orc_coarse_deposit(const orc_params* p, const int32_t* brhoc, const int64_t
           for (int64_t i = 0; i <= nt + 1; i++) {
             int64_t e = ext_index(p, i, j, k, t);
             int64_t cidx[3] = {i, j, k};
-            for (int64_t l = 0; l < brhoc[e]; l++) {
-              int64_t ip = bstart[e] + l;
-              int64_t i1[3], i2[3];
-              float d1[3], d2[3];
-              for (int d = 0; d < 3; d++) {
-                double tx2 = coarse_pos(cidx[d], ld_i(bxp, 3 * ip + d, p->izipx), p->izipx);
-                float tempx = (float)tx2;
-                i1[d] = (int64_t)floorf(tempx) + 1;
-                i2[d] = i1[d] + 1;
-                d1[d] = (float)i1[d] - tempx;
-                d2[d] = 1.0f - d1[d];
-              }
-#define RT(a, b, c) r3t[((a) + 1) + n4 * (((b) + 1) + n4 * ((c) + 1))]
-              RT(i1[0], i1[1], i1[2]) += ((d1[0] * d1[1]) * d1[2]) * mass;
-              RT(i2[0], i1[1], i1[2]) += ((d2[0] * d1[1]) * d1[2]) * mass;
-              RT(i1[0], i2[1], i1[2]) += ((d1[0] * d2[1]) * d1[2]) * mass;
-              RT(i1[0], i1[1], i2[2]) += ((d1[0] * d1[1]) * d2[2]) * mass;
-              RT(i1[0], i2[1], i2[2]) += ((d1[0] * d2[1]) * d2[2]) * mass;
-              RT(i2[0], i1[1], i2[2]) += ((d2[0] * d1[1]) * d2[2]) * mass;
-              RT(i2[0], i2[1], i1[2]) += ((d2[0] * d2[1]) * d1[2]) * mass;
-              RT(i2[0], i2[1], i2[2]) += ((d2[0] * d2[1]) * d2[2]) * mass;
-            }
+            for (int64_t l = 0; l < brhoc[e]; l++) coarse_cic(n4, cidx, bxp, bstart[e] + l, p->izipx, p->mass_p, r3t);
+            if (q)
+              for (int64_t l = 0; l < brhoc2[e]; l++)
+                coarse_cic(n4, cidx, bxp2, bstart2[e] + l, q->izipx, q->mass_p, r3t);
           }
     }
+#define RT(a, b, c) r3t[((a) + 1) + n4 * (((b) + 1) + n4 * ((c) + 1))]
     for (int64_t k = 1; k <= nt; k++)
       for (int64_t j = 1; j <= nt; j++)
         for (int64_t i = 1; i <= nt; i++)
@@ -562,18 +584,21 @@ void orc_coarse_deposit(const orc_params* p, const int32_t* brhoc, const int64_t
 
 /* Coarse kick (pm.f90:322-387). force_c is (3,nc,nc,nc); the halo
    force_c(:,0,:,:)=force_c(:,nc,:,:) etc. (pm.f90:305-313) is applied as a
-   periodic wrap. vmax_out[3] receives max|vreal+vfield| per component. */
+   periodic wrap. vmax_out[3] receives max|vreal+vfield| per component;
+   vmax_signed (may be NULL) the neutrino loop's statistic
+   max(maxval(vreal+vfield_nu)), signed, over the components (pm.f90:377). */
 void orc_coarse_kick(const orc_params* p, float a_mid, float dt, float sigma_vi, const int32_t* brhoc,
                      const int64_t* bstart, const float* bvfield, const void* bxp, void* bvp,
-                     const float* force_c, float* vmax_out) {
+                     const float* force_c, float* vmax_out, double* vmax_signed) {
   int64_t nt = p->nt, nnt = p->nnt, nc = p->nc;
   double c = vcoef(sigma_vi);
   double vm[3] = {0, 0, 0};
+  double vs = 0; /* vmax_nu starts at 0 (pm.f90:39) */
   set_threads(p);
   for (int64_t t = 0; t < nnt * nnt * nnt; t++) {
     int64_t tl[3] = {t % nnt, (t / nnt) % nnt, t / (nnt * nnt)};
-    double v0 = 0, v1 = 0, v2 = 0;
-#pragma omp parallel for schedule(static, 2) reduction(max : v0, v1, v2)
+    double v0 = 0, v1 = 0, v2 = 0, vsg = vs;
+#pragma omp parallel for schedule(static, 2) reduction(max : v0, v1, v2, vsg)
     for (int64_t k = 1; k <= nt; k++)
       for (int64_t j = 1; j <= nt; j++)
         for (int64_t i = 1; i <= nt; i++) {
@@ -604,7 +629,9 @@ void orc_coarse_kick(const orc_params* p, float a_mid, float dt, float sigma_vi,
               vr = vr + (double)kick_term(FC(d, i2[0], i1[1], i2[2]), a_mid, dt, d2[0], d1[1], d2[2]);
               vr = vr + (double)kick_term(FC(d, i2[0], i2[1], i1[2]), a_mid, dt, d2[0], d2[1], d1[2]);
               vr = vr + (double)kick_term(FC(d, i2[0], i2[1], i2[2]), a_mid, dt, d2[0], d2[1], d2[2]);
-              double a = fabs(vr + (double)bvfield[3 * e + d]);
+              double sv = vr + (double)bvfield[3 * e + d];
+              double a = fabs(sv);
+              if (sv > vsg) vsg = sv;
               if (d == 0 && a > v0) v0 = a;
               if (d == 1 && a > v1) v1 = a;
               if (d == 2 && a > v2) v2 = a;
@@ -613,11 +640,13 @@ void orc_coarse_kick(const orc_params* p, float a_mid, float dt, float sigma_vi,
 #undef FC
           }
         }
+    vs = vsg;
     if (v0 > vm[0]) vm[0] = v0;
     if (v1 > vm[1]) vm[1] = v1;
     if (v2 > vm[2]) vm[2] = v2;
   }
   for (int d = 0; d < 3; d++) vmax_out[d] = (float)vm[d];
+  if (vmax_signed) *vmax_signed = vs;
 }
 
 /* ------------------------------------------------------------------- PP */
@@ -626,7 +655,7 @@ void orc_coarse_kick(const orc_params* p, float a_mid, float dt, float sigma_vi,
    in the reference's FP64.  out[0]=f2_max_pp (as real(4)), out[1]=npairs,
    out[2]=itest1 (particles updated). */
 void orc_pp_force(const orc_params* p, float a_mid, float dt, float sigma_vi, const int32_t* brhoc,
-                  const int64_t* bstart, const void* bxp, void* bvp, double* out) {
+                  const int64_t* bstart, const void* bxp, void* bvp, double* out, double* fout) {
   int64_t nt = p->nt, nnt = p->nnt, ncell = p->ncell, nft = nt * ncell;
   int64_t pr = p->pp_range;
   int64_t nh = nft + 2 * ncell; /* hoc(1-ncell:nft+ncell)^3 */
@@ -712,6 +741,8 @@ void orc_pp_force(const orc_params* p, float a_mid, float dt, float sigma_vi, co
                     ipll2 = ll[ipll2];
                   }
                 }
+            if (fout)  /* f_tot of this particle, by buffered index (a checking output) */
+              for (int d = 0; d < 3; d++) fout[3 * ip1 + d] = ftot[d];
             for (int d = 0; d < 3; d++) {
               double kick = (((ftot[d] * (double)a_mid) * (double)dt) / 6.0) / (double)PI_F;
               vr[d] = vr[d] + kick;

@@ -61,12 +61,12 @@ def lib():
         _lib.orc_update_xp.restype = ctypes.c_int64
         _lib.orc_update_xp.argtypes = [P, ctypes.c_float, ctypes.c_float, ctypes.c_float] + [P] * 13
         _lib.orc_sigma_sums.argtypes = [P, ctypes.c_float, P, P, P, P]
-        _lib.orc_fine_deposit.argtypes = [P, ctypes.c_int64, P, P, P, P]
+        _lib.orc_fine_deposit.argtypes = [P, ctypes.c_int64, P, P, P, P, P, P, P, P]
         _lib.orc_fine_kick.argtypes = [P, ctypes.c_int64, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                        ctypes.c_float, P, P, P, P, P]
-        _lib.orc_coarse_deposit.argtypes = [P, P, P, P, P]
-        _lib.orc_coarse_kick.argtypes = [P, ctypes.c_float, ctypes.c_float, ctypes.c_float] + [P] * 7
-        _lib.orc_pp_force.argtypes = [P, ctypes.c_float, ctypes.c_float, ctypes.c_float] + [P] * 5
+        _lib.orc_coarse_deposit.argtypes = [P, P, P, P, P, P, P, P, P]
+        _lib.orc_coarse_kick.argtypes = [P, ctypes.c_float, ctypes.c_float, ctypes.c_float] + [P] * 8
+        _lib.orc_pp_force.argtypes = [P, ctypes.c_float, ctypes.c_float, ctypes.c_float] + [P] * 6
     return _lib
 
 
@@ -284,14 +284,33 @@ class OracleImage:
                          nlayer=2 * int(np.ceil(q)) + 1)
         return self.last
 
+    def physical_slots(self):
+        """Buffered index of every particle of the disjoint state, in storage
+        order (the walk of orc_unbuffer: tile, cell x fastest, rank)."""
+        p = self.p
+        nt, ncb, nte = p.nt, p.ncb, p.nt + 2 * p.ncb
+        t = np.arange(p.nnt ** 3)
+        c = np.arange(nt)
+        T, K, J, I = np.meshgrid(t, c, c, c, indexing="ij")
+        e = ((I + ncb) + nte * ((J + ncb) + nte * ((K + ncb) + nte * T))).ravel()
+        cnt = self.brhoc[e].astype(np.int64)
+        first = np.repeat(self.bstart[e] - np.cumsum(cnt) + cnt, cnt)
+        return first + np.arange(int(cnt.sum()))
+
     # ---- PP
-    def pp_force(self, a_mid, dt):
-        """ext_pp_force (ext_pp_force.f90:10-162), FP64 pair sums."""
+    def pp_force(self, a_mid, dt, want_force=False):
+        """ext_pp_force (ext_pp_force.f90:10-162), FP64 pair sums.  With
+        want_force the result carries f_tot of every particle, (np, 3) float64
+        in storage order, under "f_tot"."""
         out = np.zeros(3, np.float64)
+        fb = np.zeros((self.bxp.shape[0], 3), np.float64) if want_force else None
         lib().orc_pp_force(ctypes.byref(self.op), float(np.float32(a_mid)), float(np.float32(dt)),
                            float(self.sigma_vi), _p(self.brhoc), _p(self.bstart), _p(self.bxp), _p(self.bvp),
-                           _p(out))
-        return dict(f2_max_pp=np.float32(out[0]), npairs=int(out[1]), itest1=int(out[2]))
+                           _p(out), _p(fb))
+        r = dict(f2_max_pp=np.float32(out[0]), npairs=int(out[1]), itest1=int(out[2]))
+        if want_force:
+            r["f_tot"] = fb[self.physical_slots()]
+        return r
 
     # ---- PM
     def kern_f(self):
@@ -305,11 +324,15 @@ class OracleImage:
             self._kc = kernel_c(self.p.nc, self.p.ncell)
         return self._kc
 
-    def fine_density(self, tile):
+    def fine_density(self, tile, nu=None):
+        """Fine CIC density of one tile's nfe^3 box; nu (an OracleImage of
+        the second species, same geometry) deposits each cell's neutrinos
+        after its CDM particles into the same box (pm.f90:52-107)."""
         p = self.p
         rho = np.zeros((p.nfe, p.nfe, p.nfe), np.float32)  # [k, j, i]
+        q = (ctypes.byref(nu.op), _p(nu.brhoc), _p(nu.bstart), _p(nu.bxp)) if nu is not None else (None,) * 4
         lib().orc_fine_deposit(ctypes.byref(self.op), tile, _p(self.brhoc), _p(self.bstart), _p(self.bxp),
-                               _p(rho))
+                               _p(rho), *q)
         return rho
 
     def fine_force(self, rho):
@@ -351,16 +374,17 @@ class OracleImage:
         for t in range(self.p.nnt ** 3):
             self.fine_kick(t, self.tile_box(field_global, t), a_mid, dt)
 
-    def global_fine_force(self):
+    def global_fine_force(self, nu=None):
         """Physical regions of every tile's force box assembled on the global
-        periodic fine mesh (3,nf,nf,nf), plus the fine density."""
+        periodic fine mesh (3,nf,nf,nf), plus the fine density; nu adds the
+        second species' mass (fine_density)."""
         p = self.p
         nf, nft, nnt, nfb = p.nf, p.nft, p.nnt, p.nfb
         F = np.zeros((3, nf, nf, nf), np.float32)
         R = np.zeros((nf, nf, nf), np.float32)
         for t in range(nnt ** 3):
             tx, ty, tz = t % nnt, (t // nnt) % nnt, t // (nnt * nnt)
-            rho = self.fine_density(t)
+            rho = self.fine_density(t, nu)
             box = self.fine_force(rho)
             F[:, tz * nft:(tz + 1) * nft, ty * nft:(ty + 1) * nft, tx * nft:(tx + 1) * nft] = \
                 box[:, 1:nft + 1, 1:nft + 1, 1:nft + 1]
@@ -368,10 +392,13 @@ class OracleImage:
                 rho[nfb:nfb + nft, nfb:nfb + nft, nfb:nfb + nft]
         return F, R
 
-    def coarse_density(self):
+    def coarse_density(self, nu=None):
+        """Coarse CIC density of the image; nu as in fine_density
+        (pm.f90:205-267)."""
         p = self.p
         r3 = np.zeros((p.nc, p.nc, p.nc), np.float32)
-        lib().orc_coarse_deposit(ctypes.byref(self.op), _p(self.brhoc), _p(self.bstart), _p(self.bxp), _p(r3))
+        q = (ctypes.byref(nu.op), _p(nu.brhoc), _p(nu.bstart), _p(nu.bxp)) if nu is not None else (None,) * 4
+        lib().orc_coarse_deposit(ctypes.byref(self.op), _p(self.brhoc), _p(self.bstart), _p(self.bxp), _p(r3), *q)
         return r3
 
     def coarse_force(self, r3):
@@ -385,13 +412,17 @@ class OracleImage:
             out[d] = ((f / np.float32(nc)) / np.float32(nc)) / np.float32(nc)
         return out
 
-    def coarse_kick(self, force_c, a_mid, dt):
+    def coarse_kick(self, force_c, a_mid, dt, signed=False):
+        """Coarse kick; returns vmax(3) = max|v + vfield| per component, and
+        with signed=True also the neutrino loop's signed statistic
+        max(maxval(v + vfield)) (pm.f90:349, 377)."""
         fc = np.ascontiguousarray(np.transpose(force_c, (1, 2, 3, 0)))
         vmax = np.zeros(3, np.float32)
+        vs = np.zeros(1, np.float64)
         lib().orc_coarse_kick(ctypes.byref(self.op), float(np.float32(a_mid)), float(np.float32(dt)),
                               float(self.sigma_vi), _p(self.brhoc), _p(self.bstart), _p(self.bvfield),
-                              _p(self.bxp), _p(self.bvp), _p(fc), _p(vmax))
-        return vmax
+                              _p(self.bxp), _p(self.bvp), _p(fc), _p(vmax), _p(vs))
+        return (vmax, float(vs[0])) if signed else vmax
 
     def particle_mesh(self, a_mid, dt, keep_fields=False):
         """particle_mesh (pm.f90:2-415) without the dt bookkeeping."""
@@ -422,6 +453,46 @@ class OracleImage:
         self.fields = fields
         self.buffer_v()
         return dict(f2_max_fine=f2f, f2_max_coarse=f2c, vmax=vmax, testrhof=testrhof, testrhoc=testrhoc)
+
+    def particle_mesh2(self, nu, a_mid, dt, keep_fields=False):
+        """particle_mesh (pm.f90:2-415) with CUBEnu's second species: nu (an
+        OracleImage with its own izipx/izipv, mass and sigma) deposits into the
+        same fine and coarse meshes, both species are kicked by the same
+        forces with their own codes.  Returns (stats, nu stats); the nu
+        stats carry vmax per component and the reference's signed
+        vmax_nu (pm.f90:377)."""
+        p = self.p
+        f2f = np.float32(0)
+        testrhof = 0.0
+        fields = {}
+        nfb, nft = p.nfb, p.nft
+        for t in range(p.nnt ** 3):
+            rho = self.fine_density(t, nu)
+            testrhof += float(np.sum(rho[nfb:nft + nfb, nfb:nft + nfb, nfb:nft + nfb], dtype=np.float64))
+            force = self.fine_force(rho)
+            f2 = ((force[0] * force[0] + force[1] * force[1]) + force[2] * force[2]).max()
+            f2f = max(f2f, np.float32(f2))
+            if keep_fields:
+                fields[("rho_f", t)] = rho
+                fields[("force_f", t)] = force
+            self.fine_kick(t, force, a_mid, dt)
+            nu.fine_kick(t, force, a_mid, dt)
+        self.sigma_vi = self.sigma_vi_new  # pm.f90:193-194
+        nu.sigma_vi = nu.sigma_vi_new
+        r3 = self.coarse_density(nu)
+        testrhoc = float(np.sum(r3, dtype=np.float64))
+        fc = self.coarse_force(r3)
+        f2c = np.float32(((fc[0] * fc[0] + fc[1] * fc[1]) + fc[2] * fc[2]).max())
+        vmax = self.coarse_kick(fc, a_mid, dt)
+        vmax_nu, vsigned = nu.coarse_kick(fc, a_mid, dt, signed=True)
+        if keep_fields:
+            fields["rho_c"] = r3
+            fields["force_c"] = fc
+        self.fields = fields
+        self.buffer_v()
+        nu.buffer_v()
+        return (dict(f2_max_fine=f2f, f2_max_coarse=f2c, vmax=vmax, testrhof=testrhof, testrhoc=testrhoc),
+                dict(vmax=vmax_nu, vmax_signed=vsigned))
 
 
 def time_sample(params, state, sigma, a_mid, dt, dt_old, vz_max, tile=0, nthreads=0):

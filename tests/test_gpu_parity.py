@@ -292,3 +292,57 @@ def test_full_step_is_bitwise_deterministic():
     for k in a:
         np.testing.assert_array_equal(a[k], b[k])
     assert sa == sb
+
+
+PP_FORCE_RTOL = 1e-5  # relative L2 of the FP32 pair-force sums vs the oracle's FP64 f_tot
+
+
+@pytest.mark.parametrize("name,pk,sk", [
+    CASES[0], CASES[2], CASES[3],
+    ("dense_bricks", dict(nc=24, nnt=2, izipx=1, izipv=2), dict(mean_per_cell=3, seed=21, clump=2, clump_mult=1000)),
+], ids=["uniform_x1", "uniform_x2", "clumped", "dense_bricks"])
+def test_pp_force_vector_matches_fp64(name, pk, sk):
+    # f_tot of every particle (ext_pp_force.f90:94-112): the GPU sums FP32
+    # pair forces in 2^-32 fixed point, the oracle sums FP64 pair forces
+    p = _params(pk)
+    st = synth.random_state(p, **sk)
+    g, o = make_pair(p, st)
+    a = g.ext_pp_force(A_MID, DT)
+    b = o.pp_force(A_MID, DT, want_force=True)
+    assert a["npairs"] == b["npairs"]
+    Fg = g.get_field(C.FIELD_FORCE_PP).astype(np.float64)
+    Fo = b["f_tot"]
+    err = rel_l2(Fg, Fo)
+    mag = np.sqrt((Fo ** 2).sum(1))
+    big = mag > 1e-3 * mag.max()
+    worst = float(np.max(np.sqrt(((Fg - Fo) ** 2).sum(1))[big] / mag[big]))
+    print("PP force vs FP64 (%s): rel-L2 %.3e, worst particle %.3e" % (name, err, worst))
+    assert err < PP_FORCE_RTOL
+    assert worst < 1e-4
+    g.close()
+
+
+def test_resort_buffers_after_a_failed_allocation():
+    # host-side fault injection: the second of the general re-sort's four
+    # buffers reports failure on first use; the step returns CUBE_ERR_NOMEM
+    # with nothing launched on the half-made buffers, and the next step makes
+    # all four and gives the state of a context that never failed
+    p = _params(CASES[0][1])
+    st = synth.random_state(p, **CASES[0][2])
+    outs = []
+    for inject in (False, True):
+        g = C.CubeGPU(p)
+        g.upload(st["xp"], st["vp"], st["pid"], st["rhoc"], st["vfield"])
+        g.set_sigma(st["sigma_vi"], st["sigma_vi"])
+        g.set_option(C.OPT_RANK_WALK, 2)
+        if inject:
+            g.set_option(C.OPT_FAIL_ALLOC, 2)
+            with pytest.raises(C.CubeError) as e:
+                g.update_x(np.float32(28.0), np.float32(40.0), st["vz_max"])
+            assert e.value.code == 9  # CUBE_ERR_NOMEM
+        s = g.update_x(np.float32(28.0), np.float32(40.0), st["vz_max"])
+        assert s["rank_walked"] == 2
+        outs.append(g.download())
+        g.close()
+    for k in ("xp", "vp", "pid", "rhoc", "vfield"):
+        np.testing.assert_array_equal(outs[0][k], outs[1][k])

@@ -298,3 +298,64 @@ def test_power_spectrum_single_mode_known_answer():
     other = np.delete(xi[:, 2], k0 - 1)
     assert np.all(np.abs(other) < 1e-12)
     assert abs(xi[k0 - 1, 1] * box / (2 * float(O.PI_F)) - k0) < 0.5
+
+
+def test_pp_force_output_known_answer():
+    # the per-particle f_tot the oracle reports (storage order) is the pair
+    # force of the two-particle setup above, opposite on the two particles
+    p = one_tile(nc=24)
+    st = state_from(p, [(5, 5, 5), (5, 5, 5)], [[-128, 0, 0], [-64, 0, 0]], [[0, 0, 0], [0, 0, 0]])
+    img = O.OracleImage(p)
+    img.load(**st)
+    img.sigma_vi = img.sigma_vi_new = np.float32(0.05)
+    out = img.pp_force(np.float32(0.5), np.float32(0.02), want_force=True)
+    f = 8.0 * (1 - 1.75 * (1 / 16) ** 3 + 0.75 * (1 / 16) ** 5)
+    ft = out["f_tot"]
+    assert ft.shape == (2, 3)
+    np.testing.assert_allclose(sorted(ft[:, 0]), [-f, f], rtol=1e-12)
+    assert np.all(ft[:, 1:] == 0)
+
+
+def test_physical_slots_follow_the_storage_order():
+    # the buffered index of every stored particle: gathering the buffered
+    # codes through it gives the disjoint state back
+    p = P.small(nc=24, nnt=2)
+    st = synth.random_state(p, seed=31, clump=5)
+    img = O.OracleImage(p)
+    img.load(st["xp"], st["vp"], st["pid"], st["rhoc"], st["vfield"])
+    s = img.physical_slots()
+    assert s.shape[0] == st["xp"].shape[0]
+    np.testing.assert_array_equal(img.bxp[s], st["xp"])
+    np.testing.assert_array_equal(img.bpid[s], st["pid"])
+
+
+def test_second_species_deposit_equals_one_species_split():
+    # pm.f90:52-107 / 205-267 with NEUTRINOS: the second species deposits into
+    # the same mesh after each cell's first-species particles.  Splitting one
+    # species' particles between two images of equal mass and format gives the
+    # single-species density up to the FP32 order of the sums.
+    p = P.small(nc=24, nnt=2)
+    st = synth.random_state(p, mean_per_cell=5, seed=32, clump=4)
+    cnt = st["rhoc"].astype(np.int64)
+    start = np.concatenate([[0], np.cumsum(cnt)[:-1]])
+    na = (cnt + 1) // 2
+    rank = np.arange(cnt.sum()) - np.repeat(start, cnt)
+    ina = rank < np.repeat(na, cnt)
+    one, a, b = O.OracleImage(p), O.OracleImage(p), O.OracleImage(p)
+    one.load(st["xp"], st["vp"], st["pid"], st["rhoc"], st["vfield"])
+    a.load(st["xp"][ina], st["vp"][ina], st["pid"][ina], na.astype(np.int32), st["vfield"])
+    b.load(st["xp"][~ina], st["vp"][~ina], st["pid"][~ina], (cnt - na).astype(np.int32), st["vfield"])
+    for t in (0, 7):
+        r1, r2 = one.fine_density(t), a.fine_density(t, nu=b)
+        assert np.linalg.norm(r2 - r1) <= 1e-6 * np.linalg.norm(r1)
+    c1, c2 = one.coarse_density(), a.coarse_density(nu=b)
+    assert np.linalg.norm(c2 - c1) <= 1e-6 * np.linalg.norm(c1)
+    # and a second species of another mass adds its own mass to the total
+    q = P.small(nc=24, nnt=2, izipx=2, izipv=2)
+    q.mass_p = 0.25
+    nu = synth.random_state(q, mean_per_cell=3, seed=33)
+    bn = O.OracleImage(q)
+    bn.load(nu["xp"], nu["vp"], nu["pid"], nu["rhoc"], nu["vfield"])
+    tot = float(a.coarse_density(nu=bn).sum(dtype=np.float64))
+    want = float(a.coarse_density().sum(dtype=np.float64)) + 0.25 * nu["xp"].shape[0]
+    assert abs(tot - want) <= 1e-5 * want

@@ -38,6 +38,27 @@ def test_static_scratch_codec_check_matches_allocating_entry_point():
         g.close()
 
 
+def test_static_scratch_codec_check_allocates_nothing():
+    # after one warm call (the array's address, the kernels' first loads),
+    # calls of several sizes and sigmas leave the device's free memory as it was
+    torch = pytest.importorskip("torch")
+    p = P.CubeParams(nc=24, nnt=2, pp_on=True)
+    g = C.CubeGPU(p)
+    rng = np.random.default_rng(7)
+    try:
+        g.codec_check_static(np.float32(0.02), _velocities(rng, 64, 0.02))
+        g.synchronize()
+        free0 = torch.cuda.mem_get_info(0)[0]
+        for n, sigma in ((1, 0.011), (C.CODEC_STATIC_MAX, 0.017), (777, 0.029), (C.CODEC_STATIC_MAX // 2, 0.017)):
+            s = np.float32(sigma)
+            d, t = g.codec_check_static(s, _velocities(rng, n, s))
+            np.testing.assert_array_equal(t, d)
+        g.synchronize()
+        assert torch.cuda.mem_get_info(0)[0] == free0
+    finally:
+        g.close()
+
+
 def test_static_scratch_codec_check_rejects_oversize():
     p = P.CubeParams(nc=24, nnt=2, pp_on=True)
     g = C.CubeGPU(p)
