@@ -35,7 +35,7 @@ def _stale(objs):
     if not os.path.exists(LIB):
         return True
     t = os.path.getmtime(LIB)
-    deps = [os.path.join(SRC, f) for f in os.listdir(SRC)]
+    deps = [os.path.join(SRC, f) for f in os.listdir(SRC)] + [os.path.join(HERE, "host", "cube_main.cpp")]
     deps.append(os.path.join(HERE, "..", "include", "cube_gpu.h"))
     deps.append(os.path.abspath(__file__))
     return any(os.path.getmtime(d) > t for d in deps)
@@ -45,6 +45,8 @@ def build(force=False, verbose=False, extra=()):
     os.makedirs(OUT, exist_ok=True)
     objs = [os.path.join(OUT, s.replace(".cu", ".o")) for s in SOURCES]
     if not force and not _stale(objs):
+        if not os.path.exists(DRIVER):
+            build_driver()
         return LIB
     cc = nvcc()
 
@@ -69,7 +71,26 @@ def build(force=False, verbose=False, extra=()):
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
     os.replace(tmp, LIB)
+    build_driver()
     return LIB
+
+
+DRIVER_SRC = os.path.join(HERE, "host", "cube_main.cpp")
+DRIVER = os.path.join(OUT, "cube_main")
+
+
+def build_driver():
+    """The compiled driver (host/cube_main.cpp): CUBE's step loop calling the
+    library through include/cube_gpu.h, linked against the in-tree .so."""
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+    tmp = DRIVER + ".tmp%d" % os.getpid()
+    cmd = [cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-I" + os.path.join(HERE, "..", "include"), DRIVER_SRC,
+           "-L" + OUT, "-lcube_gb300", "-Wl,-rpath,$ORIGIN", "-o", tmp]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("driver build failed:\n" + r.stdout + r.stderr)
+    os.replace(tmp, DRIVER)
+    return DRIVER
 
 
 if __name__ == "__main__":
