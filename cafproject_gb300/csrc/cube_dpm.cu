@@ -34,8 +34,12 @@
 // start of every segment of ckpt_every steps; the backward pass re-runs each
 // segment forward, keeping its post-drift positions and potentials, and then
 // walks it in reverse.  The forward and backward passes are
-// each one captured CUDA graph (rebuilt when the schedule changes); the
-// deposits use FP32 global atomics, so results agree run to run to rounding.
+// each one captured CUDA graph (rebuilt when the schedule changes).  Both
+// scatters -- the CIC deposit and the adjoint's stencil scatter -- sum in
+// 64-bit fixed point (integer atomics, exact and order-independent) and are
+// converted to FP32 once, so every pass gives the same bits run to run.  The
+// deposit's scale follows from the mass and particle count; the stencil
+// scatter's from the largest velocity cotangent, reduced on the device first.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -65,6 +69,9 @@ struct cube_dpm {
   float* filt = nullptr;   // (npd/2+1) npd^2, 1/npd^3 folded in
   float* mesh = nullptr;   // padded ng^3: rho / phi
   float* adj = nullptr;    // padded ng^3: phibar / rhobar
+  long long* fix = nullptr;  // ng^3 fixed-point sums of the scatters (zero between uses)
+  unsigned int* gmax = nullptr;  // device: max |gv| (float bits) for the stencil scatter's scale
+  int dep_shift = 0;       // the deposit's fixed point: value = integer * 2^-dep_shift
   float* lat = nullptr;    // padded npd^3: noise / IC potential / their adjoints
   float *x = nullptr, *v = nullptr, *gx = nullptr, *gv = nullptr;
   float* seg = nullptr;    // segment starts: nseg x (x, v)
@@ -134,20 +141,66 @@ __device__ __forceinline__ void stencil_load(const float* __restrict__ m, int ng
       s.hi[2][a][b] = __ldg(m + pad_at(ng, c.i[0][1 + b], c.i[1][1 + a], c.i[2][3]));
     }
 }
-__device__ __forceinline__ void stencil_add(float* __restrict__ m, int ng, const Cic& c, const Stencil& s) {
+// dense index of the fixed-point sums
+__device__ __forceinline__ int64_t dense_at(int n, int x, int y, int z) { return x + (int64_t)n * (y + (int64_t)n * z); }
+// add v * 2^sh, rounded to an integer, to a fixed-point sum (two's complement
+// in an unsigned 64-bit atomic: the total is exact and independent of order)
+__device__ __forceinline__ void fix_add(long long* m, int64_t i, float v, float scale) {
+  atomicAdd(reinterpret_cast<unsigned long long*>(m) + i, (unsigned long long)__float2ll_rn(v * scale));
+}
+__device__ __forceinline__ void stencil_add(long long* __restrict__ m, int ng, const Cic& c, const Stencil& s,
+                                            float scale) {
 #pragma unroll
   for (int a = 0; a < 2; a++)
 #pragma unroll
     for (int b = 0; b < 2; b++) {
 #pragma unroll
-      for (int x = 0; x < 2; x++) atomicAdd(m + pad_at(ng, c.i[0][1 + x], c.i[1][1 + b], c.i[2][1 + a]), s.core[a][b][x]);
-      atomicAdd(m + pad_at(ng, c.i[0][0], c.i[1][1 + b], c.i[2][1 + a]), s.lo[0][a][b]);
-      atomicAdd(m + pad_at(ng, c.i[0][3], c.i[1][1 + b], c.i[2][1 + a]), s.hi[0][a][b]);
-      atomicAdd(m + pad_at(ng, c.i[0][1 + b], c.i[1][0], c.i[2][1 + a]), s.lo[1][a][b]);
-      atomicAdd(m + pad_at(ng, c.i[0][1 + b], c.i[1][3], c.i[2][1 + a]), s.hi[1][a][b]);
-      atomicAdd(m + pad_at(ng, c.i[0][1 + b], c.i[1][1 + a], c.i[2][0]), s.lo[2][a][b]);
-      atomicAdd(m + pad_at(ng, c.i[0][1 + b], c.i[1][1 + a], c.i[2][3]), s.hi[2][a][b]);
+      for (int x = 0; x < 2; x++) fix_add(m, dense_at(ng, c.i[0][1 + x], c.i[1][1 + b], c.i[2][1 + a]), s.core[a][b][x], scale);
+      fix_add(m, dense_at(ng, c.i[0][0], c.i[1][1 + b], c.i[2][1 + a]), s.lo[0][a][b], scale);
+      fix_add(m, dense_at(ng, c.i[0][3], c.i[1][1 + b], c.i[2][1 + a]), s.hi[0][a][b], scale);
+      fix_add(m, dense_at(ng, c.i[0][1 + b], c.i[1][0], c.i[2][1 + a]), s.lo[1][a][b], scale);
+      fix_add(m, dense_at(ng, c.i[0][1 + b], c.i[1][3], c.i[2][1 + a]), s.hi[1][a][b], scale);
+      fix_add(m, dense_at(ng, c.i[0][1 + b], c.i[1][1 + a], c.i[2][0]), s.lo[2][a][b], scale);
+      fix_add(m, dense_at(ng, c.i[0][1 + b], c.i[1][1 + a], c.i[2][3]), s.hi[2][a][b], scale);
     }
+}
+
+// The stencil scatter's fixed point: every value it adds is at most
+// 0.5*|kick|*max|gv| and a mesh point receives at most 32 of them from each of
+// np particles, so sums stay below 2^61 with scale 2^sh, sh = 60 - ilogb(16 *
+// |kick| * np * max|gv|).  Derived on the device from the reduced maximum.
+__device__ __forceinline__ int adj_shift(float kick, int64_t np, const unsigned int* gmax) {
+  const float g = __uint_as_float(*gmax);
+  if (!(g > 0.f)) return 0;
+  const double bound = 16.0 * (double)fabsf(kick) * (double)np * (double)g;
+  return 60 - ilogb(bound);
+}
+// 2^sh as a float (sh within the float exponent range)
+__device__ __forceinline__ float pow2f(int sh) { return ldexpf(1.0f, max(-126, min(127, sh))); }
+
+// max |gv| over the particles (float bits, non-negative: integer max orders them)
+__global__ void k_dpm_absmax(const float* __restrict__ v, int64_t n, unsigned int* __restrict__ out) {
+  float m = 0.f;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    m = fmaxf(m, fabsf(v[i]));
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
+}
+
+// fixed-point sums -> the padded FP32 mesh, zeroing the sums for their next use;
+// sh = the scatter's shift (from the host, or from adj_shift when gmax is set)
+__global__ void k_dpm_fix_out(long long* __restrict__ fix, int ng, int sh, float kick, int64_t np,
+                              const unsigned int* __restrict__ gmax, float* __restrict__ mesh) {
+  if (gmax) sh = adj_shift(kick, np, gmax);
+  const int64_t n = (int64_t)ng * ng * ng;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const long long q = fix[i];
+    fix[i] = 0;
+    const int x = (int)(i % ng);
+    const int64_t yz = i / ng;
+    // integer -> nearest float, then the exact power-of-two scale
+    mesh[x + (int64_t)(ng + 2) * yz] = ldexpf(__ll2float_rn(q), -sh);
+  }
 }
 
 // the central-difference force component d at corner (ax, ay, az) is
@@ -169,8 +222,8 @@ __device__ __forceinline__ float& minus_ref(Stencil& s, int d, int ax, int ay, i
 // (dout may be din: each thread reads its particle before writing it)
 __global__ void __launch_bounds__(256) k_dpm_deposit(const float* xin, const float* __restrict__ vin, float drift,
                                                      int64_t np, Lattice L, float mass, float* xout,
-                                                     float* __restrict__ pos,
-                                                     float* __restrict__ rho) {
+                                                     float* __restrict__ pos, long long* __restrict__ fix,
+                                                     float scale) {
   const int ng = L.ng;
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np; p += (int64_t)gridDim.x * blockDim.x) {
     float x[3];
@@ -192,8 +245,8 @@ __global__ void __launch_bounds__(256) k_dpm_deposit(const float* xin, const flo
       for (int ay = 0; ay < 2; ay++)
 #pragma unroll
         for (int ax = 0; ax < 2; ax++)
-          atomicAdd(rho + pad_at(ng, c.i[0][1 + ax], c.i[1][1 + ay], c.i[2][1 + az]),
-                    mass * (c.w[0][ax] * c.w[1][ay] * c.w[2][az]));
+          fix_add(fix, dense_at(ng, c.i[0][1 + ax], c.i[1][1 + ay], c.i[2][1 + az]),
+                  mass * (c.w[0][ax] * c.w[1][ay] * c.w[2][az]), scale);
   }
 }
 
@@ -253,8 +306,10 @@ __global__ void __launch_bounds__(256) k_dpm_kick(const float* __restrict__ x, f
 // differences
 __global__ void __launch_bounds__(256) k_dpm_kick_adj(const float* __restrict__ x, const float* __restrict__ gv,
                                                       int64_t np, Lattice L, const float* __restrict__ phi, float kick,
-                                                      float* __restrict__ gx, float* __restrict__ phibar) {
+                                                      float* __restrict__ gx, long long* __restrict__ phibar,
+                                                      const unsigned int* __restrict__ gmax) {
   const int ng = L.ng;
+  const float scale = pow2f(adj_shift(kick, np, gmax));
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np; p += (int64_t)gridDim.x * blockDim.x) {
     const float xp[3] = {x[3 * p], x[3 * p + 1], x[3 * p + 2]};
     const float g[3] = {kick * gv[3 * p], kick * gv[3 * p + 1], kick * gv[3 * p + 2]};
@@ -296,7 +351,7 @@ __global__ void __launch_bounds__(256) k_dpm_kick_adj(const float* __restrict__ 
         }
 #pragma unroll
     for (int e = 0; e < 3; e++) gx[3 * p + e] += gxp[e];
-    stencil_add(phibar, ng, c, b);
+    stencil_add(phibar, ng, c, b, scale);
   }
 }
 
@@ -401,15 +456,23 @@ int spectral(cube_dpm* d, float* m, const float* g, int n, cufftHandle r2c, cuff
   return CUBE_OK;
 }
 
+// fixed-point sums (zero on entry, zero again on return) -> the padded mesh
+int fix_out(cube_dpm* d, float* mesh, int sh, float kick = 0.f, const unsigned int* gmax = nullptr) {
+  cube_ctx* c = &d->base;
+  const int64_t n = (int64_t)d->ng * d->ng * d->ng;
+  k_dpm_fix_out<<<cube_grid(n, 256), 256, 0, c->stream>>>(d->fix, d->ng, sh, kick, d->np, gmax, mesh);
+  CUBE_CUDA(c, cudaGetLastError());
+  return CUBE_OK;
+}
+
 int deposit(cube_dpm* d, const float* xin, const float* vin, float drift, float* xout, float* pos,
             float* mesh = nullptr) {
   cube_ctx* c = &d->base;
   if (!mesh) mesh = d->mesh;
-  CUBE_CUDA(c, cudaMemsetAsync(mesh, 0, pad_bytes(d->ng), c->stream));
   k_dpm_deposit<<<cube_grid(d->np, 256), 256, 0, c->stream>>>(xin, vin, drift, d->np, d->lat_, d->mass, xout, pos,
-                                                               mesh);
+                                                               d->fix, std::ldexp(1.0f, d->dep_shift));
   CUBE_CUDA(c, cudaGetLastError());
-  return CUBE_OK;
+  return fix_out(d, mesh, d->dep_shift);
 }
 
 int nseg(const cube_dpm* d) { return (d->nsteps + d->p.ckpt_every - 1) / d->p.ckpt_every; }
@@ -467,9 +530,12 @@ int record_backward(cube_dpm* d) {
     for (int i = i1 - 1; i >= i0; i--) {
       const float* pos = d->pos + (size_t)(i - i0) * 3 * np;
       const float* phi = d->phis + (size_t)(i - i0) * (pad_bytes(d->ng) / sizeof(float));
-      CUBE_CUDA(c, cudaMemsetAsync(d->adj, 0, pad_bytes(d->ng), s));
-      k_dpm_kick_adj<<<cube_grid(np, 256), 256, 0, s>>>(pos, d->gv, np, d->lat_, phi, d->kick[i], d->gx, d->adj);
+      CUBE_CUDA(c, cudaMemsetAsync(d->gmax, 0, sizeof(unsigned int), s));
+      k_dpm_absmax<<<cube_grid(3 * np, 256, 4), 256, 0, s>>>(d->gv, 3 * np, d->gmax);
+      k_dpm_kick_adj<<<cube_grid(np, 256), 256, 0, s>>>(pos, d->gv, np, d->lat_, phi, d->kick[i], d->gx, d->fix,
+                                                         d->gmax);
       CUBE_CUDA(c, cudaGetLastError());
+      if ((r = fix_out(d, d->adj, 0, d->kick[i], d->gmax))) return r;
       if ((r = spectral(d, d->adj, d->green, d->ng, d->pm_r2c, d->pm_c2r))) return r;
       k_dpm_deposit_adj<<<cube_grid(np, 256), 256, 0, s>>>(pos, np, d->lat_, d->adj, d->mass, d->drift[i], d->gx, d->gv,
                                                             1);
@@ -513,7 +579,8 @@ void release(cube_dpm* d) {
   for (cufftHandle h : {d->pm_r2c, d->pm_c2r, d->ic_r2c, d->ic_c2r})
     if (h) cufftDestroy(h);
   for (void* b : {(void*)d->green, (void*)d->filt, (void*)d->mesh, (void*)d->adj, (void*)d->lat, (void*)d->x,
-                  (void*)d->v, (void*)d->gx, (void*)d->gv, (void*)d->seg, (void*)d->pos, (void*)d->phis})
+                  (void*)d->v, (void*)d->gx, (void*)d->gv, (void*)d->seg, (void*)d->pos, (void*)d->phis,
+                  (void*)d->fix, (void*)d->gmax})
     if (b) cudaFree(b);
   if (d->base.stream) cudaStreamDestroy(d->base.stream);
   d->base.stream = nullptr;
@@ -579,8 +646,13 @@ extern "C" int cube_dpm_create(const cube_dpm_params* p, const cube_cosmology* c
       (r = dalloc(d, &d->mesh, pad_bytes(d->ng))) || (r = dalloc(d, &d->adj, pad_bytes(d->ng))) ||
       (r = dalloc(d, &d->lat, pad_bytes(d->npd))) || (r = dalloc(d, &d->x, sb)) || (r = dalloc(d, &d->v, sb)) ||
       (r = dalloc(d, &d->gx, sb)) || (r = dalloc(d, &d->gv, sb)) || (r = dalloc(d, &d->seg, 2 * sb * ns)) ||
-      (r = dalloc(d, &d->pos, sb * p->ckpt_every)) || (r = dalloc(d, &d->phis, pad_bytes(d->ng) * p->ckpt_every)))
+      (r = dalloc(d, &d->pos, sb * p->ckpt_every)) || (r = dalloc(d, &d->phis, pad_bytes(d->ng) * p->ckpt_every)) ||
+      (r = dalloc(d, reinterpret_cast<float**>(&d->fix), sizeof(long long) * (size_t)d->ng * d->ng * d->ng)) ||
+      (r = dalloc(d, reinterpret_cast<float**>(&d->gmax), sizeof(unsigned int))))
     return r;
+  CUBE_CUDA(c, cudaMemsetAsync(d->fix, 0, sizeof(long long) * (size_t)d->ng * d->ng * d->ng, c->stream));
+  // deposit sums stay below 2^61: mass * np < 2^(ilogb + 1)
+  d->dep_shift = 60 - std::ilogb((double)d->mass * (double)d->np);
   if ((r = make_plan(d, &d->pm_r2c, d->ng, CUFFT_R2C)) || (r = make_plan(d, &d->pm_c2r, d->ng, CUFFT_C2R)) ||
       (r = make_plan(d, &d->ic_r2c, d->npd, CUFFT_R2C)) || (r = make_plan(d, &d->ic_c2r, d->npd, CUFFT_C2R)))
     return r;

@@ -476,6 +476,63 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
+// |h + l| of a float-float value as the bit pattern of a double, for
+// |l| <= 2^-20 |h|: bits of l below the double's last place are truncated,
+// so the pattern is within 2 units in the last place of |h + l| (callers add
+// 2^-49 |h| to their error bound).  *neg is the sign of h.  h + l = 0 gives
+// the pattern 0; otherwise returns false when h is zero, subnormal or not
+// finite, or l is not small against h.
+// Integer operations only: the conversion runs on no FP64 unit.
+__device__ __forceinline__ bool ff_abs_bits(float h, float l, long long* out, bool* neg) {
+  const unsigned int hb = __float_as_uint(h), eh = (hb >> 23) & 0xffu;
+  *neg = (hb >> 31) != 0u;
+  if ((hb << 1) == 0u && (__float_as_uint(l) << 1) == 0u) {
+    *out = 0;
+    *neg = false;
+    return true;
+  }
+  if (eh == 0u || eh == 0xffu) return false;
+  long long X = (long long)((hb & 0x7fffffu) | 0x800000u) << 29;  // |h| in units of 2^(eh-127-52)
+  const unsigned int lb = __float_as_uint(l), el = (lb >> 23) & 0xffu;
+  if (el == 0xffu) return false;
+  if (el != 0u) {  // a subnormal l is below the last place: dropped
+    const int sh = 29 + (int)el - (int)eh;
+    if (sh > 32) return false;
+    const long long ml = (long long)((lb & 0x7fffffu) | 0x800000u);
+    const long long add = sh >= 0 ? (ml << sh) : (sh > -25 ? (ml >> (-sh)) : 0);
+    X = (((lb >> 31) != 0u) != *neg) ? X - add : X + add;
+  }
+  int e = (int)eh - 127 + 1023;
+  if (X >= (1LL << 53)) {
+    X >>= 1;
+    e++;
+  } else if (X < (1LL << 52)) {
+    X <<= 1;
+    e--;
+  }
+  if (X < (1LL << 52) || X >= (1LL << 53)) return false;
+  *out = ((long long)e << 52) | (X & ((1LL << 52) - 1));
+  return true;
+}
+
+// dec (hi, lo) + t[0..n) as a float-float h + l: exact TwoSums of the running
+// high part, the low parts summed in FP32.  For the caller's error bound:
+// |(h + l) - (dec + sum t)| <= 73 * 2^-48 * M with M = |dec| + sum |t|
+// (returned; the low-part sum carries at most n + 1 roundings of 2^-24 of a
+// value below (n + 1) 2^-24 M).
+__device__ __forceinline__ void ff_sum_terms(float2 dd, const float* t, int n, float& h, float& l, float& M) {
+  h = dd.x;
+  l = dd.y;
+  M = fabsf(dd.x);
+  for (int i = 0; i < n; i++) {
+    float s, e;
+    two_sum(h, t[i], s, e);
+    h = s;
+    l = __fadd_rn(l, e);
+    M = __fadd_rn(M, fabsf(t[i]));
+  }
+}
+
 // Nearest float to the real t + lo, certified when every real within margin
 // of it rounds to the same float: its distance from rr stays below half an ulp
 // (a quarter ulp when rr is a power of two, where the spacing below halves).

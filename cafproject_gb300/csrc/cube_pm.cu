@@ -314,14 +314,20 @@ __device__ __forceinline__ float kick_tau(const KickArgs& a, int d) {
 
 // The kick velocity of the reference is the FP64 chain
 //   v = decode; v = v + t1; ...; v = v + t8       (pm.f90:145-153)
-// with t_i the real(4) CIC terms.  The fast path forms V_f = fl32(hi(decode) + S)
-// with S the FP32 sum of the terms; its distance from the reference value is
+// with t_i the real(4) CIC terms.  The fast path sums the terms in FP32 (S)
+// and adds S to the decode's float-float split (hi + lo) with one exact
+// TwoSum, giving V = vh + vl; its distance from the reference value is
 // bounded by
-//   gamma_7 sum|t_i| + 2^-24 (|decode| + |V_f|) + 9*2^-53 (|decode| + sum|t_i| + |V_f|)
-// (recursive-summation bound, gamma_7 = 7u/(1-7u), u = 2^-24; the decode table's
-// float hi is within half an ulp).  certify_abs keeps the code only when every
-// double inside that bound encodes to it; otherwise the lane runs the exact
-// chain, so the stored code is always the reference's.
+//   gamma_7 sum|t_i| + 2^-24 (|lo| + |e|) + 2^-48 |decode| + 8*2^-53 (|decode| + sum|t_i|)
+// (recursive-summation bound, gamma_7 = 7u/(1-7u), u = 2^-24; e the TwoSum
+// error; the last term the reference's own eight FP64 roundings), plus the
+// 2^-49 |vh| of the double pattern.  certify_abs keeps the code only when
+// every double inside that bound encodes to it.  A lane it does not certify
+// sums the terms in float-float too (bound 73*2^-48 (|decode| + sum|t_i|))
+// and tries again; only then does it run the exact chain, so the stored code
+// is always the reference's.  The coarse kick's vmax (pm.f90:349) is the
+// float nearest |fl64(v + vfield)|, certified from the same float-float
+// value, else from the exact chain.
 // kPre: the meshes hold force*a_mid*dt/6/pi already (k_f2max<true>)
 template <bool kFine, bool kPre>
 __global__ void __launch_bounds__(256, 4) k_kick(KickArgs a) {
@@ -378,29 +384,50 @@ __global__ void __launch_bounds__(256, 4) k_kick(KickArgs a) {
       t[7] = KT(c222, d2[0], d2[1], d2[2]);
 #undef KT
       int code = load_code(a.vp_in, 3 * p + d, g.izipv);
-      float dh = codec_decode_ff(a.cin, code).x;
+      const float2 dd = codec_decode_ff(a.cin, code);
       float S = t[0], T = fabsf(t[0]);
       for (int i = 1; i < 8; i++) {
         S = __fadd_rn(S, t[i]);
         T = __fadd_rn(T, fabsf(t[i]));
       }
-      float vf = __fadd_rn(dh, S);
-      long long vb = f2d_bits(vf), ab = vb & 0x7fffffffffffffffLL;
-      float E = 1.25f * (T * 4.76837158e-7f + (fabsf(dh) + fabsf(vf)) * 6.0e-8f + T * 1.0e-15f);
-      long long nc_ = 0;
-      bool ok = !a.exact_only && certify_abs(ab, E, a.cout, &nc_);
+      float vh, e1;
+      two_sum(dd.x, S, vh, e1);
+      float vl = __fadd_rn(dd.y, e1);
+      float E = 1.25f * (T * 4.2e-7f + (fabsf(dd.y) + fabsf(e1)) * 6.0e-8f + (fabsf(dd.x) + T + fabsf(vh)) * 1.0e-14f);
+      long long ab = 0, nc_ = 0;
+      bool neg = false;
+      bool ok = !a.exact_only && ff_abs_bits(vh, vl, &ab, &neg) && certify_abs(ab, E, a.cout, &nc_);
+      if (!ok && !a.exact_only) {  // the terms in float-float as well
+        float M;
+        ff_sum_terms(dd, t, 8, vh, vl, M);
+        E = 1.25f * (M * 2.6e-13f + fabsf(vh) * 2.0e-15f);
+        ok = ff_abs_bits(vh, vl, &ab, &neg) && certify_abs(ab, E, a.cout, &nc_);
+      }
       bool need_vmax = false;
       float vfd = 0.f;
       if (!kFine) {
         vfd = a.vfield[3 * cell + d];
-        float ub = (fabsf(vf) + E + fabsf(vfd)) * 1.000001f;
+        float ub = (fabsf(vh) + E + fabsf(vfd)) * 1.000001f;
         need_vmax = a.vmax_only || ub >= kick_tau(a, d);
+        if (ok && need_vmax) {
+          // |fl64(V + vfield)| to float: V + vfield in float-float, its bound
+          // the kick's plus the new low part's rounding and the FP64 rounding
+          float wh, e2;
+          two_sum(vh, vfd, wh, e2);
+          const float wl = __fadd_rn(vl, e2);
+          const float Ew = 1.25f * (E + (fabsf(vl) + fabsf(e2)) * 6.0e-8f + fabsf(wh) * 1.2e-16f);
+          float r;
+          if (round_certified(wh, wl, Ew, &r)) {
+            vm[d] = fmaxf(vm[d], fabsf(r));
+            need_vmax = false;
+          }
+        }
       } else if (a.vmax_est) {
-        vm[d] = fmaxf(vm[d], fabsf(__fadd_rn(vf, a.vfield[3 * cell + d])));
+        vm[d] = fmaxf(vm[d], fabsf(__fadd_rn(vh, a.vfield[3 * cell + d])));
       }
       long long out;
       if (ok && !need_vmax) {
-        out = vb < 0 ? -nc_ : nc_;
+        out = neg ? -nc_ : nc_;
       } else {
         // the reference's exact FP64 chain
         double v = codec_decode(a.cin, code);

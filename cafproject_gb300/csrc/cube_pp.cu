@@ -142,7 +142,7 @@ __device__ __forceinline__ float pp_store_force(const PPArgs& a, int64_t p, cons
 __global__ void __launch_bounds__(256) k_pp_kick(PPArgs a) {
   const Geo& g = a.g;
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.np; p += (int64_t)gridDim.x * blockDim.x) {
-    float F[3], vf[3], E[3];
+    float F[3], E[3];
     int code[3];
     long long ab[3], n[3];
     bool ok[3];
@@ -151,21 +151,28 @@ __global__ void __launch_bounds__(256) k_pp_kick(PPArgs a) {
       F[d] = a.fpp[3 * p + d];
       code[d] = load_code(a.vp, 3 * p + d, g.izipv);
     }
+    bool neg[3], split[3];
 #pragma unroll
     for (int d = 0; d < 3; d++) {
-      // vreal=vreal+f_tot*a_mid*dt/6/pi (ext_pp_force.f90:116), then the code
-      float dh = codec_decode_ff(a.cv, code[d]).x;
-      float kf = __fmul_rn(F[d], pp_kick_f(a));
-      vf[d] = __fadd_rn(dh, kf);
-      E[d] = 1.25f * (fabsf(kf) * 1.3e-7f + (2.f * fabsf(dh) + fabsf(vf[d])) * 6.0e-8f);
-      ab[d] = f2d_bits(vf[d]) & 0x7fffffffffffffffLL;
+      // vreal=vreal+f_tot*a_mid*dt/6/pi (ext_pp_force.f90:116), then the code:
+      // the kick added to the decode's float-float split with one TwoSum;
+      // bound: the kick's FP32 product, the low part's rounding, the split,
+      // the FP64 product and sum, and the double pattern's truncation
+      const float2 dd = codec_decode_ff(a.cv, code[d]);
+      const float kf = __fmul_rn(F[d], pp_kick_f(a));
+      float vh, e1;
+      two_sum(dd.x, kf, vh, e1);
+      const float vl = __fadd_rn(dd.y, e1);
+      E[d] = 1.25f * (fabsf(kf) * 1.3e-7f + (fabsf(dd.y) + fabsf(e1)) * 6.0e-8f + (fabsf(dd.x) + fabsf(vh)) * 1.0e-14f);
+      split[d] = ff_abs_bits(vh, vl, &ab[d], &neg[d]);
+      if (!split[d]) ab[d] = 0;
     }
     certify_abs3(ab, E, a.cv, n, ok);
 #pragma unroll
     for (int d = 0; d < 3; d++) {
       long long out;
-      if (!a.exact_only && ok[d]) {
-        out = vf[d] < 0.f ? -n[d] : n[d];
+      if (!a.exact_only && split[d] && ok[d]) {
+        out = neg[d] ? -n[d] : n[d];
       } else {
         out = pp_kick_exact(a.cv, code[d], F[d], pp_kick_d(a));
       }

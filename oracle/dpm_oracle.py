@@ -4,7 +4,11 @@ The same map as cafproject_gb300/csrc/cube_dpm.cu, written with torch
 float64 operations on the CPU so that autograd gives the FP64 reference
 gradient and central finite differences can be taken in FP64.  It takes the
 two spectral tables (IC filter, Green's function) as inputs, each with the
-inverse transform's 1/n^3 folded in, exactly as the device uses them.
+inverse transform's 1/n^3 folded in, exactly as the device uses them.  The
+functions run on the device of their inputs: a float64 noise tensor on a GPU
+makes the many forward passes of a finite-difference check affordable at the
+workload size (float64 scatters there are summed in varying order, a
+rounding of about 1e-16 relative).
 
 The form has no counterpart in the reference (CUBE has no gradients); its
 pieces restate the reference's step: the Zel'dovich initial conditions by
@@ -27,10 +31,10 @@ def _irfft3(spec, n):
     return torch.fft.irfftn(spec, s=(n, n, n))
 
 
-def lattice(npd, step):
+def lattice(npd, step, device=None):
     """(np, 3) integer mesh cell of each particle's lattice point, in the
     order l = x + npd*(y + npd*z); the point itself is that cell's centre."""
-    p = torch.arange(npd ** 3)
+    p = torch.arange(npd ** 3, device=device)
     return torch.stack([p % npd, (p // npd) % npd, p // (npd * npd)], 1) * step
 
 
@@ -39,7 +43,7 @@ def ic(noise, filt, npd, step, vf):
     phi = C2R(filt * R2C(noise)), gd = phi(l+e) - phi(l-e),
     d = -step*gd/(8 pi), v = -step*gd*vf/(8 pi)."""
     n3 = float(npd) ** 3
-    f = torch.as_tensor(filt, dtype=DT)
+    f = torch.as_tensor(filt, dtype=DT, device=noise.device)
     phi = _irfft3(torch.fft.rfftn(noise.reshape(npd, npd, npd)) * f, npd) * n3
     out_d, out_v = [], []
     for dim in (2, 1, 0):  # x is the last tensor dimension
@@ -54,7 +58,7 @@ def _corners(d, ng, npd):
     step = ng // npd
     fl = torch.floor(d).detach()
     f = d - fl
-    i0 = lattice(npd, step) + fl.long()
+    i0 = lattice(npd, step, d.device) + fl.long()
     for az in (0, 1):
         for ay in (0, 1):
             for ax in (0, 1):
@@ -69,14 +73,14 @@ def _corners(d, ng, npd):
 def deposit(d, ng, npd, mass):
     """CIC density on the cell-centred periodic ng^3 mesh, [z, y, x], of the
     particles at their lattice points plus displacements d."""
-    rho = torch.zeros(ng ** 3, dtype=d.dtype)
+    rho = torch.zeros(ng ** 3, dtype=d.dtype, device=d.device)
     for idx, w in _corners(d, ng, npd):
         rho = rho.index_add(0, idx, mass * w)
     return rho.reshape(ng, ng, ng)
 
 
 def potential(rho, green, ng):
-    return _irfft3(torch.fft.rfftn(rho) * torch.as_tensor(green, dtype=DT), ng) * float(ng) ** 3
+    return _irfft3(torch.fft.rfftn(rho) * torch.as_tensor(green, dtype=DT, device=rho.device), ng) * float(ng) ** 3
 
 
 def force_at(d, phi, ng, npd):
@@ -84,7 +88,7 @@ def force_at(d, phi, ng, npd):
     comps = []
     for dim in (2, 1, 0):
         comps.append((-(torch.roll(phi, -1, dim) - torch.roll(phi, 1, dim)) / 2).reshape(-1))
-    out = torch.zeros(d.shape[0], 3, dtype=d.dtype)
+    out = torch.zeros(d.shape[0], 3, dtype=d.dtype, device=d.device)
     for idx, w in _corners(d, ng, npd):
         out = out + w[:, None] * torch.stack([c[idx] for c in comps], 1)
     return out
