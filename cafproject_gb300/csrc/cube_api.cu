@@ -219,6 +219,8 @@ static int create_impl(const cube_params* p, const float* fine_table, const floa
     CUBE_CUDA(c, cudaStreamCreateWithFlags(&c->stream_pp, cudaStreamNonBlocking));
     CUBE_CUDA(c, cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
     CUBE_CUDA(c, cudaEventCreateWithFlags(&c->ev_pp, cudaEventDisableTiming));
+    int r = cube_pp_init(c);
+    if (r) return r;
   }
   {
     int nb = (p->nc + 3) / 4;

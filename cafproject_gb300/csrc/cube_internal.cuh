@@ -524,6 +524,7 @@ __device__ __forceinline__ void ff_sum_terms(float2 dd, const float* t, int n, f
   h = dd.x;
   l = dd.y;
   M = fabsf(dd.x);
+#pragma unroll
   for (int i = 0; i < n; i++) {
     float s, e;
     two_sum(h, t[i], s, e);
@@ -713,6 +714,7 @@ int cube_scan_counts(cube_ctx* c, const int32_t* counts, int64_t* starts, int64_
 int cube_update_x_impl(cube_ctx* c, float dt_old, float dt, float vz_max, cube_stats* st);
 int cube_pp_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st);
 int cube_pp_launch(cube_ctx* c, float a_mid, float dt);
+int cube_pp_init(cube_ctx* c);  // once per context: the staging kernels' shared-memory sizes
 int cube_pp_finish(cube_ctx* c, cube_stats* st);
 // density deposits; accumulate: add to the mesh (the linked species) instead of writing it
 int cube_fine_density_impl(cube_ctx* c, cube_stats* st, bool accumulate = false);

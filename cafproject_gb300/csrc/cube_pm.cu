@@ -314,20 +314,21 @@ __device__ __forceinline__ float kick_tau(const KickArgs& a, int d) {
 
 // The kick velocity of the reference is the FP64 chain
 //   v = decode; v = v + t1; ...; v = v + t8       (pm.f90:145-153)
-// with t_i the real(4) CIC terms.  The fast path sums the terms in FP32 (S)
-// and adds S to the decode's float-float split (hi + lo) with one exact
-// TwoSum, giving V = vh + vl; its distance from the reference value is
-// bounded by
-//   gamma_7 sum|t_i| + 2^-24 (|lo| + |e|) + 2^-48 |decode| + 8*2^-53 (|decode| + sum|t_i|)
-// (recursive-summation bound, gamma_7 = 7u/(1-7u), u = 2^-24; e the TwoSum
-// error; the last term the reference's own eight FP64 roundings), plus the
-// 2^-49 |vh| of the double pattern.  certify_abs keeps the code only when
-// every double inside that bound encodes to it.  A lane it does not certify
-// sums the terms in float-float too (bound 73*2^-48 (|decode| + sum|t_i|))
-// and tries again; only then does it run the exact chain, so the stored code
-// is always the reference's.  The coarse kick's vmax (pm.f90:349) is the
-// float nearest |fl64(v + vfield)|, certified from the same float-float
-// value, else from the exact chain.
+// with t_i the real(4) CIC terms.  Three tiers, each keeping a code only when
+// every double inside its error bound encodes to it (certify_abs), so the
+// stored code is always the reference's:
+//  1. V_f = fl32(hi(decode) + S), S the FP32 sum of the terms, within
+//     gamma_7 sum|t_i| + 2^-24 (|decode| + |V_f|) + 9*2^-53 (|decode| +
+//     sum|t_i| + |V_f|) of the reference value (recursive-summation bound,
+//     gamma_7 = 7u/(1-7u), u = 2^-24; the decode table's float hi is within
+//     half an ulp);
+//  2. the lanes tier 1 leaves undecided (a few per cent: those near a code
+//     edge) sum decode (hi + lo) and the terms in float-float (bound
+//     73*2^-48 (|decode| + sum|t_i|) plus the reference's own eight FP64
+//     roundings) and rebuild the double pattern with integer operations;
+//  3. the reference's exact FP64 chain.
+// The coarse kick's vmax (pm.f90:349) is the float nearest |fl64(v +
+// vfield)|, certified from the float-float value, else from the exact chain.
 // kPre: the meshes hold force*a_mid*dt/6/pi already (k_f2max<true>)
 template <bool kFine, bool kPre>
 __global__ void __launch_bounds__(256, 4) k_kick(KickArgs a) {
@@ -390,17 +391,17 @@ __global__ void __launch_bounds__(256, 4) k_kick(KickArgs a) {
         S = __fadd_rn(S, t[i]);
         T = __fadd_rn(T, fabsf(t[i]));
       }
-      float vh, e1;
-      two_sum(dd.x, S, vh, e1);
-      float vl = __fadd_rn(dd.y, e1);
-      float E = 1.25f * (T * 4.2e-7f + (fabsf(dd.y) + fabsf(e1)) * 6.0e-8f + (fabsf(dd.x) + T + fabsf(vh)) * 1.0e-14f);
-      long long ab = 0, nc_ = 0;
-      bool neg = false;
-      bool ok = !a.exact_only && ff_abs_bits(vh, vl, &ab, &neg) && certify_abs(ab, E, a.cout, &nc_);
-      if (!ok && !a.exact_only) {  // the terms in float-float as well
+      float vh = __fadd_rn(dd.x, S), vl = 0.f;
+      float E = 1.25f * (T * 4.76837158e-7f + (fabsf(dd.x) + fabsf(vh)) * 6.0e-8f + T * 1.0e-15f);
+      long long ab = f2d_bits(vh) & 0x7fffffffffffffffLL, nc_ = 0;
+      bool neg = vh < 0.f;
+      bool ok = !a.exact_only && certify_abs(ab, E, a.cout, &nc_);
+      bool split = false;  // (vh, vl) is the float-float value
+      if (!ok && !a.exact_only) {  // tier 2
         float M;
         ff_sum_terms(dd, t, 8, vh, vl, M);
         E = 1.25f * (M * 2.6e-13f + fabsf(vh) * 2.0e-15f);
+        split = true;
         ok = ff_abs_bits(vh, vl, &ab, &neg) && certify_abs(ab, E, a.cout, &nc_);
       }
       bool need_vmax = false;
@@ -412,6 +413,12 @@ __global__ void __launch_bounds__(256, 4) k_kick(KickArgs a) {
         if (ok && need_vmax) {
           // |fl64(V + vfield)| to float: V + vfield in float-float, its bound
           // the kick's plus the new low part's rounding and the FP64 rounding
+          if (!split) {  // tier 1's value as a float-float
+            float e1;
+            two_sum(dd.x, S, vh, e1);
+            vl = __fadd_rn(dd.y, e1);
+            E = 1.25f * (T * 4.2e-7f + (fabsf(dd.y) + fabsf(e1)) * 6.0e-8f + (fabsf(dd.x) + T + fabsf(vh)) * 1.0e-14f);
+          }
           float wh, e2;
           two_sum(vh, vfd, wh, e2);
           const float wl = __fadd_rn(vl, e2);

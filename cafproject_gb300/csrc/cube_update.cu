@@ -566,19 +566,28 @@ __device__ __forceinline__ void write_particle_at(const UpdArgs& a, int64_t p, i
     }
     long long x = load_code(a.xp, 3 * p + d, g.izipx);
     store_code(a.xp_new, 3 * idx + d, g.izipx, x + dx);
-    // vp = code of vreal - vfield_new (update_particle.f90:116-117): the
-    // decode's float-float split plus vfield - vfield_new (itself a TwoSum)
-    // in float-float; bound: the low parts' two roundings, the split, the
-    // reference's two FP64 roundings and the double pattern's truncation
-    float w, ew, vh, e1;
+    // vp = code of vreal - vfield_new (update_particle.f90:116-117)
+    float w, ew;
     two_sum(vfd, -vbar, w, ew);
-    two_sum(dd.x, w, vh, e1);
-    const float vl = __fadd_rn(__fadd_rn(dd.y, e1), ew);
-    const float E = 1.25f * ((fabsf(dd.y) + fabsf(e1) + fabsf(ew)) * 1.2e-7f +
-                             (fabsf(dd.x) + fabsf(vfd) + fabsf(vbar) + fabsf(vh)) * 1.0e-14f);
-    long long ab = 0, n = 0, code;
-    bool neg = false;
-    if (!a.exact_only && ff_abs_bits(vh, vl, &ab, &neg) && certify_abs(ab, E, a.cv, &n)) {
+    float Vf = __fadd_rn(dd.x, w);
+    float E = 1.25f * ((fabsf(dd.x) + fabsf(Vf)) * 6.0e-8f + fabsf(ew) +
+                       (fabsf(dd.x) + fabsf(vfd) + fabsf(vbar)) * 2.3e-16f);
+    long long ab = f2d_bits(Vf) & 0x7fffffffffffffffLL, n = 0, code;
+    bool neg = Vf < 0.f;
+    bool ok = !a.exact_only && certify_abs(ab, E, a.cv, &n);
+    if (!ok && !a.exact_only) {
+      // tier 2, near a code edge: the decode's float-float split plus
+      // vfield - vfield_new in float-float; bound: the low parts' two
+      // roundings, the split, the reference's two FP64 roundings and the
+      // double pattern's truncation
+      float vh, e1;
+      two_sum(dd.x, w, vh, e1);
+      const float vl = __fadd_rn(__fadd_rn(dd.y, e1), ew);
+      E = 1.25f * ((fabsf(dd.y) + fabsf(e1) + fabsf(ew)) * 1.2e-7f +
+                   (fabsf(dd.x) + fabsf(vfd) + fabsf(vbar) + fabsf(vh)) * 1.0e-14f);
+      ok = ff_abs_bits(vh, vl, &ab, &neg) && certify_abs(ab, E, a.cv, &n);
+    }
+    if (ok) {
       code = neg ? -n : n;
     } else {
       double v = __dadd_rn(codec_decode(a.cv, vcode), (double)vfd);
