@@ -189,6 +189,11 @@ struct cube_ctx {
   DevStats* hstats = nullptr;   // pinned
   void* cufft_work = nullptr;
   size_t cufft_work_bytes = 0;
+  // the fine force chain as this library's transforms (cube_fft.cu), for
+  // power-of-two meshes; opt_cufft = 1 keeps cuFFT
+  float2* fft_tw = nullptr;  // W_nf^m, m < nf
+  bool fft_own = false;
+  int opt_cufft = 0;
 };
 
 // ------------------------------------------------------------------ errors
@@ -476,62 +481,38 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
-// |h + l| of a float-float value as the bit pattern of a double, for
-// |l| <= 2^-20 |h|: bits of l below the double's last place are truncated,
-// so the pattern is within 2 units in the last place of |h + l| (callers add
-// 2^-49 |h| to their error bound).  *neg is the sign of h.  h + l = 0 gives
-// the pattern 0; otherwise returns false when h is zero, subnormal or not
-// finite, or l is not small against h.
-// Integer operations only: the conversion runs on no FP64 unit.
-__device__ __forceinline__ bool ff_abs_bits(float h, float l, long long* out, bool* neg) {
-  const unsigned int hb = __float_as_uint(h), eh = (hb >> 23) & 0xffu;
-  *neg = (hb >> 31) != 0u;
-  if ((hb << 1) == 0u && (__float_as_uint(l) << 1) == 0u) {
-    *out = 0;
-    *neg = false;
-    return true;
-  }
-  if (eh == 0u || eh == 0xffu) return false;
-  long long X = (long long)((hb & 0x7fffffu) | 0x800000u) << 29;  // |h| in units of 2^(eh-127-52)
-  const unsigned int lb = __float_as_uint(l), el = (lb >> 23) & 0xffu;
-  if (el == 0xffu) return false;
-  if (el != 0u) {  // a subnormal l is below the last place: dropped
-    const int sh = 29 + (int)el - (int)eh;
-    if (sh > 32) return false;
-    const long long ml = (long long)((lb & 0x7fffffu) | 0x800000u);
-    const long long add = sh >= 0 ? (ml << sh) : (sh > -25 ? (ml >> (-sh)) : 0);
-    X = (((lb >> 31) != 0u) != *neg) ? X - add : X + add;
-  }
-  int e = (int)eh - 127 + 1023;
-  if (X >= (1LL << 53)) {
-    X >>= 1;
-    e++;
-  } else if (X < (1LL << 52)) {
-    X <<= 1;
-    e--;
-  }
-  if (X < (1LL << 52) || X >= (1LL << 53)) return false;
-  *out = ((long long)e << 52) | (X & ((1LL << 52) - 1));
-  return true;
+// vreal=vreal+f_tot*a_mid*dt/6/pi in FP64 and its code (ext_pp_force.f90:
+// 116-121), for lanes the fast tiers leave undecided (not inlined: keeps
+// double conversions off the common path)
+static __device__ __noinline__ long long pp_kick_exact(CodecView cv, int code, float F, double kick) {
+  double v = __dadd_rn(codec_decode(cv, code), __dmul_rn((double)F, kick));
+  return codec_encode(cv, v);
 }
 
-// dec (hi, lo) + t[0..n) as a float-float h + l: exact TwoSums of the running
-// high part, the low parts summed in FP32.  For the caller's error bound:
-// |(h + l) - (dec + sum t)| <= 73 * 2^-48 * M with M = |dec| + sum |t|
-// (returned; the low-part sum carries at most n + 1 roundings of 2^-24 of a
-// value below (n + 1) 2^-24 M).
-__device__ __forceinline__ void ff_sum_terms(float2 dd, const float* t, int n, float& h, float& l, float& M) {
-  h = dd.x;
-  l = dd.y;
-  M = fabsf(dd.x);
+// The PP kick of one particle's three velocity codes: v = decode(code) +
+// F*kick, encoded with the same sigma.  The FP32 sum of the decode's float
+// hi and the FP32 kick product is certified against its bound (the
+// product's two roundings, the hi split and the sum's rounding) with the
+// three table probes issued together; undecided lanes take the FP64
+// expression.  code[] is updated in place.
+__device__ __forceinline__ void pp_kick3(const CodecView& cv, int code[3], const float F[3], float kick_f,
+                                         double kick_d, int exact_only) {
+  float E[3], vf[3];
+  long long ab[3], n[3];
+  bool ok[3];
 #pragma unroll
-  for (int i = 0; i < n; i++) {
-    float s, e;
-    two_sum(h, t[i], s, e);
-    h = s;
-    l = __fadd_rn(l, e);
-    M = __fadd_rn(M, fabsf(t[i]));
+  for (int d = 0; d < 3; d++) {
+    const float dh = codec_decode_ff(cv, code[d]).x;
+    const float kf = __fmul_rn(F[d], kick_f);
+    vf[d] = __fadd_rn(dh, kf);
+    E[d] = 1.25f * (fabsf(kf) * 1.3e-7f + (2.f * fabsf(dh) + fabsf(vf[d])) * 6.0e-8f);
+    ab[d] = f2d_bits(vf[d]) & 0x7fffffffffffffffLL;
   }
+  certify_abs3(ab, E, cv, n, ok);
+#pragma unroll
+  for (int d = 0; d < 3; d++)
+    code[d] = (!exact_only && ok[d]) ? (int)(vf[d] < 0.f ? -n[d] : n[d])
+                                     : (int)pp_kick_exact(cv, code[d], F[d], kick_d);
 }
 
 // Nearest float to the real t + lo, certified when every real within margin
@@ -713,7 +694,8 @@ int cube_kernels_init(cube_ctx* c, const float* fine_table, const float* coarse_
 int cube_scan_counts(cube_ctx* c, const int32_t* counts, int64_t* starts, int64_t n);
 int cube_update_x_impl(cube_ctx* c, float dt_old, float dt, float vz_max, cube_stats* st);
 int cube_pp_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st);
-int cube_pp_launch(cube_ctx* c, float a_mid, float dt);
+// defer_kick: leave the kick to the fine kick (cube_fine_kick_impl with_pp)
+int cube_pp_launch(cube_ctx* c, float a_mid, float dt, bool defer_kick = false);
 int cube_pp_init(cube_ctx* c);  // once per context: the staging kernels' shared-memory sizes
 int cube_pp_finish(cube_ctx* c, cube_stats* st);
 // density deposits; accumulate: add to the mesh (the linked species) instead of writing it
@@ -723,10 +705,14 @@ int cube_coarse_density_impl(cube_ctx* c, cube_stats* st, bool accumulate = fals
 // as the mesh part of the kick term, force*a_mid*dt/6/pi, and the kick that
 // follows is given pre=true (fused step only; the stage calls keep forces)
 int cube_fine_forces_impl(cube_ctx* c, cube_stats* st, const float* pre = nullptr);
-int cube_fine_kick_impl(cube_ctx* c, float a_mid, float dt, bool pre = false);
+// with_pp: first apply the PP kick that cube_pp_launch(.., defer_kick) left
+// to the fine kick (eager mode)
+int cube_fine_kick_impl(cube_ctx* c, float a_mid, float dt, bool pre = false, bool with_pp = false);
 int cube_coarse_forces_impl(cube_ctx* c, cube_stats* st, const float* pre = nullptr);
 int cube_coarse_kick_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st, bool pre = false);
 int cube_fine_spectral_impl(cube_ctx* c, cube_stats* st, const float* pre);
+int cube_fft_init(cube_ctx* c);
+int cube_fine_chain_own(cube_ctx* c, const float* pre);
 int cube_coarse_spectral_impl(cube_ctx* c, cube_stats* st, const float* pre);
 int cube_pk_deposit(cube_ctx* c, int ng, float* rho, unsigned long long* total);
 int dep_shift(float mass);  // deposits' fixed point: total = integer * 2^-dep_shift(mass)

@@ -304,6 +304,9 @@ struct KickArgs {
   const StepDev* sd;       // graph mode: a_mid, dt, tau from the device
   unsigned int* vmax_est;        // fine kick: record max |v + vfield| (FP32) here when set
   const unsigned int* tau_est;   // coarse kick: tau = 0.7 of this estimate when set
+  const float* fpp;              // fine kick: when set, first the PP kick by these pair forces
+  float pp_kf;                   // its factor a_mid*dt/6/pi, float and double
+  double pp_kd;
 };
 __device__ __forceinline__ float kick_amid(const KickArgs& a) { return a.sd ? __ldg(&a.sd->h.a_mid) : a.a_mid; }
 __device__ __forceinline__ float kick_dt(const KickArgs& a) { return a.sd ? __ldg(&a.sd->h.dt) : a.dt; }
@@ -314,21 +317,14 @@ __device__ __forceinline__ float kick_tau(const KickArgs& a, int d) {
 
 // The kick velocity of the reference is the FP64 chain
 //   v = decode; v = v + t1; ...; v = v + t8       (pm.f90:145-153)
-// with t_i the real(4) CIC terms.  Three tiers, each keeping a code only when
-// every double inside its error bound encodes to it (certify_abs), so the
-// stored code is always the reference's:
-//  1. V_f = fl32(hi(decode) + S), S the FP32 sum of the terms, within
-//     gamma_7 sum|t_i| + 2^-24 (|decode| + |V_f|) + 9*2^-53 (|decode| +
-//     sum|t_i| + |V_f|) of the reference value (recursive-summation bound,
-//     gamma_7 = 7u/(1-7u), u = 2^-24; the decode table's float hi is within
-//     half an ulp);
-//  2. the lanes tier 1 leaves undecided (a few per cent: those near a code
-//     edge) sum decode (hi + lo) and the terms in float-float (bound
-//     73*2^-48 (|decode| + sum|t_i|) plus the reference's own eight FP64
-//     roundings) and rebuild the double pattern with integer operations;
-//  3. the reference's exact FP64 chain.
-// The coarse kick's vmax (pm.f90:349) is the float nearest |fl64(v +
-// vfield)|, certified from the float-float value, else from the exact chain.
+// with t_i the real(4) CIC terms.  The fast path forms V_f = fl32(hi(decode) + S)
+// with S the FP32 sum of the terms; its distance from the reference value is
+// bounded by
+//   gamma_7 sum|t_i| + 2^-24 (|decode| + |V_f|) + 9*2^-53 (|decode| + sum|t_i| + |V_f|)
+// (recursive-summation bound, gamma_7 = 7u/(1-7u), u = 2^-24; the decode table's
+// float hi is within half an ulp).  certify_abs keeps the code only when every
+// double inside that bound encodes to it; otherwise the lane runs the exact
+// chain, so the stored code is always the reference's.
 // kPre: the meshes hold force*a_mid*dt/6/pi already (k_f2max<true>)
 template <bool kFine, bool kPre>
 __global__ void __launch_bounds__(256, 4) k_kick(KickArgs a) {
@@ -371,6 +367,16 @@ __global__ void __launch_bounds__(256, 4) k_kick(KickArgs a) {
     int64_t c121 = mesh_idx(n, i1[0], i2[1], i1[2]), c112 = mesh_idx(n, i1[0], i1[1], i2[2]);
     int64_t c122 = mesh_idx(n, i1[0], i2[1], i2[2]), c212 = mesh_idx(n, i2[0], i1[1], i2[2]);
     int64_t c221 = mesh_idx(n, i2[0], i2[1], i1[2]), c222 = mesh_idx(n, i2[0], i2[1], i2[2]);
+    int codes[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) codes[d] = load_code(a.vp_in, 3 * p + d, g.izipv);
+    if (kFine && a.fpp) {
+      // ext_pp_force's kick (ext_pp_force.f90:116-121) before the fine kick,
+      // both in this pass: the PP code (decoded and encoded with sigma_vi) is
+      // the one the fine kick decodes
+      const float F[3] = {a.fpp[3 * p], a.fpp[3 * p + 1], a.fpp[3 * p + 2]};
+      pp_kick3(a.cin, codes, F, a.pp_kf, a.pp_kd, a.exact_only);
+    }
     for (int d = 0; d < 3; d++) {
       const float* F = a.f[d];
       float t[8];
@@ -384,57 +390,30 @@ __global__ void __launch_bounds__(256, 4) k_kick(KickArgs a) {
       t[6] = KT(c221, d2[0], d2[1], d1[2]);
       t[7] = KT(c222, d2[0], d2[1], d2[2]);
 #undef KT
-      int code = load_code(a.vp_in, 3 * p + d, g.izipv);
-      const float2 dd = codec_decode_ff(a.cin, code);
+      const int code = codes[d];
+      float dh = codec_decode_ff(a.cin, code).x;
       float S = t[0], T = fabsf(t[0]);
       for (int i = 1; i < 8; i++) {
         S = __fadd_rn(S, t[i]);
         T = __fadd_rn(T, fabsf(t[i]));
       }
-      float vh = __fadd_rn(dd.x, S), vl = 0.f;
-      float E = 1.25f * (T * 4.76837158e-7f + (fabsf(dd.x) + fabsf(vh)) * 6.0e-8f + T * 1.0e-15f);
-      long long ab = f2d_bits(vh) & 0x7fffffffffffffffLL, nc_ = 0;
-      bool neg = vh < 0.f;
+      float vf = __fadd_rn(dh, S);
+      long long vb = f2d_bits(vf), ab = vb & 0x7fffffffffffffffLL;
+      float E = 1.25f * (T * 4.76837158e-7f + (fabsf(dh) + fabsf(vf)) * 6.0e-8f + T * 1.0e-15f);
+      long long nc_ = 0;
       bool ok = !a.exact_only && certify_abs(ab, E, a.cout, &nc_);
-      bool split = false;  // (vh, vl) is the float-float value
-      if (!ok && !a.exact_only) {  // tier 2
-        float M;
-        ff_sum_terms(dd, t, 8, vh, vl, M);
-        E = 1.25f * (M * 2.6e-13f + fabsf(vh) * 2.0e-15f);
-        split = true;
-        ok = ff_abs_bits(vh, vl, &ab, &neg) && certify_abs(ab, E, a.cout, &nc_);
-      }
       bool need_vmax = false;
       float vfd = 0.f;
       if (!kFine) {
         vfd = a.vfield[3 * cell + d];
-        float ub = (fabsf(vh) + E + fabsf(vfd)) * 1.000001f;
+        float ub = (fabsf(vf) + E + fabsf(vfd)) * 1.000001f;
         need_vmax = a.vmax_only || ub >= kick_tau(a, d);
-        if (ok && need_vmax) {
-          // |fl64(V + vfield)| to float: V + vfield in float-float, its bound
-          // the kick's plus the new low part's rounding and the FP64 rounding
-          if (!split) {  // tier 1's value as a float-float
-            float e1;
-            two_sum(dd.x, S, vh, e1);
-            vl = __fadd_rn(dd.y, e1);
-            E = 1.25f * (T * 4.2e-7f + (fabsf(dd.y) + fabsf(e1)) * 6.0e-8f + (fabsf(dd.x) + T + fabsf(vh)) * 1.0e-14f);
-          }
-          float wh, e2;
-          two_sum(vh, vfd, wh, e2);
-          const float wl = __fadd_rn(vl, e2);
-          const float Ew = 1.25f * (E + (fabsf(vl) + fabsf(e2)) * 6.0e-8f + fabsf(wh) * 1.2e-16f);
-          float r;
-          if (round_certified(wh, wl, Ew, &r)) {
-            vm[d] = fmaxf(vm[d], fabsf(r));
-            need_vmax = false;
-          }
-        }
       } else if (a.vmax_est) {
-        vm[d] = fmaxf(vm[d], fabsf(__fadd_rn(vh, a.vfield[3 * cell + d])));
+        vm[d] = fmaxf(vm[d], fabsf(__fadd_rn(vf, a.vfield[3 * cell + d])));
       }
       long long out;
       if (ok && !need_vmax) {
-        out = neg ? -nc_ : nc_;
+        out = vb < 0 ? -nc_ : nc_;
       } else {
         // the reference's exact FP64 chain
         double v = codec_decode(a.cin, code);
@@ -632,6 +611,17 @@ int cube_fine_spectral_impl(cube_ctx* c, cube_stats* st, const float* pre) {
   cudaStream_t s = c->stream;
   int64_t nfh = c->nf / 2 + 1;
   int64_t nspec = nfh * c->nf * (int64_t)c->nf;
+  if (c->fft_own && !c->opt_cufft) {  // five passes of this library's transforms (cube_fft.cu)
+    int r = cube_fine_chain_own(c, pre);
+    if (r) return r;
+    if (st) {
+      r = cube_stats_fetch(c);
+      if (r) return r;
+      st->f2_max_fine = bits_float(c->hstats->f2_fine_bits);
+      st->testrhof = std::ldexp((double)c->hstats->rhof_fix, -dep_shift(c->p.mass_p));
+    }
+    return CUBE_OK;
+  }
   cube_phase_begin(c, PH_F_R2C);
   CUBE_FFT(c, cufftExecR2C(c->plan_f_r2c, c->rho_f, (cufftComplex*)c->rho_f));
   cube_phase_end(c, PH_F_R2C);
@@ -661,8 +651,14 @@ int cube_fine_spectral_impl(cube_ctx* c, cube_stats* st, const float* pre) {
   return CUBE_OK;
 }
 
-int cube_fine_kick_impl(cube_ctx* c, float a_mid, float dt, bool pre) {
+int cube_fine_kick_impl(cube_ctx* c, float a_mid, float dt, bool pre, bool with_pp) {
   KickArgs k{};
+  if (with_pp) {  // the PP kick of cube_pp_launch(.., defer_kick), applied here
+    if (c->graph_mode || !c->fpp) return cube_fail(c, CUBE_ERR_ARG, "PP kick in the fine kick: eager mode with PP only");
+    k.fpp = c->fpp;
+    k.pp_kd = (((double)a_mid * (double)dt) / 6.0) / (double)CUBE_PI_F;
+    k.pp_kf = (float)k.pp_kd;
+  }
   if (c->graph_mode) {  // decode with sigma_vi (slot 0), encode with sigma_vi_new (slot 1)
     cube_codec_view_dev(c, 0, &c->sd->h.cf_vi, &k.cin);
     cube_codec_view_dev(c, 1, &c->sd->cf_new, &k.cout);

@@ -83,15 +83,12 @@ __device__ __forceinline__ float fine_off(int code, int izipx) {
   return __fmul_rn(pos_off_f(code, izipx), izipx == 1 ? 4.0f / 256.0f : 4.0f / 65536.0f);
 }
 
-// v*2^32 truncated toward zero as a two's-complement int64 (|v| < 2^23), from
-// the float's mantissa and exponent by integer shifts: no conversion
-// instruction (those share the narrow FP64 pipe)
+// v*2^32 as a two's-complement int64 from 32-bit conversions only (|v| < 2^23)
 __device__ __forceinline__ long long to_fix(float v) {
-  const unsigned int b = __float_as_uint(v), e = (b >> 23) & 0xffu;
-  const long long m = (long long)((b & 0x7fffffu) | 0x800000u);
-  const int sh = (int)e - 118;  // |v| * 2^32 = m * 2^(e - 118)
-  const long long q = e == 0u ? 0 : (sh >= 0 ? m << sh : (sh > -24 ? m >> (-sh) : 0));
-  return (b >> 31) ? -q : q;
+  float a = fabsf(v);
+  float ws = __fmul_rn(a, 256.0f), fh = floorf(ws);
+  long long q = ((long long)(unsigned int)fh << 24) + (unsigned int)__fmul_rn(__fsub_rn(ws, fh), 16777216.0f);
+  return v < 0.f ? -q : q;
 }
 __device__ __forceinline__ float from_fix(long long q) {
   bool neg = q < 0;
@@ -122,14 +119,6 @@ __device__ __forceinline__ void pair_force(const PPArgs& a, float rx, float ry, 
   acc[2] += to_fix(__fmul_rn(s, rz));
 }
 
-// vreal=vreal+f_tot*a_mid*dt/6/pi in FP64 and its code, for lanes whose fast
-// path was not certified (not inlined: keeps double conversions off the
-// common path)
-__device__ __noinline__ long long pp_kick_exact(CodecView cv, int code, float F, double kick) {
-  double v = __dadd_rn(codec_decode(cv, code), __dmul_rn((double)F, kick));
-  return codec_encode(cv, v);
-}
-
 // the summed pair force of particle p, kept for the kick pass; returns |F|^2
 __device__ __forceinline__ float pp_store_force(const PPArgs& a, int64_t p, const long long* acc) {
   float F[3];
@@ -145,50 +134,16 @@ __device__ __forceinline__ float pp_store_force(const PPArgs& a, int64_t p, cons
 __global__ void __launch_bounds__(256) k_pp_kick(PPArgs a) {
   const Geo& g = a.g;
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.np; p += (int64_t)gridDim.x * blockDim.x) {
-    float F[3], E[3];
+    float F[3];
     int code[3];
-    long long ab[3], n[3];
-    bool ok[3];
 #pragma unroll
     for (int d = 0; d < 3; d++) {
       F[d] = a.fpp[3 * p + d];
       code[d] = load_code(a.vp, 3 * p + d, g.izipv);
     }
-    float vf[3];
-    float2 dd[3];
+    pp_kick3(a.cv, code, F, pp_kick_f(a), pp_kick_d(a), a.exact_only);
 #pragma unroll
-    for (int d = 0; d < 3; d++) {
-      // vreal=vreal+f_tot*a_mid*dt/6/pi (ext_pp_force.f90:116), then the code
-      dd[d] = codec_decode_ff(a.cv, code[d]);
-      const float kf = __fmul_rn(F[d], pp_kick_f(a));
-      vf[d] = __fadd_rn(dd[d].x, kf);
-      E[d] = 1.25f * (fabsf(kf) * 1.3e-7f + (2.f * fabsf(dd[d].x) + fabsf(vf[d])) * 6.0e-8f);
-      ab[d] = f2d_bits(vf[d]) & 0x7fffffffffffffffLL;
-    }
-    certify_abs3(ab, E, a.cv, n, ok);
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-      long long out;
-      bool neg = vf[d] < 0.f;
-      if (!ok[d] && !a.exact_only) {
-        // tier 2: the kick added to the decode's float-float split with one
-        // TwoSum; bound: the kick's FP32 product, the low part's rounding,
-        // the split, the FP64 product and sum, the double pattern's truncation
-        const float kf = __fmul_rn(F[d], pp_kick_f(a));
-        float vh, e1;
-        two_sum(dd[d].x, kf, vh, e1);
-        const float vl = __fadd_rn(dd[d].y, e1);
-        const float E2 = 1.25f * (fabsf(kf) * 1.3e-7f + (fabsf(dd[d].y) + fabsf(e1)) * 6.0e-8f +
-                                  (fabsf(dd[d].x) + fabsf(vh)) * 1.0e-14f);
-        ok[d] = ff_abs_bits(vh, vl, &ab[d], &neg) && certify_abs(ab[d], E2, a.cv, &n[d]);
-      }
-      if (!a.exact_only && ok[d]) {
-        out = neg ? -n[d] : n[d];
-      } else {
-        out = pp_kick_exact(a.cv, code[d], F[d], pp_kick_d(a));
-      }
-      store_code(a.vp, 3 * p + d, g.izipv, out);
-    }
+    for (int d = 0; d < 3; d++) store_code(a.vp, 3 * p + d, g.izipv, code[d]);
   }
 }
 
@@ -247,40 +202,22 @@ __device__ bool pp_block(const PPArgs& a, const int C0[3], const int B[3], PPSme
   if (threadIdx.x == 0) sm.ncore = sm.nring = 0;
   __syncthreads();
   const int total = block_exclusive_scan(sm.pref, NS);
-  // stage the particles whose fine cell lies in the block or its fine ring:
-  // the fine cell is the code's top two bits (4*frac = 4*(u+0.5)/2^(8 izipx)),
-  // so membership is an integer test and only the staged particles form
-  // their FP32 positions; slots come from one shared atomic per warp
-  const int ush = 8 * g.izipx - 2, umask = (1 << (8 * g.izipx)) - 1;
-  const unsigned int lane = threadIdx.x & 31u;
+  // stage the particles whose fine cell lies in the block or its fine ring
   for_box_particles<PS_MAX>(sm.pref, sm.sstart, S0, S1 * S2, total, [&](int64_t p, int sx, int row) {
     const int sl[3] = {sx - 1, row % S1 - 1, row / S1 - 1};
-    int code[3], fi[3];
+    float x[3];
+    int fi[3];
     bool in = true, core = true;
 #pragma unroll
     for (int d = 0; d < 3; d++) {
-      code[d] = load_code(a.xp, 3 * p + d, g.izipx);
-      fi[d] = 4 * sl[d] + ((code[d] & umask) >> ush) + 1;  // 0 .. 4B+1 inside the staged region
+      x[d] = __fadd_rn((float)(4 * sl[d]), fine_off(load_code(a.xp, 3 * p + d, g.izipx), g.izipx));
+      fi[d] = (int)floorf(x[d]) + 1;  // 0 .. 4B+1 inside the staged region
       in = in && fi[d] >= 0 && fi[d] <= 4 * B[d] + 1;
       core = core && fi[d] >= 1 && fi[d] <= 4 * B[d];
     }
-    const unsigned int act = __activemask();
-    const unsigned int mc = __ballot_sync(act, in && core), mr = __ballot_sync(act, in && !core);
-    const unsigned int leader = __ffs(act) - 1;
-    int bc = 0, br = 0;
-    if (lane == leader) {
-      if (mc) bc = atomicAdd(&sm.ncore, __popc(mc));
-      if (mr) br = atomicAdd(&sm.nring, __popc(mr));
-    }
-    bc = __shfl_sync(act, bc, leader);
-    br = __shfl_sync(act, br, leader);
     if (!in) return;
-    const unsigned int below = (1u << lane) - 1u;
-    const int slot = core ? bc + __popc(mc & below) : CAP - 1 - (br + __popc(mr & below));
+    const int slot = core ? atomicAdd(&sm.ncore, 1) : CAP - 1 - atomicAdd(&sm.nring, 1);
     if (slot < 0 || slot >= CAP) return;
-    float x[3];
-#pragma unroll
-    for (int d = 0; d < 3; d++) x[d] = __fadd_rn((float)(4 * sl[d]), fine_off(code[d], g.izipx));
     int f = fi[0] + F0 * (fi[1] + F1 * fi[2]);
     const unsigned sh = 16u * (unsigned)(f & 1);
     int r = (int)((atomicAdd(&bins32[f >> 1], 1u << sh) >> sh) & 0xffffu);
@@ -419,7 +356,7 @@ __global__ void k_pp_list_all(int* list, int n, int* count) {
 }  // namespace
 
 // every PP launch on c->stream (stats in c->dstats); the host reads nothing
-int cube_pp_launch(cube_ctx* c, float a_mid, float dt) {
+int cube_pp_launch(cube_ctx* c, float a_mid, float dt, bool defer_kick) {
   if (!c->fpp) return cube_fail(c, CUBE_ERR_ARG, "PP is off for this context (pp_on = 0)");
   PPArgs a{};
   int r;
@@ -470,7 +407,7 @@ int cube_pp_launch(cube_ctx* c, float a_mid, float dt) {
   if (start <= 2) k2<<<persist, PP_THREADS, PP_SMEM, c->stream>>>(a);
   if (start <= 3) k3<<<one_per_sm, PP_THREADS1, PP_SMEM1, c->stream>>>(a);
   k_pp_dense<<<persist, PP_THREADS, 0, c->stream>>>(a);
-  k_pp_kick<<<cube_grid(c->np, 256), 256, 0, c->stream>>>(a);
+  if (!defer_kick) k_pp_kick<<<cube_grid(c->np, 256), 256, 0, c->stream>>>(a);
   CUBE_CUDA(c, cudaGetLastError());
   cube_phase_end(c, PH_PP);
   if (c->graph_mode) {

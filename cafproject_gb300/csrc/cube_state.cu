@@ -431,14 +431,6 @@ __global__ void k_codec_check(const double* __restrict__ v, int64_t n, double c,
     const long long bits = __double_as_longlong(v[i]);
     long long nq;
     if (certify_abs(bits & 0x7fffffffffffffffLL, 0.f, k, &nq) && (bits < 0 ? -nq : nq) != (long long)t) t = INT32_MIN;
-    // and the kernels' float-float route: v split into two floats, its
-    // double pattern rebuilt with integer operations, certified with the
-    // split's and the pattern's error
-    const float h = __double2float_rn(v[i]), l = __double2float_rn(__dsub_rn(v[i], (double)h));
-    long long ab;
-    bool neg;
-    if (ff_abs_bits(h, l, &ab, &neg) && certify_abs(ab, fabsf(h) * 1.0e-14f, k, &nq) && (neg ? -nq : nq) != (long long)t)
-      t = INT32_MIN;
     table[i] = t;
   }
 }

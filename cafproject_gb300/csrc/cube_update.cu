@@ -573,22 +573,8 @@ __device__ __forceinline__ void write_particle_at(const UpdArgs& a, int64_t p, i
     float E = 1.25f * ((fabsf(dd.x) + fabsf(Vf)) * 6.0e-8f + fabsf(ew) +
                        (fabsf(dd.x) + fabsf(vfd) + fabsf(vbar)) * 2.3e-16f);
     long long ab = f2d_bits(Vf) & 0x7fffffffffffffffLL, n = 0, code;
-    bool neg = Vf < 0.f;
-    bool ok = !a.exact_only && certify_abs(ab, E, a.cv, &n);
-    if (!ok && !a.exact_only) {
-      // tier 2, near a code edge: the decode's float-float split plus
-      // vfield - vfield_new in float-float; bound: the low parts' two
-      // roundings, the split, the reference's two FP64 roundings and the
-      // double pattern's truncation
-      float vh, e1;
-      two_sum(dd.x, w, vh, e1);
-      const float vl = __fadd_rn(__fadd_rn(dd.y, e1), ew);
-      E = 1.25f * ((fabsf(dd.y) + fabsf(e1) + fabsf(ew)) * 1.2e-7f +
-                   (fabsf(dd.x) + fabsf(vfd) + fabsf(vbar) + fabsf(vh)) * 1.0e-14f);
-      ok = ff_abs_bits(vh, vl, &ab, &neg) && certify_abs(ab, E, a.cv, &n);
-    }
-    if (ok) {
-      code = neg ? -n : n;
+    if (!a.exact_only && certify_abs(ab, E, a.cv, &n)) {
+      code = Vf < 0.f ? -n : n;
     } else {
       double v = __dadd_rn(codec_decode(a.cv, vcode), (double)vfd);
       code = codec_encode(a.cv, __dsub_rn(v, (double)vbar));

@@ -152,62 +152,78 @@ int64_t orc_buffer_count(const orc_params* p, const int32_t* rhoc) {
    buffer_grid.f90:28-122); bstart is the exclusive spine over extended cells
    (nzero of update_particle.f90:63 == idx_b_r - sum(rhoc(i:,j,k)),
    spine_image variables.f90:141-187); bxp/bvp/bpid hold each extended cell's
-   particles copied in stored order (redistribute_cdm + buffer_xvp). */
+   particles copied in stored order (redistribute_cdm + buffer_xvp).  The
+   spine is one serial prefix sum over the extended cells; the copies run in
+   parallel over them. */
 void orc_buffer(const orc_params* p, const void* xp, const void* vp, const int32_t* pid,
                 const int32_t* rhoc, const float* vfield, int32_t* brhoc, float* bvfield,
                 int64_t* bstart, void* bxp, void* bvp, int32_t* bpid) {
-  int64_t nt = p->nt, nnt = p->nnt, ncb = p->ncb, nc = p->nc;
-  int64_t ncell_phys = nc * nc * nc;
+  int64_t nt = p->nt, nnt = p->nnt, ncb = p->ncb, nc = p->nc, nte = nt + 2 * ncb;
+  int64_t ncell_phys = nc * nc * nc, next = nte * nte * nte * nnt * nnt * nnt;
   int64_t* cstart = (int64_t*)malloc(sizeof(int64_t) * (ncell_phys + 1));
+  int64_t* src_of = (int64_t*)malloc(sizeof(int64_t) * next);
   cstart[0] = 0;
   for (int64_t c = 0; c < ncell_phys; c++) cstart[c + 1] = cstart[c] + rhoc[c];
-  int64_t pos = 0;
-  for (int64_t t = 0; t < nnt * nnt * nnt; t++) {
+  set_threads(p);
+  /* the physical cell behind every extended cell, its count and field */
+#pragma omp parallel for schedule(static)
+  for (int64_t e = 0; e < next; e++) {
+    int64_t i = e % nte, j = (e / nte) % nte, k = (e / (nte * nte)) % nte, t = e / (nte * nte * nte);
     int64_t tx = t % nnt, ty = (t / nnt) % nnt, tz = t / (nnt * nnt);
-    for (int64_t k = 1 - ncb; k <= nt + ncb; k++)
-      for (int64_t j = 1 - ncb; j <= nt + ncb; j++)
-        for (int64_t i = 1 - ncb; i <= nt + ncb; i++) {
-          int64_t gx = wrapc(tx * nt + i - 1, nc), gy = wrapc(ty * nt + j - 1, nc),
-                  gz = wrapc(tz * nt + k - 1, nc);
-          int64_t c = phys_index(p, gx, gy, gz);
-          int64_t e = ext_index(p, i, j, k, t);
-          brhoc[e] = rhoc[c];
-          for (int d = 0; d < 3; d++) bvfield[3 * e + d] = vfield[3 * c + d];
-          bstart[e] = pos;
-          for (int64_t l = 0; l < rhoc[c]; l++) {
-            int64_t src = cstart[c] + l, dst = pos + l;
-            for (int d = 0; d < 3; d++) {
-              st_i(bxp, 3 * dst + d, p->izipx, ld_i(xp, 3 * src + d, p->izipx));
-              st_i(bvp, 3 * dst + d, p->izipv, ld_i(vp, 3 * src + d, p->izipv));
-            }
-            if (pid && bpid) bpid[dst] = pid[src];
-          }
-          pos += rhoc[c];
-        }
+    int64_t gx = wrapc(tx * nt + i - ncb, nc), gy = wrapc(ty * nt + j - ncb, nc), gz = wrapc(tz * nt + k - ncb, nc);
+    int64_t c = phys_index(p, gx, gy, gz);
+    src_of[e] = c;
+    brhoc[e] = rhoc[c];
+    for (int d = 0; d < 3; d++) bvfield[3 * e + d] = vfield[3 * c + d];
   }
+  int64_t pos = 0;
+  for (int64_t e = 0; e < next; e++) {
+    bstart[e] = pos;
+    pos += brhoc[e];
+  }
+#pragma omp parallel for schedule(dynamic, 4096)
+  for (int64_t e = 0; e < next; e++) {
+    int64_t c = src_of[e];
+    for (int64_t l = 0; l < brhoc[e]; l++) {
+      int64_t src = cstart[c] + l, dst = bstart[e] + l;
+      for (int d = 0; d < 3; d++) {
+        st_i(bxp, 3 * dst + d, p->izipx, ld_i(xp, 3 * src + d, p->izipx));
+        st_i(bvp, 3 * dst + d, p->izipv, ld_i(vp, 3 * src + d, p->izipv));
+      }
+      if (pid && bpid) bpid[dst] = pid[src];
+    }
+  }
+  free(src_of);
   free(cstart);
 }
 
 /* Copy the physical cells of the buffered state back to the disjoint layout
-   (the particle order of checkpoint.f90:38-47). */
+   (the particle order of checkpoint.f90:38-47), in parallel over cells. */
 void orc_unbuffer(const orc_params* p, const int32_t* brhoc, const int64_t* bstart, const void* bxp,
                   const void* bvp, const int32_t* bpid, void* xp, void* vp, int32_t* pid) {
-  int64_t nt = p->nt, nnt = p->nnt, pos = 0;
-  for (int64_t t = 0; t < nnt * nnt * nnt; t++)
-    for (int64_t k = 1; k <= nt; k++)
-      for (int64_t j = 1; j <= nt; j++)
-        for (int64_t i = 1; i <= nt; i++) {
-          int64_t e = ext_index(p, i, j, k, t);
-          for (int64_t l = 0; l < brhoc[e]; l++) {
-            int64_t src = bstart[e] + l;
-            for (int d = 0; d < 3; d++) {
-              st_i(xp, 3 * pos + d, p->izipx, ld_i(bxp, 3 * src + d, p->izipx));
-              st_i(vp, 3 * pos + d, p->izipv, ld_i(bvp, 3 * src + d, p->izipv));
-            }
-            if (pid && bpid) pid[pos] = bpid[src];
-            pos++;
-          }
-        }
+  int64_t nt = p->nt, nnt = p->nnt, ncell = nt * nt * nt * nnt * nnt * nnt;
+  int64_t* out = (int64_t*)malloc(sizeof(int64_t) * (ncell + 1));
+  out[0] = 0;
+  /* physical cells in the disjoint order: tile, then k, j, i inside it */
+  for (int64_t c = 0; c < ncell; c++) {
+    int64_t i = c % nt + 1, j = (c / nt) % nt + 1, k = (c / (nt * nt)) % nt + 1, t = c / (nt * nt * nt);
+    out[c + 1] = out[c] + brhoc[ext_index(p, i, j, k, t)];
+  }
+  set_threads(p);
+#pragma omp parallel for schedule(dynamic, 4096)
+  for (int64_t c = 0; c < ncell; c++) {
+    int64_t i = c % nt + 1, j = (c / nt) % nt + 1, k = (c / (nt * nt)) % nt + 1, t = c / (nt * nt * nt);
+    int64_t e = ext_index(p, i, j, k, t);
+    for (int64_t l = 0; l < brhoc[e]; l++) {
+      int64_t src = bstart[e] + l, dst = out[c] + l;
+      for (int d = 0; d < 3; d++) {
+        st_i(xp, 3 * dst + d, p->izipx, ld_i(bxp, 3 * src + d, p->izipx));
+        st_i(vp, 3 * dst + d, p->izipv, ld_i(bvp, 3 * src + d, p->izipv));
+      }
+      if (pid && bpid) pid[dst] = bpid[src];
+    }
+  }
+  free(out);
 }
 
 /* ------------------------------------------------------------- update_xp */

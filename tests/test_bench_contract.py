@@ -35,7 +35,7 @@ def _run(monkeypatch, argv):
     monkeypatch.setattr(bench, "run_redshifts", lambda args, lrank: {"5": {"ms_per_step": 84.0, "value": 1.6e9},
                                                                      "0": {"ms_per_step": 102.0, "value": 1.3e9}})
     monkeypatch.setattr(bench, "run_reference", lambda args, ws, rank: dict(value=4.8e6, ms=27000.0, n=p.npglobal,
-                                                                             p=p, sample=3.0))
+                                                                             p=p, steps=2, step_s=[27.0, 27.0]))
     buf = io.StringIO()
     with redirect_stdout(buf):
         bench.main()
@@ -63,6 +63,8 @@ def test_library_arm_line(monkeypatch):
 def test_reference_arm_line(monkeypatch):
     d = _run(monkeypatch, ["--impl", "reference"])
     assert BASE_KEYS <= set(d) and d["impl"] == "reference"
+    # the same workload description as the library's arm
+    assert d["config"] == _run(monkeypatch, [])["config"]
     assert d["cpu_baseline"]["value"] == d["value"] and d["e2e"]["value"] == d["value"]
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
 
