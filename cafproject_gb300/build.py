@@ -15,7 +15,7 @@ SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libcube_gb300.so")
 SOURCES = ["cube_api.cu", "cube_state.cu", "cube_update.cu", "cube_pm.cu", "cube_pp.cu", "cube_pk.cu", "cube_io.cu", "cube_ic.cu", "cube_timing.cu",
-           "cube_dpm.cu", "cube_batch.cu", "cube_sort.cu", "cube_fft.cu"]
+           "cube_dpm.cu", "cube_batch.cu", "cube_sort.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -66,7 +66,7 @@ static void release(cube_ctx* c) {
                   c->scan_tmp, c->red_tmp, c->tan_tab, c->codec[0].dec, c->codec[1].dec, c->codec[0].bnd, c->codec[1].bnd, c->codec[0].dech, c->codec[1].dech, c->rho_f, c->force_f[0],
                   c->force_f[1], c->force_f[2], c->kern_f, c->kern_f_raw, c->rho_c, c->force_c[0],
                   c->force_c[1], c->force_c[2], c->kern_c, c->fpp, c->pp_list[0], c->pp_list[1], c->pp_list[2], c->pp_list[3], c->pp_nlist, c->dstats,
-                  c->cufft_work, c->fft_tw};
+                  c->cufft_work};
   for (void* b : bufs)
     if (b) cudaFree(b);
   for (int i = 0; i < 2; i++) {
@@ -251,8 +251,6 @@ static int create_impl(const cube_params* p, const float* fine_table, const floa
   if (r) return r;
   if (!owner) {
     r = cube_kernels_init(c, fine_table, coarse_table);
-    if (r) return r;
-    r = cube_fft_init(c);
     if (r) return r;
   }
   CUBE_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -521,9 +519,6 @@ extern "C" int cube_set_option(cube_ctx* c, int option, int64_t value) {
     case CUBE_OPT_DEPOSIT_COARSE:
       if (value < 0 || value > 3) return cube_fail(c, CUBE_ERR_ARG, "deposit brick shape must be 0 to 3");
       (option == CUBE_OPT_DEPOSIT_FINE ? c->opt_dep_fine : c->opt_dep_coarse) = (int)value;
-      return CUBE_OK;
-    case CUBE_OPT_CUFFT:
-      c->opt_cufft = value ? 1 : 0;
       return CUBE_OK;
     case CUBE_OPT_FAIL_ALLOC:
       if (value < 0 || value > 64) return cube_fail(c, CUBE_ERR_ARG, "allocation fault index must be 0 to 64");

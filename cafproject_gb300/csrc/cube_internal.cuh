@@ -189,11 +189,6 @@ struct cube_ctx {
   DevStats* hstats = nullptr;   // pinned
   void* cufft_work = nullptr;
   size_t cufft_work_bytes = 0;
-  // the fine force chain as this library's transforms (cube_fft.cu), for
-  // power-of-two meshes; opt_cufft = 1 keeps cuFFT
-  float2* fft_tw = nullptr;  // W_nf^m, m < nf
-  bool fft_own = false;
-  int opt_cufft = 0;
 };
 
 // ------------------------------------------------------------------ errors
@@ -711,8 +706,6 @@ int cube_fine_kick_impl(cube_ctx* c, float a_mid, float dt, bool pre = false, bo
 int cube_coarse_forces_impl(cube_ctx* c, cube_stats* st, const float* pre = nullptr);
 int cube_coarse_kick_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st, bool pre = false);
 int cube_fine_spectral_impl(cube_ctx* c, cube_stats* st, const float* pre);
-int cube_fft_init(cube_ctx* c);
-int cube_fine_chain_own(cube_ctx* c, const float* pre);
 int cube_coarse_spectral_impl(cube_ctx* c, cube_stats* st, const float* pre);
 int cube_pk_deposit(cube_ctx* c, int ng, float* rho, unsigned long long* total);
 int dep_shift(float mass);  // deposits' fixed point: total = integer * 2^-dep_shift(mass)

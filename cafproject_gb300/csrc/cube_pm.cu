@@ -611,17 +611,6 @@ int cube_fine_spectral_impl(cube_ctx* c, cube_stats* st, const float* pre) {
   cudaStream_t s = c->stream;
   int64_t nfh = c->nf / 2 + 1;
   int64_t nspec = nfh * c->nf * (int64_t)c->nf;
-  if (c->fft_own && !c->opt_cufft) {  // five passes of this library's transforms (cube_fft.cu)
-    int r = cube_fine_chain_own(c, pre);
-    if (r) return r;
-    if (st) {
-      r = cube_stats_fetch(c);
-      if (r) return r;
-      st->f2_max_fine = bits_float(c->hstats->f2_fine_bits);
-      st->testrhof = std::ldexp((double)c->hstats->rhof_fix, -dep_shift(c->p.mass_p));
-    }
-    return CUBE_OK;
-  }
   cube_phase_begin(c, PH_F_R2C);
   CUBE_FFT(c, cufftExecR2C(c->plan_f_r2c, c->rho_f, (cufftComplex*)c->rho_f));
   cube_phase_end(c, PH_F_R2C);

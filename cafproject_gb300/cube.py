@@ -48,7 +48,6 @@ OPT_RANK_WALK = 3
 OPT_DEPOSIT_FINE = 4
 OPT_DEPOSIT_COARSE = 5
 OPT_FAIL_ALLOC = 6
-OPT_CUFFT = 7
 NPHASE = 16
 
 

@@ -326,11 +326,6 @@ void* cube_stream(cube_ctx* ctx);
    of the fine / coarse density deposit (0-3; fine: 8x4x4, 4x4x4, 8x4x2,
    4x4x2 coarse cells; coarse: 8x8x8, 16x8x8, 8x8x4, 4x4x4): a tile-size
    choice for the autotuner, same exact sums for every shape.
-   CUBE_OPT_CUFFT=7: 1 runs the fine force chain (pm.f90:112-126) through
-   cuFFT and separate multiply and maxima passes; 0 (default) uses this
-   library's fused transforms where the fine mesh is a power of two from 64
-   to 2048 points a side (other sizes always use cuFFT).  Forces agree to
-   FP32 round-off; a test compares the two.
    CUBE_OPT_FAIL_ALLOC=6 is host-side fault injection for tests: value n > 0
    makes the n-th device allocation the library makes lazily (the general
    re-sort's key buffers, on first use) report failure, 0 turns it off. */
@@ -340,8 +335,7 @@ enum cube_option {
   CUBE_OPT_RANK_WALK = 3,
   CUBE_OPT_DEPOSIT_FINE = 4,
   CUBE_OPT_DEPOSIT_COARSE = 5,
-  CUBE_OPT_FAIL_ALLOC = 6,
-  CUBE_OPT_CUFFT = 7
+  CUBE_OPT_FAIL_ALLOC = 6
 };
 int cube_set_option(cube_ctx* ctx, int option, int64_t value);
 
