@@ -17,10 +17,11 @@ stream), state resident in HBM.  ``e2e``: the same metric when every step also
 uploads the state from pinned host arrays and downloads it again (what a host
 caller holding the reference's arrays pays).  ``--impl reference`` times the
 reference's CPU algorithm (the oracle restatement, OpenMP on every host core)
-on a one-tile sample per step.  ``--gpus N`` runs N independent replicas
+over whole steps of the same workload (at most two, each about half a minute).  ``--gpus N`` runs N independent replicas
 (the path does not shard on one-GPU machines); value sums them, time is the max.
 """
 import argparse
+import copy
 import json
 import os
 import statistics
@@ -55,6 +56,8 @@ def parse():
     ap.add_argument("--batched-only", action="store_true", help="run only the batched-ensemble measurement")
     ap.add_argument("--no-two-species", action="store_true", help="skip the two-species line")
     ap.add_argument("--no-redshifts", action="store_true", help="skip the later-redshift steps")
+    ap.add_argument("--redshifts", default="5,1",
+                    help="redshifts of the evolved run at which to time the step (z=0 takes ~1500 steps)")
     ap.add_argument("--two-species-only", action="store_true", help="run only the two-species measurement")
     ap.add_argument("--boxes", type=int, default=256, help="batched ensemble size")
     return ap.parse_args()
@@ -372,8 +375,17 @@ def run_gb300(args, ws, rank, lrank):
     # xp and vp travel to the device in pieces beside the re-sort's first
     # pass, pid beside the rest of it; xp, pid, rhoc and vfield to the host
     # beside PP+PM, vp behind the coarse kick
+    # every e2e step is the same step: the snapshot, its codec sigma and the
+    # time state it was taken at (a time state left to advance would drift
+    # the same snapshot by ever longer dt, until the re-sort's multi-cell path
+    # ran every step)
+    sig0 = g.get_sigma()
+    ts0 = copy.deepcopy(ts)
+
     def e2e_step():
+        ts.__dict__.update(copy.deepcopy(ts0.__dict__))
         g.upload_begin(hin["xp"], hin["vp"], hin["pid"], hin["rhoc"], hin["vfield"])
+        g.set_sigma(*sig0)
         step(after_x=lambda: g.download_begin(out))
         g.download_finish()
 
@@ -714,7 +726,8 @@ def main():
     adj = run_adjoint(args, lrank) if (rank == 0 and ws == 1 and not args.no_adjoint) else None
     bat = run_batched(args, lrank) if (rank == 0 and ws == 1 and not args.no_batched) else None
     two = run_two_species(args, lrank) if (rank == 0 and ws == 1 and not args.no_two_species) else None
-    zs = run_redshifts(args, lrank) if (rank == 0 and ws == 1 and not args.no_redshifts) else None
+    zs = (run_redshifts(args, lrank, tuple(float(z) for z in args.redshifts.split(",")))
+          if (rank == 0 and ws == 1 and not args.no_redshifts) else None)
     if rank == 0:
         p = r["p"]
         line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,

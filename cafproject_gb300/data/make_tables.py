@@ -60,4 +60,6 @@ def main(kdir):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/CUBEnu/kernels")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python make_tables.py <path to CUBEnu/kernels>")
+    main(sys.argv[1])

@@ -26,13 +26,13 @@ PI_F = np.float32(4.0) * np.arctan(np.float32(1.0))  # parameters.f90:67
 
 
 def build(force=False):
-    """Compile cube_oracle.c (plain gcc, no FMA contraction, OpenMP)."""
+    """Compile cube_oracle.c (gcc -O3, no FMA contraction, no fast-math, OpenMP)."""
     src = os.path.join(HERE, "cube_oracle.c")
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(src):
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     tmp = LIB + ".tmp%d" % os.getpid()
-    subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC",
+    subprocess.check_call(["gcc", "-O3", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC",
                            "-shared", "-o", tmp, src, "-lm"])
     os.replace(tmp, LIB)
     return LIB

@@ -32,8 +32,8 @@ def _run(monkeypatch, argv):
     monkeypatch.setattr(bench, "run_adjoint", lambda args, lrank: {"ratio": 2.3})
     monkeypatch.setattr(bench, "run_batched", lambda args, lrank: {"speedup": 2.3})
     monkeypatch.setattr(bench, "run_two_species", lambda args, lrank: {"value": 3.3e9})
-    monkeypatch.setattr(bench, "run_redshifts", lambda args, lrank: {"5": {"ms_per_step": 84.0, "value": 1.6e9},
-                                                                     "0": {"ms_per_step": 102.0, "value": 1.3e9}})
+    monkeypatch.setattr(bench, "run_redshifts", lambda args, lrank, zs: {"5": {"ms_per_step": 84.0, "value": 1.6e9},
+                                                                         "1": {"ms_per_step": 102.0, "value": 1.3e9}})
     monkeypatch.setattr(bench, "run_reference", lambda args, ws, rank: dict(value=4.8e6, ms=27000.0, n=p.npglobal,
                                                                              p=p, steps=2, step_s=[27.0, 27.0]))
     buf = io.StringIO()
@@ -55,7 +55,7 @@ def test_library_arm_line(monkeypatch):
     assert {"value", "unit", "cores", "kind", "sample"} <= set(d["cpu_baseline"])
     assert d["gpu_launches"] == 27 * 5  # this library's launches per step, as the launch list shows
     assert "workload" in d["config"] and "model" not in d["config"]
-    assert set(d["redshifts"]) == {"49", "5", "0"}
+    assert set(d["redshifts"]) == {"49", "5", "1"}
     for k in ("adjoint", "batched", "two_species"):
         assert k in d
 
