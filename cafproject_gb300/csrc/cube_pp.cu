@@ -235,7 +235,16 @@ __device__ bool pp_block(const PPArgs& a, const int C0[3], const int B[3], PPSme
     order[bins[k & 8191u] + (int)(k >> 13)] = (unsigned short)t;
   }
   __syncthreads();
-  for (int t = threadIdx.x; t < ncore; t += blockDim.x) {
+  // A crowded block (a quarter of a staged particle per fine cell or more:
+  // a few neighbours per particle and up) walks its particles in fine-cell
+  // order, so the lanes of a warp share their neighbour cells: the same trip
+  // counts and broadcast shared-memory loads.  A sparse one walks the
+  // block's own particles in slot order (no idle lanes on ring particles).
+  const bool by_cell = 4 * nst >= NF;
+  const int nwalk = by_cell ? nst : ncore;
+  for (int i = threadIdx.x; i < nwalk; i += blockDim.x) {
+    const int t = by_cell ? (int)order[i] : i;
+    if (t >= ncore) continue;  // a ring particle: a neighbour only
     float4 q = pts[t];
     int f = (int)(kinfo[t] & 8191u);
     long long F[3] = {0, 0, 0};
@@ -243,10 +252,10 @@ __device__ bool pp_block(const PPArgs& a, const int C0[3], const int B[3], PPSme
     for (int dz = -1; dz <= 1; dz++)
       for (int dy = -1; dy <= 1; dy++) {
         const int f2 = f + F0 * (dy + F1 * dz);
-        const int k1 = bins[f2 + 2];
-        for (int k = bins[f2 - 1]; k < k1; k++) {
+        const int k0 = bins[f2 - 1], k1 = bins[f2 + 2];
+        acc.npairs += (unsigned)(k1 - k0);
+        for (int k = k0; k < k1; k++) {
           float4 o = pts[order[k]];
-          acc.npairs++;
           pair_force(a, o.x - q.x, o.y - q.y, o.z - q.z, F);
         }
       }
