@@ -65,7 +65,7 @@ static void release(cube_ctx* c) {
                   c->vfield[0], c->vfield[1], c->cstart[0], c->cstart[1], c->dest, c->dframe, c->doff, c->lrank, c->offc, c->perm, c->vdense, c->rank, c->xtra,
                   c->scan_tmp, c->red_tmp, c->tan_tab, c->codec[0].dec, c->codec[1].dec, c->codec[0].bnd, c->codec[1].bnd, c->codec[0].dech, c->codec[1].dech, c->rho_f, c->force_f[0],
                   c->force_f[1], c->force_f[2], c->kern_f, c->kern_f_raw, c->rho_c, c->force_c[0],
-                  c->force_c[1], c->force_c[2], c->kern_c, c->fpp, c->pp_list[0], c->pp_list[1], c->pp_list[2], c->pp_list[3], c->pp_nlist, c->dstats,
+                  c->force_c[1], c->force_c[2], c->kern_c, c->fpp, c->pp_list[0], c->pp_list[1], c->pp_list[2], c->pp_list[3], c->pp_list[4], c->pp_scr_pts, c->pp_nlist, c->dstats,
                   c->cufft_work};
   for (void* b : bufs)
     if (b) cudaFree(b);
@@ -214,6 +214,11 @@ static int create_impl(const cube_params* p, const float* fine_table, const floa
   }
   if (p->pp_on) {
     ALLOC(c->fpp, 12 * (size_t)np);
+    // PP's global staging for cells too dense for shared memory: a cell and
+    // its fine ring stage at most 27 copies of every particle (tiny periodic
+    // boxes), capped at 2^22 entries (24 bytes each)
+    c->pp_scr_cap = std::min<int64_t>(27 * (int64_t)np + 64, (int64_t)1 << 22);
+    ALLOC(c->pp_scr_pts, 24 * (size_t)c->pp_scr_cap);
     ALLOC(c->dstats_pp, sizeof(DevStats));
     CUBE_CUDA(c, cudaMallocHost((void**)&c->hstats_pp, sizeof(DevStats)));
     CUBE_CUDA(c, cudaStreamCreateWithFlags(&c->stream_pp, cudaStreamNonBlocking));
@@ -229,9 +234,10 @@ static int create_impl(const cube_params* p, const float* fine_table, const floa
     ALLOC(c->pp_list[1], 4 * (size_t)c->pp_brick_cap);
     ALLOC(c->pp_list[2], 4 * (size_t)c->ncells);
     ALLOC(c->pp_list[3], 4 * (size_t)c->ncells);
-    ALLOC(c->pp_nlist, 16);
-    CUBE_CUDA(c, cudaMallocHost((void**)&c->pp_nlist_host, 16));
-    for (int l = 0; l < 4; l++) c->pp_nlist_host[l] = 0;
+    ALLOC(c->pp_list[4], 4 * (size_t)c->ncells);
+    ALLOC(c->pp_nlist, 32);
+    CUBE_CUDA(c, cudaMallocHost((void**)&c->pp_nlist_host, 32));
+    for (int l = 0; l < 5; l++) c->pp_nlist_host[l] = 0;
   }
   ALLOC(c->dstats, sizeof(DevStats));
   CUBE_CUDA(c, cudaMallocHost((void**)&c->hstats, sizeof(DevStats)));
@@ -512,7 +518,7 @@ extern "C" int cube_set_option(cube_ctx* c, int option, int64_t value) {
       c->opt_rank_walk = (int)value;
       return CUBE_OK;
     case CUBE_OPT_PP_LEVEL:
-      if (value < 0 || value > 4) return cube_fail(c, CUBE_ERR_ARG, "PP level must be 0 to 4");
+      if (value < 0 || value > 5) return cube_fail(c, CUBE_ERR_ARG, "PP level must be 0 to 5");
       c->opt_pp_level = (int)value;
       return CUBE_OK;
     case CUBE_OPT_DEPOSIT_FINE:

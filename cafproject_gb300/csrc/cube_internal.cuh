@@ -42,6 +42,7 @@ struct DevStats {
   unsigned int vmax_est_bits[3]; // fine kick: max |v + vfield| in FP32, when the last vmax is unknown
   double testrhof, testrhoc;
   unsigned long long rhof_fix, rhoc_fix;  // deposited mass in 2^-32 fixed point
+  unsigned int pp_overflow;               // PP cells too dense for the global staging
 };
 
 // Scalars of one step when the step runs inside a captured CUDA graph
@@ -157,7 +158,9 @@ struct cube_ctx {
   float* kern_c = nullptr;      // scaled by 1/nc^3 (exact: power of two)
   // PP
   float* fpp = nullptr;         // per-particle PP force (3*np_max): pair kernels -> kick pass
-  int* pp_list[4] = {nullptr, nullptr, nullptr, nullptr};  // work of PP levels 1-4 (bricks, bricks, cells, cells)
+  int* pp_list[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // work of PP levels 1-5 (bricks, bricks, cells x3)
+  float4* pp_scr_pts = nullptr;  // PP global staging (levels 4-5): pp_scr_cap float4, then 2 x pp_scr_cap uint32
+  int64_t pp_scr_cap = 0;
   int* pp_nlist = nullptr;          // their lengths
   int* pp_nlist_host = nullptr;     // pinned copy of the last call's lengths
   int pp_brick_cap = 0;             // ceil(nc/4)^3

@@ -9,20 +9,25 @@
 // the block and of the one-fine-cell layer around it, read from the block's
 // cells and its ring of coarse cells (storage is ordered by coarse cell), as
 // FP32 positions relative to the block (exact: 4*frac has at most 17 bits),
-// then counting-sorted by fine cell, so each particle of the block walks
-// exactly its 27 neighbouring fine cells, as the linked list does.  Pair
-// forces are FP32, each component summed in 2^-32 fixed point (int64) so the
-// sum does not depend on the visit order (bitwise reproducible whichever
-// kernel handles a particle).
+// then counting-sorted by fine cell, each fine cell's particles by index, so
+// each particle of the block walks exactly its 27 neighbouring fine cells, as
+// the linked list does.  Pair forces are FP32, summed with compensation
+// (Kahan) in that fixed order: bitwise reproducible whichever kernel handles
+// a particle, within about one rounding of the exact sum of the FP32 terms.
 //
-// Five levels keep dense regions correct without a host round trip; each
+// Six levels keep dense regions correct without a host round trip; each
 // level lists what did not fit for the next one:
 //   0. one block per brick of 4^3 coarse cells, 1536 staged particles at most
 //      (several blocks per SM; a uniform brick stages about 1100);
 //   1. listed bricks again, one 1024-thread block per SM with 8960 of room;
 //   2. the cells of bricks listed by level 1, one at a time, 1536 of room;
 //   3. listed cells with 8960 of room;
-//   4. cells still too dense, from global memory, one block per cell.
+//   4. listed cells staged in a global scratch, an equal region per block;
+//   5. the rest, one block with the whole scratch (2^22 entries at most; a
+//      cell beyond that is reported as a PP overflow, ext_pp_force.f90:41-45).
+// A crowded block walks its particles in fine-cell order, so the lanes of a
+// warp share their neighbour bins (at z = 0 this took PP from 59 to 24 ms
+// for 256^3 particles).
 // The kick (a pass of its own over the particles in storage order, from the
 // per-particle sums the pair kernels leave) adds F*a_mid*dt/(6 pi) in FP64 as
 // one product with the precomputed factor -- the FP32 pair sum already sets
@@ -40,6 +45,7 @@ constexpr int PS_MAX = PB + 2;                 // staged coarse cells per edge
 constexpr int PNS_MAX = PS_MAX * PS_MAX * PS_MAX;
 constexpr int PNCORE_MAX = PB * PB * PB;
 constexpr int PNF_MAX = (4 * PB + 2) * (4 * PB + 2) * (4 * PB + 2);
+constexpr int PNROW_MAX = (4 * PB) * (4 * PB);  // core rows of fine cells in a brick
 constexpr int PP_CAP = 1536;      // staged particles per brick (several blocks per SM)
 constexpr int PP_CAP1 = 8960;     // staged particles per single cell (one block per SM)
 constexpr int PP_THREADS = 256;
@@ -54,7 +60,8 @@ constexpr size_t PP_SMEM = pp_smem(PP_CAP, PNF_MAX);
 constexpr size_t PP_SMEM1 = pp_smem(PP_CAP1, PNF1);
 constexpr size_t PP_SMEM1B = pp_smem(PP_CAP1, PNF_MAX);
 static_assert(PP_CAP1 < 65536 && PP_CAP1 < (1 << 19), "slots are 16-bit, ranks fit 19 bits");
-static_assert(PP_SMEM1B + 4096 < 227 * 1024, "the large brick block fits the shared memory of an SM");
+static_assert(PNF_MAX < (1 << 13) && PNF1 < (1 << 8), "bins fit 13 bits (bricks) and 8 bits (cells)");
+static_assert(PP_SMEM1B + 4096 + 1024 < 227 * 1024, "the large brick block fits the shared memory of an SM");
 
 struct PPArgs {
   Geo g;
@@ -70,8 +77,12 @@ struct PPArgs {
   int exact_only;
   float* fpp;    // per-particle summed pair force (3 per particle), pair kernels -> kick pass
   int nb;        // bricks per dimension
-  int* list[4];    // work of levels 1..4: bricks, bricks, cells, cells
+  int* list[5];    // work of levels 1..5: bricks, bricks, cells, cells, cells
   int* nlist;      // their lengths
+  float4* scr_pts;     // global staging of levels 4-5 (scr_cap entries each)
+  unsigned* scr_kinfo;
+  unsigned* scr_order;
+  int64_t scr_cap;
   DevStats* st;
   const StepDev* sd;  // graph mode: the kick factors from the device
 };
@@ -83,27 +94,24 @@ __device__ __forceinline__ float fine_off(int code, int izipx) {
   return __fmul_rn(pos_off_f(code, izipx), izipx == 1 ? 4.0f / 256.0f : 4.0f / 65536.0f);
 }
 
-// v*2^32 as a two's-complement int64 from 32-bit conversions only (|v| < 2^23)
-__device__ __forceinline__ long long to_fix(float v) {
-  float a = fabsf(v);
-  float ws = __fmul_rn(a, 256.0f), fh = floorf(ws);
-  long long q = ((long long)(unsigned int)fh << 24) + (unsigned int)__fmul_rn(__fsub_rn(ws, fh), 16777216.0f);
-  return v < 0.f ? -q : q;
-}
-__device__ __forceinline__ float from_fix(long long q) {
-  bool neg = q < 0;
-  unsigned long long u = neg ? (unsigned long long)(-q) : (unsigned long long)q;
-  float hi = (float)(unsigned int)(u >> 32), lo = (float)(unsigned int)(u & 0xffffffffull);
-  float r = __fmaf_rn(lo, 2.3283064365386963e-10f, hi);
-  return neg ? -r : r;
+// Compensated (Kahan) FP32 summation: the sum of a particle's pair forces,
+// taken in one fixed order (its 27 neighbouring fine cells row by row, each
+// fine cell's particles by increasing index), so every level and every run
+// gives the same bits; the compensation keeps the sum within about one
+// rounding of the exact sum of the FP32 pair forces.
+__device__ __forceinline__ void kahan_add(float& sum, float& comp, float x) {
+  const float y = __fsub_rn(x, comp);
+  const float t = __fadd_rn(sum, y);
+  comp = __fsub_rn(__fsub_rn(t, sum), y);
+  sum = t;
 }
 
-// one pair: accumulate the force of a particle at offset r (FP32).  1/|r| is
-// the correctly rounded reciprocal square root, |r| = r^2 * (1/|r|), and
-// 1/|r|^3 three more roundings: within about two ulps like the square root
-// plus division it replaces, at fewer instructions (the approximate hardware
+// one pair: add the force of a particle at offset r (FP32).  1/|r| is the
+// correctly rounded reciprocal square root, |r| = r^2 * (1/|r|), and 1/|r|^3
+// three more roundings: within about two ulps like the square root plus
+// division it replaces, at fewer instructions (the approximate hardware
 // reciprocal square root alone moved the codes of the strongest kicks by two)
-__device__ __forceinline__ void pair_force(const PPArgs& a, float rx, float ry, float rz, long long* acc) {
+__device__ __forceinline__ void pair_force(const PPArgs& a, float rx, float ry, float rz, float* sum, float* comp) {
   // explicit roundings: every kernel evaluates the same bits for a pair
   float r2 = __fmaf_rn(rx, rx, __fmaf_rn(ry, ry, __fmul_rn(rz, rz)));
   float ri = __frsqrt_rn(r2);    // +inf for the self pair
@@ -114,19 +122,19 @@ __device__ __forceinline__ void pair_force(const PPArgs& a, float rx, float ry, 
   // pcut = 1 - 1.75 rc^3 + 0.75 rc^5  (ext_pp_force.f90:107)
   float pcut = __fmaf_rn(__fmul_rn(0.75f, rc3), __fmul_rn(rc, rc), __fmaf_rn(-1.75f, rc3, 1.0f));
   float s = __fmul_rn(__fmul_rn(a.mass, pcut), __fmul_rn(__fmul_rn(ri, ri), ri));
-  acc[0] += to_fix(__fmul_rn(s, rx));
-  acc[1] += to_fix(__fmul_rn(s, ry));
-  acc[2] += to_fix(__fmul_rn(s, rz));
+  kahan_add(sum[0], comp[0], __fmul_rn(s, rx));
+  kahan_add(sum[1], comp[1], __fmul_rn(s, ry));
+  kahan_add(sum[2], comp[2], __fmul_rn(s, rz));
 }
 
 // the summed pair force of particle p, kept for the kick pass; returns |F|^2
-__device__ __forceinline__ float pp_store_force(const PPArgs& a, int64_t p, const long long* acc) {
+__device__ __forceinline__ float pp_store_force(const PPArgs& a, int64_t p, const float* sum, const float* comp) {
   float F[3];
   for (int d = 0; d < 3; d++) {
-    F[d] = from_fix(acc[d]);
+    F[d] = __fsub_rn(sum[d], comp[d]);
     a.fpp[3 * p + d] = F[d];
   }
-  return F[0] * F[0] + F[1] * F[1] + F[2] * F[2];
+  return __fmaf_rn(F[0], F[0], __fmaf_rn(F[1], F[1], __fmul_rn(F[2], F[2])));
 }
 
 // kick + exact velocity code of every particle, in storage order (coalesced
@@ -164,7 +172,8 @@ __device__ __forceinline__ void pp_reduce(const PPArgs& a, unsigned long long np
 struct PPSmem {
   int pref[PNS_MAX + 1];         // ring-and-block particles before each staged cell
   long long sstart[PNS_MAX];     // first particle of each staged cell
-  int ncore, nring;              // staged particles of the block (slots from 0 up) and of the ring (from CAP-1 down)
+  int rows[PNROW_MAX + 1];       // crowded walk: the block's particles before each core row of fine cells
+  int ncore, nring;              // staged particles of the block (slots from 0 up) and of the ring (from cap-1 down)
 };
 
 struct PPAcc {
@@ -172,111 +181,216 @@ struct PPAcc {
   float f2max = 0.f;
 };
 
-// Pair forces + kicks for the B[0]xB[1]xB[2] coarse cells starting at C0.
-// The particles of the block and of the fine-cell layer around it are staged
-// (compacted: the block's own from slot 0 up, the ring's from CAP-1 down, so
-// the force loop runs over the block's particles without idle lanes), binned
-// by fine cell (counting sort of slot numbers), and every particle of the
-// block then walks its 27 neighbouring fine-cell bins.
-// Returns false (nothing kicked) when more than PP_CAP particles would be
-// staged.  Block-uniform control flow; ends with a barrier.
-template <int CAP>
-__device__ bool pp_block(const PPArgs& a, const int C0[3], const int B[3], PPSmem& sm, float4* dyn, PPAcc& acc) {
+// Where a block stages: shared memory (levels 0-3; 16-bit slots and bin
+// offsets) or a region of the global scratch (levels 4-5; 32-bit).
+template <typename Idx, int kBinBits>
+struct PPBuf {
+  float4* pts;      // x, y, z relative to the block, particle index
+  unsigned* kinfo;  // fine-cell bin | rank in the bin << kBinBits
+  Idx* order;       // slots by bin, each bin's by increasing particle index
+  Idx* bins;        // NF + 1 bin offsets (counts while staging)
+  int cap;
+};
+
+// add n to a bin's count, return the count before: 16-bit counts two to a
+// 32-bit word, or 32-bit counts
+__device__ __forceinline__ unsigned bin_add(unsigned short* bins, unsigned f, unsigned n) {
+  unsigned* b32 = reinterpret_cast<unsigned*>(bins);
+  const unsigned sh = 16u * (f & 1u);
+  return (atomicAdd(&b32[f >> 1], n << sh) >> sh) & 0xffffu;
+}
+__device__ __forceinline__ unsigned bin_add(unsigned* bins, unsigned f, unsigned n) { return atomicAdd(&bins[f], n); }
+
+// Pair forces for the B[0]xB[1]xB[2] coarse cells starting at C0.  The
+// particles of the block and of the fine-cell layer around it are staged
+// (compacted: the block's own from slot 0 up, the ring's from cap-1 down),
+// binned by fine cell with each bin in particle-index order, and every
+// particle of the block then walks its 27 neighbouring fine-cell bins in
+// that order.  Returns false (nothing summed) when more than cap particles
+// would be staged.  Block-uniform control flow; ends with a barrier.
+template <typename Idx, int kBinBits>
+__device__ bool pp_block(const PPArgs& a, const int C0[3], const int B[3], PPSmem& sm,
+                         const PPBuf<Idx, kBinBits>& buf, PPAcc& acc) {
   const Geo& g = a.g;
-  const int nc = g.nc;
+  const int nc = g.nc, cap = buf.cap;
   const int S0 = B[0] + 2, S1 = B[1] + 2, S2 = B[2] + 2, NS = S0 * S1 * S2;
   const int F0 = 4 * B[0] + 2, F1 = 4 * B[1] + 2, F2 = 4 * B[2] + 2, NF = F0 * F1 * F2;
-  float4* pts = dyn;                                              // x, y, z, particle index
-  unsigned* kinfo = reinterpret_cast<unsigned*>(pts + CAP);    // bin | rank in bin << 13
-  unsigned short* order = reinterpret_cast<unsigned short*>(kinfo + CAP);  // slots by bin
-  // NF+1 16-bit bin offsets, counted two to a 32-bit word
-  unsigned short* bins = order + CAP;
-  unsigned* bins32 = reinterpret_cast<unsigned*>(bins);
+  constexpr unsigned kBinMask = (1u << kBinBits) - 1u;
+  float4* pts = buf.pts;
+  unsigned* kinfo = buf.kinfo;
+  Idx* order = buf.order;
+  Idx* bins = buf.bins;
   for (int t = threadIdx.x; t < NS; t += blockDim.x) {
     int sx = t % S0, sy = (t / S0) % S1, sz = t / (S0 * S1);
     int64_t c = cell_id(g, wrap1(C0[0] + sx - 1, nc), wrap1(C0[1] + sy - 1, nc), wrap1(C0[2] + sz - 1, nc));
     sm.pref[t] = a.rhoc[c];
     sm.sstart[t] = a.cstart[c];
   }
-  for (int t = threadIdx.x; t < (NF + 2) / 2; t += blockDim.x) bins32[t] = 0u;
+  if constexpr (sizeof(Idx) == 2) {
+    unsigned* bins32 = reinterpret_cast<unsigned*>(bins);
+    for (int t = threadIdx.x; t < (NF + 2) / 2; t += blockDim.x) bins32[t] = 0u;
+  } else {
+    for (int t = threadIdx.x; t <= NF; t += blockDim.x) bins[t] = 0u;
+  }
   if (threadIdx.x == 0) sm.ncore = sm.nring = 0;
   __syncthreads();
   const int total = block_exclusive_scan(sm.pref, NS);
-  // stage the particles whose fine cell lies in the block or its fine ring
-  for_box_particles<PS_MAX>(sm.pref, sm.sstart, S0, S1 * S2, total, [&](int64_t p, int sx, int row) {
-    const int sl[3] = {sx - 1, row % S1 - 1, row / S1 - 1};
-    float x[3];
-    int fi[3];
-    bool in = true, core = true;
+  // Stage the particles whose fine cell lies in the block or its fine ring:
+  // one warp per row of staged coarse cells, in storage order.  A fine cell's
+  // particles all come from one coarse cell, so from one warp; its lanes of
+  // one pass take consecutive ranks (one atomic, lane order) after those of
+  // the warp's earlier passes, so every bin ends up in particle-index order
+  // whatever the block's shape, level or scheduling.
+  const int lane = threadIdx.x & 31, nrow = S1 * S2;
+  for (int row = threadIdx.x >> 5; row < nrow; row += blockDim.x >> 5) {
+    const int t0 = row * S0;
+    int rp[PS_MAX];
 #pragma unroll
-    for (int d = 0; d < 3; d++) {
-      x[d] = __fadd_rn((float)(4 * sl[d]), fine_off(load_code(a.xp, 3 * p + d, g.izipx), g.izipx));
-      fi[d] = (int)floorf(x[d]) + 1;  // 0 .. 4B+1 inside the staged region
-      in = in && fi[d] >= 0 && fi[d] <= 4 * B[d] + 1;
-      core = core && fi[d] >= 1 && fi[d] <= 4 * B[d];
+    for (int q = 0; q < PS_MAX; q++) rp[q] = q < S0 ? sm.pref[t0 + q] : 0x7fffffff;
+    const int jend = row + 1 < nrow ? sm.pref[t0 + S0] : total;
+    const int sly = row % S1 - 1, slz = row / S1 - 1;
+    for (int j0 = rp[0]; j0 < jend; j0 += 32) {  // warp-uniform trip count
+      const int j = j0 + lane;
+      unsigned key = 0xffffffffu;  // the lane's bin, or none
+      int slot = 0, pi = 0;
+      float x[3] = {0.f, 0.f, 0.f};
+      if (j < jend) {
+        int cs = rp[0], sx = 0;
+#pragma unroll
+        for (int q = 1; q < PS_MAX; q++)
+          if (rp[q] <= j) {
+            cs = rp[q];
+            sx = q;
+          }
+        const int64_t p = sm.sstart[t0 + sx] + (j - cs);
+        pi = (int)p;
+        const int sl[3] = {sx - 1, sly, slz};
+        int fi[3];
+        bool in = true, core = true;
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          x[d] = __fadd_rn((float)(4 * sl[d]), fine_off(load_code(a.xp, 3 * p + d, g.izipx), g.izipx));
+          fi[d] = (int)floorf(x[d]) + 1;  // 0 .. 4B+1 inside the staged region
+          in = in && fi[d] >= 0 && fi[d] <= 4 * B[d] + 1;
+          core = core && fi[d] >= 1 && fi[d] <= 4 * B[d];
+        }
+        if (in) {
+          slot = core ? atomicAdd(&sm.ncore, 1) : cap - 1 - atomicAdd(&sm.nring, 1);
+          if (slot >= 0 && slot < cap) key = (unsigned)(fi[0] + F0 * (fi[1] + F1 * fi[2]));
+        }
+      }
+      const unsigned peers = __match_any_sync(0xffffffffu, key);
+      const int leader = __ffs(peers) - 1;
+      unsigned base = 0;
+      if (key != 0xffffffffu && lane == leader) base = bin_add(bins, key, (unsigned)__popc(peers));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (key != 0xffffffffu) {
+        const unsigned r = base + (unsigned)__popc(peers & ((1u << lane) - 1u));
+        pts[slot] = make_float4(x[0], x[1], x[2], __int_as_float(pi));
+        kinfo[slot] = key | (r << kBinBits);
+      }
     }
-    if (!in) return;
-    const int slot = core ? atomicAdd(&sm.ncore, 1) : CAP - 1 - atomicAdd(&sm.nring, 1);
-    if (slot < 0 || slot >= CAP) return;
-    int f = fi[0] + F0 * (fi[1] + F1 * fi[2]);
-    const unsigned sh = 16u * (unsigned)(f & 1);
-    int r = (int)((atomicAdd(&bins32[f >> 1], 1u << sh) >> sh) & 0xffffu);
-    pts[slot] = make_float4(x[0], x[1], x[2], __int_as_float((int)p));
-    kinfo[slot] = (unsigned)f | ((unsigned)r << 13);
-  });
-  __syncthreads();
-  const int ncore = sm.ncore, nring = sm.nring, nst = ncore + nring;
-  if (nst > CAP) return false;
-  block_exclusive_scan_u16(bins, NF);
-  if (threadIdx.x == 0) bins[NF] = (unsigned short)nst;
-  for (int i = threadIdx.x; i < nst; i += blockDim.x) {
-    const int t = i < ncore ? i : CAP - nring + (i - ncore);
-    unsigned k = kinfo[t];
-    order[bins[k & 8191u] + (int)(k >> 13)] = (unsigned short)t;
   }
   __syncthreads();
+  const int ncore = sm.ncore, nring = sm.nring, nst = ncore + nring;
+  if (nst > cap) return false;
+  if constexpr (sizeof(Idx) == 2)
+    block_exclusive_scan_u16(bins, NF);
+  else
+    block_exclusive_scan(reinterpret_cast<int*>(bins), NF);
+  if (threadIdx.x == 0) bins[NF] = (Idx)nst;
+  for (int i = threadIdx.x; i < nst; i += blockDim.x) {
+    const int t = i < ncore ? i : cap - nring + (i - ncore);
+    const unsigned k = kinfo[t];
+    order[(int)bins[k & kBinMask] + (int)(k >> kBinBits)] = (Idx)t;
+  }
   // A crowded block (a quarter of a staged particle per fine cell or more:
-  // a few neighbours per particle and up) walks its particles in fine-cell
-  // order, so the lanes of a warp share their neighbour cells: the same trip
-  // counts and broadcast shared-memory loads.  A sparse one walks the
-  // block's own particles in slot order (no idle lanes on ring particles).
-  const bool by_cell = 4 * nst >= NF;
-  const int nwalk = by_cell ? nst : ncore;
-  for (int i = threadIdx.x; i < nwalk; i += blockDim.x) {
-    const int t = by_cell ? (int)order[i] : i;
-    if (t >= ncore) continue;  // a ring particle: a neighbour only
-    float4 q = pts[t];
-    int f = (int)(kinfo[t] & 8191u);
-    long long F[3] = {0, 0, 0};
-    // the three bins dx = -1..1 of one (dy, dz) row are consecutive: one range
+  // a few neighbours per particle and up) walks its own particles in bin
+  // order, so the lanes of a warp share their neighbour bins: the same trip
+  // counts and broadcast loads.  Its particles in bin order are the core
+  // rows of fine cells (4B[0] consecutive bins each) one after another.  A
+  // sparse block walks its particles in slot order.
+  const bool crowded = 4 * nst >= NF;
+  const int RX = 4 * B[1], nrc = RX * 4 * B[2];
+  if (crowded)
+    for (int r = threadIdx.x; r < nrc; r += blockDim.x) {
+      const int rs = F0 * ((1 + r % RX) + F1 * (1 + r / RX));
+      sm.rows[r] = (int)bins[rs + 4 * B[0] + 1] - (int)bins[rs + 1];
+    }
+  __syncthreads();
+  if (crowded) block_exclusive_scan(sm.rows, nrc);
+  for (int i = threadIdx.x; i < ncore; i += blockDim.x) {
+    int t = i;
+    if (crowded) {  // the core row holding the block's i-th particle in bin order
+      int lo = 0, hi = nrc;  // rows[lo] <= i < rows[hi] (rows[nrc] = ncore)
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (sm.rows[mid] <= i) lo = mid;
+        else hi = mid;
+      }
+      const int rs = F0 * ((1 + lo % RX) + F1 * (1 + lo / RX));
+      t = (int)order[(int)bins[rs + 1] + (i - sm.rows[lo])];
+    }
+    const float4 q = pts[t];
+    const int f = (int)(kinfo[t] & kBinMask);
+    float sum[3] = {0.f, 0.f, 0.f}, comp[3] = {0.f, 0.f, 0.f};
+#ifndef PP_FLAT
+#define PP_FLAT 0
+#endif
+#if PP_FLAT
+    // The three bins dx = -1..1 of one (dy, dz) row are consecutive: nine
+    // ranges, rows dz-major.  One loop over their concatenation: a warp runs
+    // as many passes as its busiest lane has pairs, not the sum over rows of
+    // each row's busiest lane.
+    int rk = 0, k = 0, kend = 0;
+    for (;;) {
+      while (k == kend && rk < 9) {
+        const int f2 = f + F0 * ((rk % 3 - 1) + F1 * (rk / 3 - 1));
+        k = (int)bins[f2 - 1];
+        kend = (int)bins[f2 + 2];
+        acc.npairs += (unsigned)(kend - k);
+        rk++;
+      }
+      if (k == kend) break;
+      const float4 o = pts[order[k++]];
+      pair_force(a, o.x - q.x, o.y - q.y, o.z - q.z, sum, comp);
+    }
+#else
     for (int dz = -1; dz <= 1; dz++)
       for (int dy = -1; dy <= 1; dy++) {
         const int f2 = f + F0 * (dy + F1 * dz);
-        const int k0 = bins[f2 - 1], k1 = bins[f2 + 2];
+        const int k0 = (int)bins[f2 - 1], k1 = (int)bins[f2 + 2];
         acc.npairs += (unsigned)(k1 - k0);
         for (int k = k0; k < k1; k++) {
-          float4 o = pts[order[k]];
-          pair_force(a, o.x - q.x, o.y - q.y, o.z - q.z, F);
+          const float4 o = pts[order[k]];
+          pair_force(a, o.x - q.x, o.y - q.y, o.z - q.z, sum, comp);
         }
       }
+#endif
     acc.nwork++;
-    acc.f2max = fmaxf(acc.f2max, pp_store_force(a, (int64_t)__float_as_int(q.w), F));
+    acc.f2max = fmaxf(acc.f2max, pp_store_force(a, (int64_t)__float_as_int(q.w), sum, comp));
   }
   __syncthreads();
   return true;
 }
 
-// Levels 0-3: kLevel selects the work item of iteration it (a brick: its
-// index, or listed; a cell: of a listed brick, or listed) and where an item
-// that did not fit is listed.
+// Levels 0-3 (shared-memory staging): kLevel selects the work item of
+// iteration it (a brick: its index, or listed; a cell: of a listed brick, or
+// listed) and where an item that did not fit is listed.
 template <int kLevel, int CAP, int NT>
 __global__ void __launch_bounds__(NT) k_pp_level(PPArgs a) {
   __shared__ PPSmem sm;
-  extern __shared__ float4 pts[];
+  extern __shared__ float4 dyn[];
   const Geo& g = a.g;
   const int nc = g.nc, nb = a.nb;
   const int n = kLevel == 0 ? nb * nb * nb
                             : (kLevel == 2 ? a.nlist[1] * PNCORE_MAX : a.nlist[kLevel - 1]);
+  PPBuf<unsigned short, 13> buf;
+  buf.pts = dyn;
+  buf.kinfo = reinterpret_cast<unsigned*>(dyn + CAP);
+  buf.order = reinterpret_cast<unsigned short*>(buf.kinfo + CAP);
+  buf.bins = buf.order + CAP;
+  buf.cap = CAP;
   PPAcc acc;
   for (int it = blockIdx.x; it < n; it += gridDim.x) {
     int C0[3], B[3];
@@ -302,7 +416,7 @@ __global__ void __launch_bounds__(NT) k_pp_level(PPArgs a) {
       }
       B[0] = B[1] = B[2] = 1;
     }
-    if (!pp_block<CAP>(a, C0, B, sm, pts, acc)) {
+    if (!pp_block(a, C0, B, sm, buf, acc)) {
       if (threadIdx.x == 0) a.list[kLevel][atomicAdd(&a.nlist[kLevel], 1)] = item;
       __syncthreads();
     }
@@ -310,52 +424,41 @@ __global__ void __launch_bounds__(NT) k_pp_level(PPArgs a) {
   pp_reduce(a, acc.npairs, acc.nwork, acc.f2max);
 }
 
-// level 4: listed cells from global memory, one CTA per cell (persistent)
-__global__ void __launch_bounds__(PP_THREADS) k_pp_dense(PPArgs a) {
+// Levels 4 and 5: listed cells staged in the global scratch (32-bit slots
+// and offsets; the bins stay in shared memory).  Level 4 gives each block an
+// equal region and lists a cell that does not fit for level 5, one block
+// with the whole scratch; a cell even that cannot hold is counted as an
+// overflow and its particles keep no PP force (the call reports it).
+template <int kLevel>
+__global__ void __launch_bounds__(PP_THREADS1) k_pp_global(PPArgs a) {
+  __shared__ PPSmem sm;
+  __shared__ unsigned bins[PNF1 + 2];
   const Geo& g = a.g;
-  const int n = a.nlist[3];
+  const int n = a.nlist[kLevel - 1];
+  const int64_t share = kLevel == 4 ? a.scr_cap / gridDim.x : a.scr_cap;
+  const int64_t off = kLevel == 4 ? share * blockIdx.x : 0;
+  PPBuf<unsigned, 8> buf;
+  buf.pts = a.scr_pts + off;
+  buf.kinfo = a.scr_kinfo + off;
+  buf.order = a.scr_order + off;
+  buf.bins = bins;
+  buf.cap = (int)share;
   PPAcc acc;
   for (int it = blockIdx.x; it < n; it += gridDim.x) {
-    int64_t c = a.list[3][it];
-    int gc[3];
-    cell_coords(g, c, gc[0], gc[1], gc[2]);
-    int64_t p1 = a.cstart[c + 1];
-    for (int64_t p = a.cstart[c] + threadIdx.x; p < p1; p += blockDim.x) {
-      float x1[3];
-      int fi[3], lo[3], hi[3];
-      for (int d = 0; d < 3; d++) {
-        x1[d] = fine_off(load_code(a.xp, 3 * p + d, g.izipx), g.izipx);
-        fi[d] = (int)floorf(x1[d]);
-        lo[d] = fi[d] == 0 ? -1 : 0;
-        hi[d] = fi[d] == g.ncell - 1 ? 1 : 0;
+    const int item = a.list[kLevel - 1][it];
+    int C0[3];
+    const int B[3] = {1, 1, 1};
+    cell_coords(g, item, C0[0], C0[1], C0[2]);
+    if (!pp_block(a, C0, B, sm, buf, acc)) {
+      if (threadIdx.x == 0) {
+        if (kLevel == 4) a.list[4][atomicAdd(&a.nlist[4], 1)] = item;
+        else atomicAdd(&a.st->pp_overflow, 1u);
       }
-      long long f[3] = {0, 0, 0};
-      for (int dz = lo[2]; dz <= hi[2]; dz++)
-        for (int dy = lo[1]; dy <= hi[1]; dy++)
-          for (int dx = lo[0]; dx <= hi[0]; dx++) {
-            int64_t S = cell_id(g, wrap1(gc[0] + dx, g.nc), wrap1(gc[1] + dy, g.nc), wrap1(gc[2] + dz, g.nc));
-            int64_t q1 = a.cstart[S + 1];
-            float sh[3] = {(float)(4 * dx), (float)(4 * dy), (float)(4 * dz)};
-            for (int64_t q = a.cstart[S]; q < q1; q++) {
-              float r[3];
-              bool near = true;
-              for (int d = 0; d < 3; d++) {
-                float x2 = __fadd_rn(sh[d], fine_off(load_code(a.xp, 3 * q + d, g.izipx), g.izipx));
-                near = near && abs((int)floorf(x2) - fi[d]) <= 1;
-                r[d] = x2 - x1[d];
-              }
-              if (!near) continue;
-              acc.npairs++;
-              pair_force(a, r[0], r[1], r[2], f);
-            }
-          }
-      acc.nwork++;
-      acc.f2max = fmaxf(acc.f2max, pp_store_force(a, p, f));
+      __syncthreads();
     }
   }
   pp_reduce(a, acc.npairs, acc.nwork, acc.f2max);
 }
-
 // forced start level (tests): list every brick, or every cell
 __global__ void k_pp_list_all(int* list, int n, int* count) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) list[i] = i;
@@ -394,9 +497,13 @@ int cube_pp_launch(cube_ctx* c, float a_mid, float dt, bool defer_kick) {
   a.nb = (c->p.nc + PB - 1) / PB;
   int64_t nbrick = (int64_t)a.nb * a.nb * a.nb;
   if (nbrick > c->pp_brick_cap) return cube_fail(c, CUBE_ERR_ARG, "PP brick list too small");
-  for (int l = 0; l < 4; l++) a.list[l] = c->pp_list[l];
+  for (int l = 0; l < 5; l++) a.list[l] = c->pp_list[l];
   a.nlist = c->pp_nlist;
-  CUBE_CUDA(c, cudaMemsetAsync(c->pp_nlist, 0, 4 * sizeof(int), c->stream));
+  a.scr_cap = c->pp_scr_cap;
+  a.scr_pts = c->pp_scr_pts;
+  a.scr_kinfo = reinterpret_cast<unsigned*>(c->pp_scr_pts + c->pp_scr_cap);
+  a.scr_order = a.scr_kinfo + c->pp_scr_cap;
+  CUBE_CUDA(c, cudaMemsetAsync(c->pp_nlist, 0, 5 * sizeof(int), c->stream));
   auto k0 = k_pp_level<0, PP_CAP, PP_THREADS>;
   auto k1 = k_pp_level<1, PP_CAP1, PP_THREADS1>;
   auto k2 = k_pp_level<2, PP_CAP, PP_THREADS>;
@@ -408,14 +515,15 @@ int cube_pp_launch(cube_ctx* c, float a_mid, float dt, bool defer_kick) {
   if (start == 1 || start == 2)
     k_pp_list_all<<<cube_grid(nbrick, 256), 256, 0, c->stream>>>(c->pp_list[start - 1], (int)nbrick,
                                                                  c->pp_nlist + start - 1);
-  else if (start >= 3)
+  else if (start >= 3)  // cells
     k_pp_list_all<<<cube_grid(c->ncells, 256), 256, 0, c->stream>>>(c->pp_list[start - 1], (int)c->ncells,
                                                                      c->pp_nlist + start - 1);
   if (start <= 0) k0<<<(unsigned)nbrick, PP_THREADS, PP_SMEM, c->stream>>>(a);
   if (start <= 1) k1<<<one_per_sm, PP_THREADS1, PP_SMEM1B, c->stream>>>(a);
   if (start <= 2) k2<<<persist, PP_THREADS, PP_SMEM, c->stream>>>(a);
   if (start <= 3) k3<<<one_per_sm, PP_THREADS1, PP_SMEM1, c->stream>>>(a);
-  k_pp_dense<<<persist, PP_THREADS, 0, c->stream>>>(a);
+  if (start <= 4) k_pp_global<4><<<one_per_sm, PP_THREADS1, 0, c->stream>>>(a);
+  k_pp_global<5><<<1, PP_THREADS1, 0, c->stream>>>(a);
   if (!defer_kick) k_pp_kick<<<cube_grid(c->np, 256), 256, 0, c->stream>>>(a);
   CUBE_CUDA(c, cudaGetLastError());
   cube_phase_end(c, PH_PP);
@@ -423,7 +531,7 @@ int cube_pp_launch(cube_ctx* c, float a_mid, float dt, bool defer_kick) {
     CUBE_CUDA(c, cudaMemcpyAsync(&c->sout->pp, c->dstats, sizeof(DevStats), cudaMemcpyDeviceToDevice, c->stream));
     return CUBE_OK;
   }
-  CUBE_CUDA(c, cudaMemcpyAsync(c->pp_nlist_host, c->pp_nlist, 4 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CUBE_CUDA(c, cudaMemcpyAsync(c->pp_nlist_host, c->pp_nlist, 5 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   return CUBE_OK;
 }
 
@@ -446,6 +554,10 @@ int cube_pp_init(cube_ctx* c) {
 int cube_pp_finish(cube_ctx* c, cube_stats* st) {
   int r = cube_stats_fetch(c);
   if (r) return r;
+  if (c->hstats->pp_overflow)
+    return cube_fail(c, CUBE_ERR_PP_OVERFLOW, "PP: " + std::to_string(c->hstats->pp_overflow) +
+                                                   " cell(s) with their fine-cell ring hold more particles than the " +
+                                                   std::to_string(c->pp_scr_cap) + " the PP scratch stages");
   if ((int64_t)c->hstats->itest1 != c->np)
     return cube_fail(c, CUBE_ERR_COUNT_MISMATCH, "PP updated a different number of particles than nplocal");
   if (st) {

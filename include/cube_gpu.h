@@ -309,12 +309,13 @@ void* cube_stream(cube_ctx* ctx);
    reference's FP64 expressions directly instead of the certified FP32 /
    float-float fast paths (results are identical by construction; used to test
    that claim and to time it).  CUBE_OPT_PP_LEVEL=2 sets the first of the
-   five PP levels (0: 4^3-cell bricks staged in shared memory, the default;
+   six PP levels (0: 4^3-cell bricks staged in shared memory, the default;
    1: bricks in a large block; 2: single cells; 3: single cells in a large
-   block; 4: global memory, one block per cell), which otherwise serve only
-   regions too dense for the level before.  The pair sums
-   are order-independent, so every level gives bitwise the same result; used
-   to test the dense-region paths.  CUBE_OPT_RANK_WALK=3 picks how
+   block; 4: single cells staged in a global scratch, a region per block;
+   5: the same with the whole scratch), which otherwise serve only regions
+   too dense for the level before.  Every level sums a particle's pairs in
+   the same order, so every level gives bitwise the same result; used to
+   test the dense-region paths.  CUBE_OPT_RANK_WALK=3 picks how
    cube_update_x finds each particle's rank in its destination cell (the
    reference's visit order): 0 (default) the counting path when every
    particle moved at most one cell and landed in one frame, else a radix

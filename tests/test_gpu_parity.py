@@ -233,12 +233,14 @@ def test_pp_dense_bricks_match_oracle():
 
 @pytest.mark.parametrize("clump", [0, 2])
 def test_pp_levels_agree_bitwise(clump):
-    # fixed-point pair sums make the result independent of which kernel (staged
-    # brick, staged cell, global memory) handles a particle
+    # every kernel (staged brick, staged cell, global-memory staging) sums a
+    # particle's pairs in the same order (neighbour fine cells row by row,
+    # each cell's particles by index), so the result does not depend on
+    # which one handles it
     p = _params(dict(nc=24, nnt=2))
     st = synth.random_state(p, mean_per_cell=6, seed=22, clump=clump, clump_mult=600)
     outs = []
-    for level in (0, 1, 2, 3, 4):
+    for level in (0, 1, 2, 3, 4, 5):
         g = C.CubeGPU(p)
         g.upload(st["xp"], st["vp"], st["pid"], st["rhoc"], st["vfield"])
         s = np.float32(st["sigma_vi"])
@@ -303,7 +305,7 @@ PP_FORCE_RTOL = 1e-5  # relative L2 of the FP32 pair-force sums vs the oracle's 
 ], ids=["uniform_x1", "uniform_x2", "clumped", "dense_bricks"])
 def test_pp_force_vector_matches_fp64(name, pk, sk):
     # f_tot of every particle (ext_pp_force.f90:94-112): the GPU sums FP32
-    # pair forces in 2^-32 fixed point, the oracle sums FP64 pair forces
+    # FP32 pair forces in a compensated sum, the oracle sums FP64 pair forces
     p = _params(pk)
     st = synth.random_state(p, **sk)
     g, o = make_pair(p, st)
