@@ -60,6 +60,9 @@ def parse():
                     help="redshifts of the evolved run at which to time the step (z=0 takes ~1500 steps)")
     ap.add_argument("--two-species-only", action="store_true", help="run only the two-species measurement")
     ap.add_argument("--boxes", type=int, default=256, help="batched ensemble size")
+    ap.add_argument("--profile-range", choices=["step", "z"], default=None,
+                    help="bracket the timed steps (step) or the last redshift's timed steps (z) with "
+                         "cudaProfilerStart/Stop, for ncu --profile-from-start off")
     return ap.parse_args()
 
 
@@ -249,11 +252,16 @@ def run_redshifts(args, lrank, zs=(5.0, 0.0)):
             for _ in range(args.warmup):
                 step()
             g.synchronize()
+            prof = args.profile_range == "z" and z == zs[-1]
+            if prof:
+                torch.cuda.profiler.start()
             e0.record(stream)
             for _ in range(args.steps):
                 pps = step()
             e1.record(stream)
             g.synchronize()
+            if prof:
+                torch.cuda.profiler.stop()
             ms = e0.elapsed_time(e1) / args.steps
             out["%g" % z] = {"ms_per_step": round(ms, 2), "value": g.nplocal() / (ms / 1000.0),
                              "pp_pairs_per_step": int(pps["npairs"]), "steps_from_ics": reached,
@@ -313,12 +321,16 @@ def run_gb300(args, ws, rank, lrank):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     g.synchronize()
     torch.cuda.synchronize()
+    if args.profile_range == "step":
+        torch.cuda.profiler.start()
     e0.record(stream)
     for _ in range(args.steps):
         step()
     e1.record(stream)
     g.synchronize()
     torch.cuda.synchronize()
+    if args.profile_range == "step":
+        torch.cuda.profiler.stop()
     ms = e0.elapsed_time(e1)
     clk = clocks.stop()
     barrier(ws)

@@ -1,6 +1,7 @@
 // cube_api.cu -- the C ABI (include/cube_gpu.h): context life cycle, state
 // transfer, field inspection, and the entry points that replace the bodies of
 // the reference subroutines update_x, ext_pp_force and particle_mesh.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -65,7 +66,8 @@ static void release(cube_ctx* c) {
                   c->vfield[0], c->vfield[1], c->cstart[0], c->cstart[1], c->dest, c->dframe, c->doff, c->lrank, c->offc, c->perm, c->vdense, c->rank, c->xtra,
                   c->scan_tmp, c->red_tmp, c->tan_tab, c->codec[0].dec, c->codec[1].dec, c->codec[0].bnd, c->codec[1].bnd, c->codec[0].dech, c->codec[1].dech, c->rho_f, c->force_f[0],
                   c->force_f[1], c->force_f[2], c->kern_f, c->kern_f_raw, c->rho_c, c->force_c[0],
-                  c->force_c[1], c->force_c[2], c->kern_c, c->fpp, c->pp_list[0], c->pp_list[1], c->pp_list[2], c->pp_list[3], c->pp_list[4], c->pp_scr_pts, c->pp_nlist, c->dstats,
+                  c->force_c[1], c->force_c[2], c->kern_c, c->fpp, c->pp_list[0], c->pp_list[1], c->pp_list[2], c->pp_list[3], c->pp_list[4], c->pp_scr_pts,
+                  c->pp_lpart[0], c->pp_lpart[1], c->pp_lpart[2], c->pp_lpart[3], c->pp_lpart[4], c->pp_nlist, c->dstats,
                   c->cufft_work};
   for (void* b : bufs)
     if (b) cudaFree(b);
@@ -214,10 +216,10 @@ static int create_impl(const cube_params* p, const float* fine_table, const floa
   }
   if (p->pp_on) {
     ALLOC(c->fpp, 12 * (size_t)np);
-    // PP's global staging for cells too dense for shared memory: a cell and
-    // its fine ring stage at most 27 copies of every particle (tiny periodic
-    // boxes), capped at 2^22 entries (24 bytes each)
-    c->pp_scr_cap = std::min<int64_t>(27 * (int64_t)np + 64, (int64_t)1 << 22);
+    // PP's global staging for cells too dense for shared memory (24 bytes an
+    // entry): a cell and its fine ring stage each particle once when nc >= 3
+    // (27 times in a smaller periodic box), and at most 2^22 entries
+    c->pp_scr_cap = std::min<int64_t>((p->nc >= 3 ? 1 : 27) * (int64_t)np, (int64_t)1 << 22) + 64;
     ALLOC(c->pp_scr_pts, 24 * (size_t)c->pp_scr_cap);
     ALLOC(c->dstats_pp, sizeof(DevStats));
     CUBE_CUDA(c, cudaMallocHost((void**)&c->hstats_pp, sizeof(DevStats)));
@@ -230,12 +232,12 @@ static int create_impl(const cube_params* p, const float* fine_table, const floa
   {
     int nb = (p->nc + 3) / 4;
     c->pp_brick_cap = nb * nb * nb;
-    ALLOC(c->pp_list[0], 4 * (size_t)c->pp_brick_cap);
-    ALLOC(c->pp_list[1], 4 * (size_t)c->pp_brick_cap);
-    ALLOC(c->pp_list[2], 4 * (size_t)c->ncells);
-    ALLOC(c->pp_list[3], 4 * (size_t)c->ncells);
-    ALLOC(c->pp_list[4], 4 * (size_t)c->ncells);
-    ALLOC(c->pp_nlist, 32);
+    for (int l = 0; l < 5; l++) {
+      const size_t cap = l < 2 ? (size_t)c->pp_brick_cap : (size_t)c->ncells;
+      ALLOC(c->pp_list[l], 4 * cap);
+      ALLOC(c->pp_lpart[l], 4 * cap);
+    }
+    ALLOC(c->pp_nlist, 64);
     CUBE_CUDA(c, cudaMallocHost((void**)&c->pp_nlist_host, 32));
     for (int l = 0; l < 5; l++) c->pp_nlist_host[l] = 0;
   }
@@ -520,6 +522,14 @@ extern "C" int cube_set_option(cube_ctx* c, int option, int64_t value) {
     case CUBE_OPT_PP_LEVEL:
       if (value < 0 || value > 5) return cube_fail(c, CUBE_ERR_ARG, "PP level must be 0 to 5");
       c->opt_pp_level = (int)value;
+      return CUBE_OK;
+    case CUBE_OPT_PP_HEAVY:
+      if (value < 0 || value > (1 << 30)) return cube_fail(c, CUBE_ERR_ARG, "PP warp-walk threshold out of range");
+      c->opt_pp_heavy = (int)value;
+      return CUBE_OK;
+    case CUBE_OPT_PP_PARTS:
+      if (value < 0 || value > 255) return cube_fail(c, CUBE_ERR_ARG, "PP parts must be 0 to 255");
+      c->opt_pp_parts = (int)value;
       return CUBE_OK;
     case CUBE_OPT_DEPOSIT_FINE:
     case CUBE_OPT_DEPOSIT_COARSE:

@@ -141,7 +141,9 @@ struct cube_ctx {
   int opt_exact_kicks = 0;
   int opt_rank_walk = 0;   // ranks: 0 counting path (sort when it does not apply), 1 walker, 2 sort
   int rank_walked = 0;     // the last update used the walker
-  int opt_pp_level = 0;  // first PP level (0-4)
+  int opt_pp_level = 0;  // first PP level (0-5)
+  int opt_pp_heavy = 0;  // PP: entries from which a crowded block walks a particle with a warp (0: default)
+  int opt_pp_parts = 0;  // PP: most parts a dense item is split into (0: default, 255)
   int opt_dep_fine = 0, opt_dep_coarse = 0;  // deposit brick shapes (0-3)
   int fail_alloc = 0;    // host fault injection: the n-th lazy allocation fails (0: off)
   cube_ctx* linked = nullptr;  // the second species linked to this context, if any
@@ -159,6 +161,7 @@ struct cube_ctx {
   // PP
   float* fpp = nullptr;         // per-particle PP force (3*np_max): pair kernels -> kick pass
   int* pp_list[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // work of PP levels 1-5 (bricks, bricks, cells x3)
+  int* pp_lpart[5] = {nullptr, nullptr, nullptr, nullptr, nullptr}; // their items' parts and claims
   float4* pp_scr_pts = nullptr;  // PP global staging (levels 4-5): pp_scr_cap float4, then 2 x pp_scr_cap uint32
   int64_t pp_scr_cap = 0;
   int* pp_nlist = nullptr;          // their lengths

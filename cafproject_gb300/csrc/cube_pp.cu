@@ -34,6 +34,7 @@
 // this kick's tolerance against the reference's FP64 sum -- and the velocity
 // code is the exact code of
 // update_particle.f90:117 (certified FP32 fast path, FP64 when ambiguous).
+#include <algorithm>
 #include <cmath>
 
 #include "cube_internal.cuh"
@@ -61,7 +62,6 @@ constexpr size_t PP_SMEM1 = pp_smem(PP_CAP1, PNF1);
 constexpr size_t PP_SMEM1B = pp_smem(PP_CAP1, PNF_MAX);
 static_assert(PP_CAP1 < 65536 && PP_CAP1 < (1 << 19), "slots are 16-bit, ranks fit 19 bits");
 static_assert(PNF_MAX < (1 << 13) && PNF1 < (1 << 8), "bins fit 13 bits (bricks) and 8 bits (cells)");
-static_assert(PP_SMEM1B + 4096 + 1024 < 227 * 1024, "the large brick block fits the shared memory of an SM");
 
 struct PPArgs {
   Geo g;
@@ -75,10 +75,13 @@ struct PPArgs {
   double kick;   // a_mid*dt/6/pi
   float kick_f;  // the same rounded to float (fast path)
   int exact_only;
+  int heavy;     // entries from which a crowded block walks a particle with a warp
+  int max_parts; // most parts a dense item is split into
   float* fpp;    // per-particle summed pair force (3 per particle), pair kernels -> kick pass
   int nb;        // bricks per dimension
   int* list[5];    // work of levels 1..5: bricks, bricks, cells, cells, cells
-  int* nlist;      // their lengths
+  int* lpart[5];   // per listed item: parts (low 8 bits), parts claimed (above)
+  int* nlist;      // their lengths (5), then each level's next-item counter (6)
   float4* scr_pts;     // global staging of levels 4-5 (scr_cap entries each)
   unsigned* scr_kinfo;
   unsigned* scr_order;
@@ -106,6 +109,43 @@ __device__ __forceinline__ void kahan_add(float& sum, float& comp, float x) {
   sum = t;
 }
 
+// v*2^32 as a two's-complement int64 from 32-bit conversions only (|v| < 2^23;
+// truncated toward zero)
+__device__ __forceinline__ long long to_fix(float v) {
+  float a = fabsf(v);
+  float ws = __fmul_rn(a, 256.0f), fh = floorf(ws);
+  long long q = ((long long)(unsigned int)fh << 24) + (unsigned int)__fmul_rn(__fsub_rn(ws, fh), 16777216.0f);
+  return v < 0.f ? -q : q;
+}
+__device__ __forceinline__ float from_fix(long long q) {
+  bool neg = q < 0;
+  unsigned long long u = neg ? (unsigned long long)(-q) : (unsigned long long)q;
+  float hi = (float)(unsigned int)(u >> 32), lo = (float)(unsigned int)(u & 0xffffffffull);
+  float r = __fmaf_rn(lo, 2.3283064365386963e-10f, hi);
+  return neg ? -r : r;
+}
+
+// A particle's neighbour list (27 fine cells, 9 row ranges, particles by
+// index) is summed in chunks of PP_CHUNK consecutive entries: each chunk's
+// pair forces in a compensated sum from zero, the chunks' values (sum minus
+// compensation) added in 2^-32 fixed point, exactly and in any order.  A
+// thread walking the whole list and a warp whose lanes take one chunk each
+// therefore give the same bits.
+constexpr int PP_CHUNK = 32;
+// entries from which a crowded block's particle is walked by a warp: only
+// extreme lists (parts already spread dense items over SMs, and the warp
+// walk's own overhead made 1024 and 256 slower at z = 0)
+constexpr int PP_HEAVY = 8192;
+constexpr int PP_HEAVY_LIST = 256;  // heavy particles a block lists (more: the warp walk scans the part)
+
+__device__ __forceinline__ void pp_fold(long long* Q, float* s, float* c) {
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    Q[d] += to_fix(__fsub_rn(s[d], c[d]));
+    s[d] = c[d] = 0.f;
+  }
+}
+
 // one pair: add the force of a particle at offset r (FP32).  1/|r| is the
 // correctly rounded reciprocal square root, |r| = r^2 * (1/|r|), and 1/|r|^3
 // three more roundings: within about two ulps like the square root plus
@@ -128,10 +168,10 @@ __device__ __forceinline__ void pair_force(const PPArgs& a, float rx, float ry, 
 }
 
 // the summed pair force of particle p, kept for the kick pass; returns |F|^2
-__device__ __forceinline__ float pp_store_force(const PPArgs& a, int64_t p, const float* sum, const float* comp) {
+__device__ __forceinline__ float pp_store_force(const PPArgs& a, int64_t p, const long long* Q) {
   float F[3];
   for (int d = 0; d < 3; d++) {
-    F[d] = __fsub_rn(sum[d], comp[d]);
+    F[d] = from_fix(Q[d]);
     a.fpp[3 * p + d] = F[d];
   }
   return __fmaf_rn(F[0], F[0], __fmaf_rn(F[1], F[1], __fmul_rn(F[2], F[2])));
@@ -173,8 +213,12 @@ struct PPSmem {
   int pref[PNS_MAX + 1];         // ring-and-block particles before each staged cell
   long long sstart[PNS_MAX];     // first particle of each staged cell
   int rows[PNROW_MAX + 1];       // crowded walk: the block's particles before each core row of fine cells
+  int heavy[PP_HEAVY_LIST];      // the part's particles left to the warp walk (walk indices)
   int ncore, nring;              // staged particles of the block (slots from 0 up) and of the ring (from cap-1 down)
+  int nheavy;
 };
+// the large brick block: staging buffers, this struct and the scans' warp sums in one SM
+static_assert(PP_SMEM1B + sizeof(PPSmem) + 512 <= 227 * 1024, "the large brick block fits the shared memory of an SM");
 
 struct PPAcc {
   unsigned long long npairs = 0, nwork = 0;
@@ -210,7 +254,7 @@ __device__ __forceinline__ unsigned bin_add(unsigned* bins, unsigned f, unsigned
 // would be staged.  Block-uniform control flow; ends with a barrier.
 template <typename Idx, int kBinBits>
 __device__ bool pp_block(const PPArgs& a, const int C0[3], const int B[3], PPSmem& sm,
-                         const PPBuf<Idx, kBinBits>& buf, PPAcc& acc) {
+                         const PPBuf<Idx, kBinBits>& buf, PPAcc& acc, int part = 0, int nparts = 1) {
   const Geo& g = a.g;
   const int nc = g.nc, cap = buf.cap;
   const int S0 = B[0] + 2, S1 = B[1] + 2, S2 = B[2] + 2, NS = S0 * S1 * S2;
@@ -232,7 +276,7 @@ __device__ bool pp_block(const PPArgs& a, const int C0[3], const int B[3], PPSme
   } else {
     for (int t = threadIdx.x; t <= NF; t += blockDim.x) bins[t] = 0u;
   }
-  if (threadIdx.x == 0) sm.ncore = sm.nring = 0;
+  if (threadIdx.x == 0) sm.ncore = sm.nring = sm.nheavy = 0;
   __syncthreads();
   const int total = block_exclusive_scan(sm.pref, NS);
   // Stage the particles whose fine cell lies in the block or its fine ring:
@@ -309,82 +353,219 @@ __device__ bool pp_block(const PPArgs& a, const int C0[3], const int B[3], PPSme
   // order, so the lanes of a warp share their neighbour bins: the same trip
   // counts and broadcast loads.  Its particles in bin order are the core
   // rows of fine cells (4B[0] consecutive bins each) one after another.  A
-  // sparse block walks its particles in slot order.
+  // sparse block walks its particles in slot order.  Part `part` of `nparts`
+  // walks the block's particles [i0, i1) in bin order (slots differ from one
+  // staging to the next; bin order does not).
   const bool crowded = 4 * nst >= NF;
+  const bool by_bin = crowded || nparts > 1;
   const int RX = 4 * B[1], nrc = RX * 4 * B[2];
-  if (crowded)
+  if (by_bin)
     for (int r = threadIdx.x; r < nrc; r += blockDim.x) {
       const int rs = F0 * ((1 + r % RX) + F1 * (1 + r / RX));
       sm.rows[r] = (int)bins[rs + 4 * B[0] + 1] - (int)bins[rs + 1];
     }
   __syncthreads();
-  if (crowded) block_exclusive_scan(sm.rows, nrc);
-  for (int i = threadIdx.x; i < ncore; i += blockDim.x) {
-    int t = i;
-    if (crowded) {  // the core row holding the block's i-th particle in bin order
-      int lo = 0, hi = nrc;  // rows[lo] <= i < rows[hi] (rows[nrc] = ncore)
-      while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (sm.rows[mid] <= i) lo = mid;
-        else hi = mid;
-      }
-      const int rs = F0 * ((1 + lo % RX) + F1 * (1 + lo / RX));
-      t = (int)order[(int)bins[rs + 1] + (i - sm.rows[lo])];
+  if (by_bin) block_exclusive_scan(sm.rows, nrc);
+  const int i0 = (int)((int64_t)ncore * part / nparts), i1 = (int)((int64_t)ncore * (part + 1) / nparts);
+  // the slot of the block's i-th particle in bin order or slot order
+  auto slot_of = [&](int i) -> int {
+    if (!by_bin) return i;
+    int lo = 0, hi = nrc;  // rows[lo] <= i < rows[hi] (rows[nrc] = ncore)
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (sm.rows[mid] <= i) lo = mid;
+      else hi = mid;
     }
+    const int rs = F0 * ((1 + lo % RX) + F1 * (1 + lo / RX));
+    return (int)order[(int)bins[rs + 1] + (i - sm.rows[lo])];
+  };
+  // the bin offset of neighbour row r (dz-major): its bins dx = -1..1 are
+  // consecutive, one range [bins[f + off - 1], bins[f + off + 2])
+  auto row_off = [&](int r) { return F0 * ((r % 3 - 1) + F1 * (r / 3 - 1)); };
+  // thread walks: one particle per thread (in a crowded block, the light ones)
+  for (int i = i0 + (int)threadIdx.x; i < i1; i += blockDim.x) {
+    const int t = slot_of(i);
     const float4 q = pts[t];
     const int f = (int)(kinfo[t] & kBinMask);
-    float sum[3] = {0.f, 0.f, 0.f}, comp[3] = {0.f, 0.f, 0.f};
-#ifndef PP_FLAT
-#define PP_FLAT 0
-#endif
-#if PP_FLAT
-    // The three bins dx = -1..1 of one (dy, dz) row are consecutive: nine
-    // ranges, rows dz-major.  One loop over their concatenation: a warp runs
-    // as many passes as its busiest lane has pairs, not the sum over rows of
-    // each row's busiest lane.
-    int rk = 0, k = 0, kend = 0;
-    for (;;) {
-      while (k == kend && rk < 9) {
-        const int f2 = f + F0 * ((rk % 3 - 1) + F1 * (rk / 3 - 1));
-        k = (int)bins[f2 - 1];
-        kend = (int)bins[f2 + 2];
-        acc.npairs += (unsigned)(kend - k);
-        rk++;
+    long long Q[3] = {0, 0, 0};
+    float s[3] = {0.f, 0.f, 0.f}, c[3] = {0.f, 0.f, 0.f};
+    int cnt = 0;
+    if (crowded) {
+      int E = 0;
+      for (int r = 0; r < 9; r++) E += (int)bins[f + row_off(r) + 2] - (int)bins[f + row_off(r) - 1];
+      if (E >= a.heavy) {  // left to the warp walk below
+        const int h = atomicAdd(&sm.nheavy, 1);
+        if (h < PP_HEAVY_LIST) sm.heavy[h] = i;
+        continue;
       }
-      if (k == kend) break;
-      const float4 o = pts[order[k++]];
-      pair_force(a, o.x - q.x, o.y - q.y, o.z - q.z, sum, comp);
-    }
-#else
-    for (int dz = -1; dz <= 1; dz++)
-      for (int dy = -1; dy <= 1; dy++) {
-        const int f2 = f + F0 * (dy + F1 * dz);
-        const int k0 = (int)bins[f2 - 1], k1 = (int)bins[f2 + 2];
-        acc.npairs += (unsigned)(k1 - k0);
-        for (int k = k0; k < k1; k++) {
+      acc.npairs += (unsigned)E;
+      for (int r = 0; r < 9; r++) {
+        const int k1 = (int)bins[f + row_off(r) + 2];
+        for (int k = (int)bins[f + row_off(r) - 1]; k < k1; k++) {
           const float4 o = pts[order[k]];
-          pair_force(a, o.x - q.x, o.y - q.y, o.z - q.z, sum, comp);
+          pair_force(a, o.x - q.x, o.y - q.y, o.z - q.z, s, c);
+          if (++cnt == PP_CHUNK) {
+            pp_fold(Q, s, c);
+            cnt = 0;
+          }
         }
       }
-#endif
+    } else {
+      // the nine ranges as one loop over their concatenation: a warp runs as
+      // many passes as its busiest lane has pairs, not the sum over rows of
+      // each row's busiest lane
+      int rk = 0, k = 0, kend = 0;
+      for (;;) {
+        while (k == kend && rk < 9) {
+          k = (int)bins[f + row_off(rk) - 1];
+          kend = (int)bins[f + row_off(rk) + 2];
+          acc.npairs += (unsigned)(kend - k);
+          rk++;
+        }
+        if (k == kend) break;
+        const float4 o = pts[order[k++]];
+        pair_force(a, o.x - q.x, o.y - q.y, o.z - q.z, s, c);
+        if (++cnt == PP_CHUNK) {
+          pp_fold(Q, s, c);
+          cnt = 0;
+        }
+      }
+    }
+    if (cnt) pp_fold(Q, s, c);
     acc.nwork++;
-    acc.f2max = fmaxf(acc.f2max, pp_store_force(a, (int64_t)__float_as_int(q.w), sum, comp));
+    acc.f2max = fmaxf(acc.f2max, pp_store_force(a, (int64_t)__float_as_int(q.w), Q));
+  }
+  // warp walks: a crowded block's heavy particles (a.heavy entries or more),
+  // one per warp, lane l taking chunks l, l+32, ...; the chunks' fixed-point
+  // values are summed across the warp, so the result is the thread walk's to
+  // the bit
+  __syncthreads();
+  const int nheavy = sm.nheavy;
+  if (crowded && nheavy > 0) {
+    // the listed heavy particles, or (list overflowed) every particle of the part
+    const bool listed = nheavy <= PP_HEAVY_LIST;
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int h = (int)(threadIdx.x >> 5); h < (listed ? nheavy : i1 - i0); h += nw) {
+      const int i = listed ? sm.heavy[h] : i0 + h;
+      const int t = slot_of(i);
+      const int f = (int)(kinfo[t] & kBinMask);
+      int E = 0;
+      for (int r = 0; r < 9; r++) E += (int)bins[f + row_off(r) + 2] - (int)bins[f + row_off(r) - 1];
+      if (E < a.heavy) continue;  // warp-uniform: every lane has the same E
+      const float4 q = pts[t];
+      const int J = (E + PP_CHUNK - 1) / PP_CHUNK;
+      long long Q[3] = {0, 0, 0};
+      for (int j0 = 0; j0 < J; j0 += 32) {
+        const int j = j0 + lane;
+        float s[3] = {0.f, 0.f, 0.f}, c[3] = {0.f, 0.f, 0.f};
+        if (j < J) {
+          // entry j*PP_CHUNK of the concatenated rows, then PP_CHUNK entries on
+          int e = j * PP_CHUNK, r = 0, k = 0, kend = 0;
+          for (;;) {
+            k = (int)bins[f + row_off(r) - 1];
+            kend = (int)bins[f + row_off(r) + 2];
+            if (e < kend - k) break;
+            e -= kend - k;
+            r++;
+          }
+          k += e;
+          for (int m = 0; m < PP_CHUNK; m++) {
+            while (k == kend && r < 8) {
+              r++;
+              k = (int)bins[f + row_off(r) - 1];
+              kend = (int)bins[f + row_off(r) + 2];
+            }
+            if (k == kend) break;
+            const float4 o = pts[order[k++]];
+            pair_force(a, o.x - q.x, o.y - q.y, o.z - q.z, s, c);
+          }
+        }
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          long long v = j < J ? to_fix(__fsub_rn(s[d], c[d])) : 0;
+          for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+          Q[d] += v;
+        }
+      }
+      if (lane == 0) {
+        acc.npairs += (unsigned)E;
+        acc.nwork++;
+        acc.f2max = fmaxf(acc.f2max, pp_store_force(a, (int64_t)__float_as_int(q.w), Q));
+      }
+    }
   }
   __syncthreads();
   return true;
 }
 
-// Levels 0-3 (shared-memory staging): kLevel selects the work item of
-// iteration it (a brick: its index, or listed; a cell: of a listed brick, or
-// listed) and where an item that did not fit is listed.
+// The next item of a listed level for this block: the lists are shared out
+// as blocks finish (a dense item can take many times another's time).
+__device__ __forceinline__ int pp_next(int* counter, int* s_it) {
+  if (threadIdx.x == 0) *s_it = atomicAdd(counter, 1);
+  __syncthreads();
+  const int it = *s_it;
+  __syncthreads();
+  return it;
+}
+
+// The next (item, part) of a listed level whose items are split into parts
+// (each part walks a slice of the item's particles, on its own SM): a cursor
+// runs over the n items, each item's word counts its parts (low 8 bits) and
+// the parts claimed so far (above).  Lock-free: each pass either claims a
+// part or moves the cursor past an item whose parts are all claimed.
+__device__ __forceinline__ bool pp_next_part(int* cursor, int n, int* word, int* s3, int& it, int& part,
+                                             int& nparts) {
+  if (threadIdx.x == 0) {
+    int ri = -1, rp = 0, rn = 1;
+    for (;;) {
+      const int cur = *(volatile int*)cursor;
+      if (cur >= n) break;
+      const int w = atomicAdd(&word[cur], 256);
+      if ((w >> 8) < (w & 255)) {
+        ri = cur;
+        rp = w >> 8;
+        rn = w & 255;
+        break;
+      }
+      atomicCAS(cursor, cur, cur + 1);
+    }
+    s3[0] = ri;
+    s3[1] = rp;
+    s3[2] = rn;
+  }
+  __syncthreads();
+  it = s3[0];
+  part = s3[1];
+  nparts = s3[2];
+  __syncthreads();
+  return it >= 0;
+}
+
+// List an item that did not fit (thread 0 of its block) for level l+1, with
+// the number of parts that level splits it into: about 2^22 staged-pair
+// candidates (core x staged particles) a part, 32 core particles at least.
+__device__ __forceinline__ void pp_list_item(const PPArgs& a, int l, int item, int ncore, int nst, bool split) {
+  const int idx = atomicAdd(&a.nlist[l], 1);
+  a.list[l][idx] = item;
+  int64_t P = 1;
+  if (split) {
+    P = (((int64_t)ncore * nst) >> 22) + 1;
+    P = min(P, (int64_t)max(1, ncore / 32));
+    P = max((int64_t)1, min(P, (int64_t)a.max_parts));
+  }
+  a.lpart[l][idx] = (int)P;
+}
+
+// Levels 0-3 (shared-memory staging).  Level 0: a brick per block; level 2:
+// the cells of the bricks level 1 could not hold; levels 1 and 3: listed
+// bricks / cells in parts.  What does not fit is listed for the next level.
 template <int kLevel, int CAP, int NT>
 __global__ void __launch_bounds__(NT) k_pp_level(PPArgs a) {
   __shared__ PPSmem sm;
+  __shared__ int s3[3];
   extern __shared__ float4 dyn[];
   const Geo& g = a.g;
   const int nc = g.nc, nb = a.nb;
-  const int n = kLevel == 0 ? nb * nb * nb
-                            : (kLevel == 2 ? a.nlist[1] * PNCORE_MAX : a.nlist[kLevel - 1]);
   PPBuf<unsigned short, 13> buf;
   buf.pts = dyn;
   buf.kinfo = reinterpret_cast<unsigned*>(dyn + CAP);
@@ -392,33 +573,52 @@ __global__ void __launch_bounds__(NT) k_pp_level(PPArgs a) {
   buf.bins = buf.order + CAP;
   buf.cap = CAP;
   PPAcc acc;
-  for (int it = blockIdx.x; it < n; it += gridDim.x) {
-    int C0[3], B[3];
-    int item;  // what is listed for the next level if this one does not fit
-    if (kLevel <= 1) {
-      const int b = kLevel == 0 ? it : a.list[0][it];
-      C0[0] = (b % nb) * PB;
-      C0[1] = ((b / nb) % nb) * PB;
-      C0[2] = (b / (nb * nb)) * PB;
-      for (int d = 0; d < 3; d++) B[d] = min(PB, nc - C0[d]);
-      item = b;
-    } else {
-      if (kLevel == 2) {
+  auto brick = [&](int b, int C0[3], int B[3]) {
+    C0[0] = (b % nb) * PB;
+    C0[1] = ((b / nb) % nb) * PB;
+    C0[2] = (b / (nb * nb)) * PB;
+    for (int d = 0; d < 3; d++) B[d] = min(PB, nc - C0[d]);
+  };
+  if (kLevel == 0 || kLevel == 2) {
+    const int n = kLevel == 0 ? nb * nb * nb : a.nlist[1] * PNCORE_MAX;
+    for (int it = kLevel == 0 ? (int)blockIdx.x : pp_next(a.nlist + 5 + kLevel, &s3[0]); it < n;
+         it = kLevel == 0 ? it + (int)gridDim.x : pp_next(a.nlist + 5 + kLevel, &s3[0])) {
+      int C0[3], B[3];
+      int item;  // what is listed for the next level if this one does not fit
+      if (kLevel == 0) {
+        brick(it, C0, B);
+        item = it;
+      } else {
         const int b = a.list[1][it / PNCORE_MAX], l = it % PNCORE_MAX;
         C0[0] = (b % nb) * PB + l % PB;
         C0[1] = ((b / nb) % nb) * PB + (l / PB) % PB;
         C0[2] = (b / (nb * nb)) * PB + l / (PB * PB);
         if (C0[0] >= nc || C0[1] >= nc || C0[2] >= nc) continue;
         item = (int)cell_id(g, C0[0], C0[1], C0[2]);
-      } else {
-        item = a.list[2][it];
-        cell_coords(g, item, C0[0], C0[1], C0[2]);
+        B[0] = B[1] = B[2] = 1;
       }
-      B[0] = B[1] = B[2] = 1;
+      if (!pp_block(a, C0, B, sm, buf, acc)) {
+        if (threadIdx.x == 0) pp_list_item(a, kLevel, item, sm.ncore, sm.ncore + sm.nring, true);
+        __syncthreads();
+      }
     }
-    if (!pp_block(a, C0, B, sm, buf, acc)) {
-      if (threadIdx.x == 0) a.list[kLevel][atomicAdd(&a.nlist[kLevel], 1)] = item;
-      __syncthreads();
+  } else {
+    const int n = a.nlist[kLevel - 1];
+    int it, part, np;
+    while (pp_next_part(a.nlist + 5 + kLevel, n, a.lpart[kLevel - 1], s3, it, part, np)) {
+      const int item = a.list[kLevel - 1][it];
+      int C0[3], B[3];
+      if (kLevel == 1) {
+        brick(item, C0, B);
+      } else {
+        cell_coords(g, item, C0[0], C0[1], C0[2]);
+        B[0] = B[1] = B[2] = 1;
+      }
+      if (!pp_block(a, C0, B, sm, buf, acc, part, np)) {
+        // level 2 takes a brick cell by cell (no parts), level 4 a cell in parts
+        if (threadIdx.x == 0 && part == 0) pp_list_item(a, kLevel, item, sm.ncore, sm.ncore + sm.nring, kLevel == 3);
+        __syncthreads();
+      }
     }
   }
   pp_reduce(a, acc.npairs, acc.nwork, acc.f2max);
@@ -426,13 +626,15 @@ __global__ void __launch_bounds__(NT) k_pp_level(PPArgs a) {
 
 // Levels 4 and 5: listed cells staged in the global scratch (32-bit slots
 // and offsets; the bins stay in shared memory).  Level 4 gives each block an
-// equal region and lists a cell that does not fit for level 5, one block
-// with the whole scratch; a cell even that cannot hold is counted as an
-// overflow and its particles keep no PP force (the call reports it).
+// equal region and takes its cells in parts; a cell that does not fit goes
+// to level 5, one block with the whole scratch; a cell even that cannot
+// hold is counted as an overflow and its particles keep no PP force (the
+// call reports it).
 template <int kLevel>
 __global__ void __launch_bounds__(PP_THREADS1) k_pp_global(PPArgs a) {
   __shared__ PPSmem sm;
   __shared__ unsigned bins[PNF1 + 2];
+  __shared__ int s3[3];
   const Geo& g = a.g;
   const int n = a.nlist[kLevel - 1];
   const int64_t share = kLevel == 4 ? a.scr_cap / gridDim.x : a.scr_cap;
@@ -444,14 +646,15 @@ __global__ void __launch_bounds__(PP_THREADS1) k_pp_global(PPArgs a) {
   buf.bins = bins;
   buf.cap = (int)share;
   PPAcc acc;
-  for (int it = blockIdx.x; it < n; it += gridDim.x) {
+  int it, part, np;
+  while (pp_next_part(a.nlist + 5 + kLevel, n, a.lpart[kLevel - 1], s3, it, part, np)) {
     const int item = a.list[kLevel - 1][it];
     int C0[3];
     const int B[3] = {1, 1, 1};
     cell_coords(g, item, C0[0], C0[1], C0[2]);
-    if (!pp_block(a, C0, B, sm, buf, acc)) {
-      if (threadIdx.x == 0) {
-        if (kLevel == 4) a.list[4][atomicAdd(&a.nlist[4], 1)] = item;
+    if (!pp_block(a, C0, B, sm, buf, acc, part, np)) {
+      if (threadIdx.x == 0 && part == 0) {
+        if (kLevel == 4) pp_list_item(a, 4, item, sm.ncore, sm.ncore + sm.nring, false);
         else atomicAdd(&a.st->pp_overflow, 1u);
       }
       __syncthreads();
@@ -459,9 +662,13 @@ __global__ void __launch_bounds__(PP_THREADS1) k_pp_global(PPArgs a) {
   }
   pp_reduce(a, acc.npairs, acc.nwork, acc.f2max);
 }
-// forced start level (tests): list every brick, or every cell
-__global__ void k_pp_list_all(int* list, int n, int* count) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) list[i] = i;
+
+// forced start level (tests): list every brick, or every cell, in `parts` parts
+__global__ void k_pp_list_all(int* list, int* word, int n, int* count, int parts) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    list[i] = i;
+    word[i] = parts;
+  }
   if (blockIdx.x == 0 && threadIdx.x == 0) *count = n;
 }
 
@@ -497,13 +704,18 @@ int cube_pp_launch(cube_ctx* c, float a_mid, float dt, bool defer_kick) {
   a.nb = (c->p.nc + PB - 1) / PB;
   int64_t nbrick = (int64_t)a.nb * a.nb * a.nb;
   if (nbrick > c->pp_brick_cap) return cube_fail(c, CUBE_ERR_ARG, "PP brick list too small");
-  for (int l = 0; l < 5; l++) a.list[l] = c->pp_list[l];
+  for (int l = 0; l < 5; l++) {
+    a.list[l] = c->pp_list[l];
+    a.lpart[l] = c->pp_lpart[l];
+  }
+  a.heavy = c->opt_pp_heavy > 0 ? c->opt_pp_heavy : PP_HEAVY;
+  a.max_parts = c->opt_pp_parts > 0 ? c->opt_pp_parts : 255;
   a.nlist = c->pp_nlist;
   a.scr_cap = c->pp_scr_cap;
   a.scr_pts = c->pp_scr_pts;
   a.scr_kinfo = reinterpret_cast<unsigned*>(c->pp_scr_pts + c->pp_scr_cap);
   a.scr_order = a.scr_kinfo + c->pp_scr_cap;
-  CUBE_CUDA(c, cudaMemsetAsync(c->pp_nlist, 0, 5 * sizeof(int), c->stream));
+  CUBE_CUDA(c, cudaMemsetAsync(c->pp_nlist, 0, 11 * sizeof(int), c->stream));
   auto k0 = k_pp_level<0, PP_CAP, PP_THREADS>;
   auto k1 = k_pp_level<1, PP_CAP1, PP_THREADS1>;
   auto k2 = k_pp_level<2, PP_CAP, PP_THREADS>;
@@ -513,16 +725,20 @@ int cube_pp_launch(cube_ctx* c, float a_mid, float dt, bool defer_kick) {
   // a forced first level lists everything for it (tests of the dense paths)
   const int start = c->opt_pp_level;
   if (start == 1 || start == 2)
-    k_pp_list_all<<<cube_grid(nbrick, 256), 256, 0, c->stream>>>(c->pp_list[start - 1], (int)nbrick,
-                                                                 c->pp_nlist + start - 1);
+    k_pp_list_all<<<cube_grid(nbrick, 256), 256, 0, c->stream>>>(c->pp_list[start - 1], c->pp_lpart[start - 1],
+                                                                 (int)nbrick, c->pp_nlist + start - 1,
+                                                                 start == 1 ? 3 : 1);
   else if (start >= 3)  // cells
-    k_pp_list_all<<<cube_grid(c->ncells, 256), 256, 0, c->stream>>>(c->pp_list[start - 1], (int)c->ncells,
-                                                                     c->pp_nlist + start - 1);
+    k_pp_list_all<<<cube_grid(c->ncells, 256), 256, 0, c->stream>>>(c->pp_list[start - 1], c->pp_lpart[start - 1],
+                                                                     (int)c->ncells, c->pp_nlist + start - 1,
+                                                                     start == 5 ? 1 : 3);
   if (start <= 0) k0<<<(unsigned)nbrick, PP_THREADS, PP_SMEM, c->stream>>>(a);
   if (start <= 1) k1<<<one_per_sm, PP_THREADS1, PP_SMEM1B, c->stream>>>(a);
   if (start <= 2) k2<<<persist, PP_THREADS, PP_SMEM, c->stream>>>(a);
   if (start <= 3) k3<<<one_per_sm, PP_THREADS1, PP_SMEM1, c->stream>>>(a);
-  if (start <= 4) k_pp_global<4><<<one_per_sm, PP_THREADS1, 0, c->stream>>>(a);
+  // level 4: a block per SM, each region at least twice level 3's room
+  const int g4 = (int)std::max<int64_t>(1, std::min<int64_t>(one_per_sm, c->pp_scr_cap / (2 * PP_CAP1)));
+  if (start <= 4) k_pp_global<4><<<g4, PP_THREADS1, 0, c->stream>>>(a);
   k_pp_global<5><<<1, PP_THREADS1, 0, c->stream>>>(a);
   if (!defer_kick) k_pp_kick<<<cube_grid(c->np, 256), 256, 0, c->stream>>>(a);
   CUBE_CUDA(c, cudaGetLastError());

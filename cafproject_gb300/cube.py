@@ -48,6 +48,8 @@ OPT_RANK_WALK = 3
 OPT_DEPOSIT_FINE = 4
 OPT_DEPOSIT_COARSE = 5
 OPT_FAIL_ALLOC = 6
+OPT_PP_HEAVY = 7
+OPT_PP_PARTS = 8
 NPHASE = 16
 
 

@@ -329,14 +329,22 @@ void* cube_stream(cube_ctx* ctx);
    choice for the autotuner, same exact sums for every shape.
    CUBE_OPT_FAIL_ALLOC=6 is host-side fault injection for tests: value n > 0
    makes the n-th device allocation the library makes lazily (the general
-   re-sort's key buffers, on first use) report failure, 0 turns it off. */
+   re-sort's key buffers, on first use) report failure, 0 turns it off.
+   CUBE_OPT_PP_HEAVY=7 sets how many neighbour entries make a particle of a
+   crowded PP block walked by a whole warp instead of one thread (0: the
+   default, 8192); the two walks give bitwise the same sums, so this too only
+   serves tests and timing.  CUBE_OPT_PP_PARTS=8 caps the parts a dense PP
+   brick or cell is split into, each part on its own SM (0: the default cap,
+   255; 1: no split); same sums for every value. */
 enum cube_option {
   CUBE_OPT_EXACT_KICKS = 1,
   CUBE_OPT_PP_LEVEL = 2,
   CUBE_OPT_RANK_WALK = 3,
   CUBE_OPT_DEPOSIT_FINE = 4,
   CUBE_OPT_DEPOSIT_COARSE = 5,
-  CUBE_OPT_FAIL_ALLOC = 6
+  CUBE_OPT_FAIL_ALLOC = 6,
+  CUBE_OPT_PP_HEAVY = 7,
+  CUBE_OPT_PP_PARTS = 8
 };
 int cube_set_option(cube_ctx* ctx, int option, int64_t value);
 

@@ -118,7 +118,7 @@ def corrected_kernel(nf):
     ks = np.maximum(ks, 1.0 / nf ** 2)
     kern = -4 * np.pi / ks
     kern[0, 0, 0] = 0.0
-    r3 = np.fft.irfftn(kern, s=(nf, nf, nf))  # normalised inverse (pencil_fft_backward divides by nf^3)
+    r3 = np.fft.irfftn(kern, s=(nf, nf, nf), axes=(0, 1, 2))  # normalised inverse (pencil_fft_backward divides by nf^3)
     phi8 = (r3[0, 0, 8] + r3[0, 8, 0] + r3[8, 0, 0] + r3[0, 0, nf - 8] + r3[0, nf - 8, 0] + r3[nf - 8, 0, 0]) / 6
     c = _freq(nf)
     rr = np.sqrt(c[:, None, None] ** 2 + c[None, :, None] ** 2 + c[None, None, :] ** 2)

@@ -239,13 +239,17 @@ def test_pp_levels_agree_bitwise(clump):
     # which one handles it
     p = _params(dict(nc=24, nnt=2))
     st = synth.random_state(p, mean_per_cell=6, seed=22, clump=clump, clump_mult=600)
+    # forced levels 1, 3 and 4 take every item in three parts; heavy = 1 walks
+    # every particle of a crowded block with a warp (chunk sums folded in
+    # order), heavy = 0 keeps the default threshold
     outs = []
-    for level in (0, 1, 2, 3, 4, 5):
+    for level, heavy in ((0, 0), (1, 0), (2, 0), (3, 0), (4, 0), (5, 0), (0, 1), (3, 1), (4, 1)):
         g = C.CubeGPU(p)
         g.upload(st["xp"], st["vp"], st["pid"], st["rhoc"], st["vfield"])
         s = np.float32(st["sigma_vi"])
         g.set_sigma(s, s)
         g.set_option(C.OPT_PP_LEVEL, level)
+        g.set_option(C.OPT_PP_HEAVY, heavy)
         outs.append((g.ext_pp_force(A_MID, DT), g.download()["vp"]))
         g.close()
     if clump:

@@ -42,7 +42,7 @@ def test_sigma8_normalisation():
 
 def test_corrected_kernel_real_space_values():
     nf = 32
-    r3 = np.fft.irfftn(I.corrected_kernel(nf), s=(nf, nf, nf))
+    r3 = np.fft.irfftn(I.corrected_kernel(nf), s=(nf, nf, nf), axes=(0, 1, 2))
     assert abs(r3[0, 0, 0] + 2.5) < 1e-9
     assert abs(r3[0, 0, 1] + 1.0) < 1e-9
     assert abs(r3[0, 3, 4] + 1.0 / 5.0) < 1e-9
