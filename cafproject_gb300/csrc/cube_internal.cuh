@@ -43,6 +43,7 @@ struct DevStats {
   double testrhof, testrhoc;
   unsigned long long rhof_fix, rhoc_fix;  // deposited mass in 2^-32 fixed point
   unsigned int pp_overflow;               // PP cells too dense for the global staging
+  unsigned int nrank_dense;               // re-sort: source cells left to k_rank_dense
 };
 
 // Scalars of one step when the step runs inside a captured CUDA graph

@@ -264,8 +264,9 @@ constexpr int NOFF = 27;
 // one thread per particle: its rank among the earlier particles of its cell
 // bound for the same neighbour (storage order); the last of them also writes
 // that neighbour's count (the counts start at zero).  Cells denser than
-// RL_MAX particles are left to the walker.
-constexpr int RL_MAX = 2048;
+// RL_MAX particles are listed for k_rank_dense (a block per cell).
+constexpr int RL_MAX = 128;
+constexpr int RD_THREADS = 256;
 
 __global__ void k_rank_local(UpdArgs a) {
   if (a.st->max_disp > 1 || a.st->ndup_list != 0) {
@@ -273,15 +274,15 @@ __global__ void k_rank_local(UpdArgs a) {
     return;
   }
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.np; p += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t S = a.pcell[p];
+    const int64_t p0 = a.cstart[S], p1 = a.cstart[S + 1];
+    if (p1 - p0 > RL_MAX) {  // the cell's first particle lists it
+      if (p == p0) a.vdense[atomicAdd(&a.st->nrank_dense, 1u)] = (int32_t)S;
+      continue;
+    }
     const int o = a.doff[p];
     if (o == 255) {
       if (a.dest[p] >= 0) atomicOr(&a.st->flags, 4);  // moved farther than one cell
-      continue;
-    }
-    const int64_t S = a.pcell[p];
-    const int64_t p0 = a.cstart[S], p1 = a.cstart[S + 1];
-    if (p1 - p0 > RL_MAX) {
-      atomicOr(&a.st->flags, 4);
       continue;
     }
     int r = 0;
@@ -293,6 +294,61 @@ __global__ void k_rank_local(UpdArgs a) {
     }
     a.lrank[p] = (uint16_t)r;
     if (last) a.offc[o * a.ncells + S] = (uint16_t)(r + 1);
+  }
+}
+
+// The source cells k_rank_local listed (over RL_MAX particles), one block
+// per cell: each particle's rank among the cell's earlier particles bound for
+// the same neighbour and the 27 counts, as k_rank_local gives them.  The
+// cell's particles go in chunks of RD_THREADS, in storage order: within a
+// warp the rank is the count of lower lanes with the same neighbour
+// (__match_any_sync), across the chunk's warps a table of per-warp counts,
+// across chunks running counts.  A cell over 65535 particles (16-bit ranks)
+// sends the step to the sort path.
+__global__ void __launch_bounds__(RD_THREADS) k_rank_dense(UpdArgs a) {
+  constexpr int NW = RD_THREADS / 32;
+  __shared__ int wcnt[NW][NOFF];
+  __shared__ int run[NOFF];
+  const int n = (int)a.st->nrank_dense;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int it = blockIdx.x; it < n; it += gridDim.x) {
+    const int64_t S = a.vdense[it];
+    const int64_t p0 = a.cstart[S], p1 = a.cstart[S + 1];
+    if (p1 - p0 > 65535) {
+      if (threadIdx.x == 0) atomicOr(&a.st->flags, 4);
+      continue;
+    }
+    for (int o = threadIdx.x; o < NOFF; o += blockDim.x) run[o] = 0;
+    for (int64_t b = p0; b < p1; b += RD_THREADS) {
+      for (int k = threadIdx.x; k < NW * NOFF; k += blockDim.x) (&wcnt[0][0])[k] = 0;
+      __syncthreads();
+      const int64_t p = b + threadIdx.x;
+      int o = 255;
+      if (p < p1) {
+        o = a.doff[p];
+        if (o == 255 && a.dest[p] >= 0) atomicOr(&a.st->flags, 4);  // moved farther than one cell
+      }
+      const unsigned peers = __match_any_sync(0xffffffffu, o);
+      const int rw = __popc(peers & ((1u << lane) - 1u));
+      if (o != 255 && rw == 0) wcnt[w][o] = __popc(peers);
+      __syncthreads();
+      if (o != 255) {
+        int r = run[o] + rw;
+        for (int v = 0; v < w; v++) r += wcnt[v][o];
+        a.lrank[p] = (uint16_t)r;
+      }
+      __syncthreads();
+      for (int k = threadIdx.x; k < NOFF; k += blockDim.x) {
+        int s = 0;
+        for (int v = 0; v < NW; v++) s += wcnt[v][k];
+        run[k] += s;
+      }
+      __syncthreads();  // the table is read before the next chunk clears it
+    }
+    __syncthreads();
+    for (int o = threadIdx.x; o < NOFF; o += blockDim.x)
+      if (run[o]) a.offc[o * a.ncells + S] = (uint16_t)run[o];
+    __syncthreads();
   }
 }
 
@@ -831,6 +887,7 @@ static int update_x_graph(cube_ctx* c) {
   k_dest<<<cube_grid(c->np, B), B, 0, s>>>(a);
   CUBE_CUDA(c, cudaMemsetAsync(c->offc, 0, sizeof(uint16_t) * NOFF * (size_t)c->ncells, s));
   k_rank_local<<<cube_grid(c->np, 256), 256, 0, s>>>(a);
+  k_rank_dense<<<cube_grid((int64_t)1 << 40, 1, 4), RD_THREADS, 0, s>>>(a);
   k_rank_base<<<cube_grid(c->ncells, 256), 256, 0, s>>>(a);
   k_rank<<<cube_grid(c->ncells, 128, 32), 128, 0, s>>>(a);
   CUBE_CUDA(c, cudaGetLastError());
@@ -944,6 +1001,7 @@ int cube_update_x_impl(cube_ctx* c, float dt_old, float dt, float vz_max, cube_s
     cube_phase_begin(c, PH_UPD_RANK);
     CUBE_CUDA(c, cudaMemsetAsync(c->offc, 0, sizeof(uint16_t) * NOFF * (size_t)c->ncells, c->stream));
     k_rank_local<<<cube_grid(c->np, 256), 256, 0, c->stream>>>(a);
+    k_rank_dense<<<cube_grid((int64_t)1 << 40, 1, 4), RD_THREADS, 0, c->stream>>>(a);
     k_rank_base<<<cube_grid(c->ncells, 256), 256, 0, c->stream>>>(a);
     cube_phase_end(c, PH_UPD_RANK);
     CUBE_CUDA(c, cudaGetLastError());

@@ -52,6 +52,10 @@ CASES = [
     # warp-per-cell pass
     ("nnt2_dense", dict(nc=24, nnt=2, izipx=1, izipv=2), dict(mean_per_cell=4, seed=5, vsig=0.02, clump=3,
                                                              clump_mult=150)),
+    # three source cells of ~3200 particles: the counting path ranks them (and
+    # every cell over 128) a block per cell (k_rank_dense), not the sort
+    ("nnt2_rankdense", dict(nc=24, nnt=2, izipx=1, izipv=2), dict(mean_per_cell=4, seed=6, vsig=0.02, clump=3,
+                                                                 clump_mult=800)),
 ]
 
 
