@@ -86,7 +86,7 @@ __global__ void k_batch_head(StepDev* sd, const float2* __restrict__ sched, int 
   const float q2 = __fdiv_rn(__fmul_rn(h.dt_mid, sd->vz_max), (float)ncell);  // :37, real(4)
   int nl = 2 * (int)ceil((double)q2) + 1;
   h.nlayer = nl < 1 ? 1 : nl;
-  for (int d = 0; d < 3; d++) h.tau[d] = __fmul_rn(0.7f, sd->vmax_prev[d]);
+  for (int d = 0; d < 3; d++) h.tau[d] = __fmul_rn(kVmaxTau, sd->vmax_prev[d]);
   h.kick = __ddiv_rn(__ddiv_rn(__dmul_rn((double)a_mid, (double)dt), 6.0), (double)CUBE_PI_F);
   h.kick_f = __double2float_rn(h.kick);
   h.cf_vi = __double2float_rn(vcoef(sd->sigma_vi));

@@ -44,7 +44,12 @@ struct DevStats {
   unsigned long long rhof_fix, rhoc_fix;  // deposited mass in 2^-32 fixed point
   unsigned int pp_overflow;               // PP cells too dense for the global staging
   unsigned int nrank_dense;               // re-sort: source cells left to k_rank_dense
+  unsigned int vmax_lo_bits[3];           // coarse kick: max of certified lower bounds of |v + vfield|
 };
+
+// share of the last step's vmax above which the coarse kick evaluates a
+// lane's |v + vfield| exactly (pm.f90:349)
+constexpr float kVmaxTau = 0.95f;
 
 // Scalars of one step when the step runs inside a captured CUDA graph
 // (cube_batch_*).  A head kernel derives them on the device at the start of

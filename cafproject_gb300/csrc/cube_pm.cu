@@ -298,7 +298,8 @@ struct KickArgs {
   float a_mid, dt;
   unsigned int* vmax_bits; // coarse kick only: exact vmax per component
   float tau[3];            // coarse kick: lanes whose |v+vfield| may reach tau are evaluated exactly
-  int vmax_only;           // recompute the exact vmax of every lane, write nothing
+  unsigned int* vmax_lo;   // coarse kick: the largest lower bound of |v+vfield| (certain to be <= vmax)
+  int vmax_only;           // rerun for the exact vmax (write nothing): lanes whose bound reaches vmax_lo
   int exact_only;          // skip the certified fast path
   unsigned long long* nexact;
   const StepDev* sd;       // graph mode: a_mid, dt, tau from the device
@@ -336,6 +337,7 @@ __global__ void __launch_bounds__(256, 4) k_kick(KickArgs a) {
   }
   const Geo& g = a.g;
   float vm[3] = {0.f, 0.f, 0.f};  // coarse: exact vmax; fine: the FP32 estimate
+  float vlo[3] = {0.f, 0.f, 0.f};  // coarse: lower bounds of |v + vfield|
   unsigned long long nex = 0;
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.np; p += (int64_t)gridDim.x * blockDim.x) {
     int64_t cell = a.pcell[p];
@@ -406,8 +408,13 @@ __global__ void __launch_bounds__(256, 4) k_kick(KickArgs a) {
       float vfd = 0.f;
       if (!kFine) {
         vfd = a.vfield[3 * cell + d];
+        // |v + vfield| of the reference's FP64 v lies in [lo, ub]
         float ub = (fabsf(vf) + E + fabsf(vfd)) * 1.000001f;
-        need_vmax = a.vmax_only || ub >= kick_tau(a, d);
+        float lo = __fmul_rn(__fsub_rn(fabsf(__fadd_rn(vf, vfd)), E), 0.99999f);
+        vlo[d] = fmaxf(vlo[d], lo);
+        // the first pass: lanes that may reach tau; the rerun: lanes that may
+        // reach the largest lower bound, which the maximum does
+        need_vmax = ub >= (a.vmax_only ? __uint_as_float(__ldg(&a.vmax_lo[d])) : kick_tau(a, d));
       } else if (a.vmax_est) {
         vm[d] = fmaxf(vm[d], fabsf(__fadd_rn(vf, a.vfield[3 * cell + d])));
       }
@@ -434,6 +441,13 @@ __global__ void __launch_bounds__(256, 4) k_kick(KickArgs a) {
       float m = vm[d];
       for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
       if ((threadIdx.x & 31) == 0) atomic_max_pos(kFine ? &a.vmax_est[d] : &a.vmax_bits[d], m);
+    }
+  }
+  if (!kFine && !a.vmax_only) {
+    for (int d = 0; d < 3; d++) {
+      float m = vlo[d];
+      for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+      if ((threadIdx.x & 31) == 0 && m > 0.f) atomic_max_pos(&a.vmax_lo[d], m);
     }
   }
   for (int o = 16; o > 0; o >>= 1) nex += __shfl_xor_sync(0xffffffffu, nex, o);
@@ -768,6 +782,7 @@ int cube_coarse_kick_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st, bo
   }
   int cur = c->cur, alt = 1 - cur;
   CUBE_CUDA(c, cudaMemsetAsync(c->dstats->vmax_bits, 0, 12, c->stream));
+  CUBE_CUDA(c, cudaMemsetAsync(c->dstats->vmax_lo_bits, 0, 12, c->stream));
   CUBE_CUDA(c, cudaMemsetAsync(&c->dstats->nexact, 0, 8, c->stream));
   k.g = make_geo(c);
   k.np = c->np;
@@ -778,9 +793,11 @@ int cube_coarse_kick_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st, bo
   k.vfield = c->vfield[cur];
   for (int d = 0; d < 3; d++) {
     k.f[d] = c->force_c[d];
-    // velocities change little per step: every lane that could reach 0.7 of the
-    // last vmax is evaluated exactly; if none does, the whole vmax is redone
-    k.tau[d] = 0.7f * c->vmax_prev[d];
+    // velocities change little per step: every lane that could reach 0.95 of
+    // the last vmax is evaluated exactly; if the maximum ends below that, a
+    // rerun evaluates the lanes that could reach this pass's largest lower
+    // bound (the maximum's lane among them)
+    k.tau[d] = kVmaxTau * c->vmax_prev[d];
   }
   // last vmax unknown: 0.7 of the fine kick's FP32 maxima instead (zero when
   // no fine kick recorded them: every lane exact)
@@ -789,6 +806,7 @@ int cube_coarse_kick_impl(cube_ctx* c, float a_mid, float dt, cube_stats* st, bo
   k.a_mid = a_mid;
   k.dt = dt;
   k.vmax_bits = c->dstats->vmax_bits;
+  k.vmax_lo = c->dstats->vmax_lo_bits;
   k.nexact = &c->dstats->nexact;
   k.vmax_only = 0;
   k.exact_only = c->opt_exact_kicks;
