@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include "cube_internal.cuh"
 
@@ -64,10 +65,11 @@ static void release(cube_ctx* c) {
   void* bufs[] = {c->xp[0], c->xp[1], c->vp[0], c->vp[1], c->pid[0], c->pid[1], c->pcell[0], c->pcell[1],
                   c->rhoc[0], c->rhoc[1],
                   c->vfield[0], c->vfield[1], c->cstart[0], c->cstart[1], c->dest, c->dframe, c->doff, c->lrank, c->offc, c->perm, c->vdense, c->rank, c->xtra,
-                  c->scan_tmp, c->red_tmp, c->tan_tab, c->codec[0].dec, c->codec[1].dec, c->codec[0].bnd, c->codec[1].bnd, c->codec[0].dech, c->codec[1].dech, c->rho_f, c->force_f[0],
+                  c->scan_tmp, c->red_tmp, c->tan_tab, c->codec[0].dec, c->codec[1].dec, c->codec[0].bnd, c->codec[1].bnd, c->codec[0].dech, c->codec[1].dech, c->codec[0].rt, c->codec[1].rt, c->rho_f, c->force_f[0],
                   c->force_f[1], c->force_f[2], c->kern_f, c->kern_f_raw, c->rho_c, c->force_c[0],
                   c->force_c[1], c->force_c[2], c->kern_c, c->fpp, c->pp_list[0], c->pp_list[1], c->pp_list[2], c->pp_list[3], c->pp_list[4], c->pp_scr_pts,
                   c->pp_lpart[0], c->pp_lpart[1], c->pp_lpart[2], c->pp_lpart[3], c->pp_lpart[4], c->pp_nlist, c->dstats,
+                  c->pp_occ, c->pp_act, c->pp_wcnt, c->pp_wstart, c->pp_arhoc, c->pp_acstart, c->pp_aidx,
                   c->cufft_work};
   for (void* b : bufs)
     if (b) cudaFree(b);
@@ -183,7 +185,8 @@ static int create_impl(const cube_params* p, const float* fine_table, const floa
   ALLOC(c->rank, 4 * np);
   c->xtra_cap = 1 << 20;
   ALLOC(c->xtra, sizeof(int4) * c->xtra_cap);
-  c->scan_tmp_bytes = 8 * (c->ncells / 256 + 1024);
+  // the cell-count scans, and PP's prefilter scan of one count per 32 particles
+  c->scan_tmp_bytes = 8 * (std::max<int64_t>(c->ncells, np / 32 + 1) / 256 + 1024);
   ALLOC(c->scan_tmp, c->scan_tmp_bytes);
   c->red_blocks = 2048;
   ALLOC(c->red_tmp, sizeof(double) * 4 * c->red_blocks);
@@ -192,6 +195,7 @@ static int create_impl(const cube_params* p, const float* fine_table, const floa
     ALLOC(c->codec[k].dec, 8 * c->nvbin);
     ALLOC(c->codec[k].dech, 8 * c->nvbin);
     ALLOC(c->codec[k].bnd, 8 * (c->nvbin / 2 + 1));
+    ALLOC(c->codec[k].rt, 4 * c->nvbin);
   }
   if (owner) {
     c->rho_f = owner->rho_f;
@@ -221,6 +225,14 @@ static int create_impl(const cube_params* p, const float* fine_table, const floa
     // (27 times in a smaller periodic box), and at most 2^22 entries
     c->pp_scr_cap = std::min<int64_t>((p->nc >= 3 ? 1 : 27) * (int64_t)np, (int64_t)1 << 22) + 64;
     ALLOC(c->pp_scr_pts, 24 * (size_t)c->pp_scr_cap);
+    const int64_t nw = (np + 31) / 32;
+    ALLOC(c->pp_occ, 16 * (size_t)c->ncells);
+    ALLOC(c->pp_act, 4 * (size_t)nw);
+    ALLOC(c->pp_wcnt, 4 * (size_t)nw);
+    ALLOC(c->pp_wstart, 8 * (size_t)(nw + 1));
+    ALLOC(c->pp_arhoc, 4 * (size_t)c->ncells);
+    ALLOC(c->pp_acstart, 8 * (size_t)(c->ncells + 1));
+    ALLOC(c->pp_aidx, 4 * (size_t)np);
     ALLOC(c->dstats_pp, sizeof(DevStats));
     CUBE_CUDA(c, cudaMallocHost((void**)&c->hstats_pp, sizeof(DevStats)));
     CUBE_CUDA(c, cudaStreamCreateWithFlags(&c->stream_pp, cudaStreamNonBlocking));
@@ -531,6 +543,10 @@ extern "C" int cube_set_option(cube_ctx* c, int option, int64_t value) {
       if (value < 0 || value > 255) return cube_fail(c, CUBE_ERR_ARG, "PP parts must be 0 to 255");
       c->opt_pp_parts = (int)value;
       return CUBE_OK;
+    case CUBE_OPT_PP_FILTER:
+      if (value < 0 || value > 2) return cube_fail(c, CUBE_ERR_ARG, "PP prefilter is 0 (automatic), 1 (off) or 2 (on)");
+      c->opt_pp_filter = (int)value;
+      return CUBE_OK;
     case CUBE_OPT_DEPOSIT_FINE:
     case CUBE_OPT_DEPOSIT_COARSE:
       if (value < 0 || value > 3) return cube_fail(c, CUBE_ERR_ARG, "deposit brick shape must be 0 to 3");
@@ -606,6 +622,16 @@ static int field_io(cube_ctx* c, int field, void* host, bool to_host) {
       if (!c->fpp) return cube_fail(c, CUBE_ERR_ARG, "PP is off for this context (pp_on = 0)");
       if (!c->have_state) return cube_fail(c, CUBE_ERR_STATE, "no state uploaded");
       CUBE_CUDA(c, cudaMemcpyAsync(host, c->fpp, 12 * (size_t)c->np, cudaMemcpyDeviceToHost, c->stream));
+      if (c->pp_act_valid) {
+        // a filtered call wrote the active particles' forces only: the others' are zero
+        std::vector<unsigned> act((size_t)((c->np + 31) / 32));
+        CUBE_CUDA(c, cudaMemcpyAsync(act.data(), c->pp_act, 4 * act.size(), cudaMemcpyDeviceToHost, c->stream));
+        CUBE_CUDA(c, cudaStreamSynchronize(c->stream));
+        float* f = (float*)host;
+        for (int64_t p = 0; p < c->np; p++)
+          if (!((act[(size_t)(p >> 5)] >> (p & 31)) & 1u)) f[3 * p] = f[3 * p + 1] = f[3 * p + 2] = 0.f;
+        return CUBE_OK;
+      }
       CUBE_CUDA(c, cudaStreamSynchronize(c->stream));
       return CUBE_OK;
     }

@@ -45,6 +45,7 @@ struct DevStats {
   unsigned int pp_overflow;               // PP cells too dense for the global staging
   unsigned int nrank_dense;               // re-sort: source cells left to k_rank_dense
   unsigned int vmax_lo_bits[3];           // coarse kick: max of certified lower bounds of |v + vfield|
+  unsigned long long pp_active;           // PP prefilter: particles with a neighbour besides themselves
 };
 
 // share of the last step's vmax above which the coarse kick evaluates a
@@ -134,6 +135,7 @@ struct cube_ctx {
     double* dec = nullptr;     // dec[v+nvbin/2] = tan code / vcoef(sigma), real(8)
     float2* dech = nullptr;    // the same split into float hi + lo
     long long* bnd = nullptr;  // bnd[n] = bits of the smallest |v| that encodes to n (n=1..nvbin/2-1)
+    int32_t* rt = nullptr;     // rt[v+nvbin/2] = the code of dec[v+nvbin/2] (a kick by zero)
   } codec[2];
   int codec_next = 0;
   float sigma_vi = 0.f, sigma_vi_new = 0.f;
@@ -173,6 +175,20 @@ struct cube_ctx {
   int* pp_nlist = nullptr;          // their lengths
   int* pp_nlist_host = nullptr;     // pinned copy of the last call's lengths
   int pp_brick_cap = 0;             // ceil(nc/4)^3
+  // PP's prefilter (cube_pp.cu): a particle whose 27 neighbouring fine cells
+  // hold no other particle has a zero pair force and a one-entry list; the
+  // staging kernels then run over the other ("active") particles only
+  unsigned long long* pp_occ = nullptr;  // 2 x ncells: occupied fine sub-cells, and those held twice or more
+  unsigned* pp_act = nullptr;            // one bit per particle: active
+  int32_t* pp_wcnt = nullptr;            // active particles per 32-particle word
+  int64_t* pp_wstart = nullptr;          // their exclusive scan (words + 1)
+  int32_t* pp_arhoc = nullptr;           // active particles per coarse cell
+  int64_t* pp_acstart = nullptr;         // and their first position in pp_aidx
+  int32_t* pp_aidx = nullptr;            // active particle indices, in storage order
+  bool pp_act_valid = false;             // the last PP launch filtered: fpp holds the active particles only
+  int opt_pp_filter = 0;                 // 0 automatic, 1 off, 2 on
+  float pp_active_frac = 0.f;            // active share of the last filtered call (0: none yet)
+  int pp_unfiltered = 0;                 // calls since the automatic choice last left the filter off
   // PP beside the PM force chain (cube_pp_particle_mesh): its own stream,
   // stats and pinned copy, and the fork / join events
   cudaStream_t stream_pp = nullptr;
@@ -391,6 +407,7 @@ struct CodecView {
   int half, nmax;  // nvbin/2, nvbin/2-1
   float cf, amp;   // vcoef(sigma) and (nvbin-1)/pi as floats (estimate only)
   const float* cfp;  // when set, cf is read from the device (graph mode)
+  const int32_t* rt;  // code of a zero kick: encode(decode(code)) (may be null)
 };
 __device__ __forceinline__ float codec_cf(const CodecView& k) { return k.cfp ? __ldg(k.cfp) : k.cf; }
 __device__ __forceinline__ double codec_decode(const CodecView& k, int code) { return __ldg(k.dec + code + k.half); }

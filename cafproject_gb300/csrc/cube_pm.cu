@@ -308,6 +308,7 @@ struct KickArgs {
   const float* fpp;              // fine kick: when set, first the PP kick by these pair forces
   float pp_kf;                   // its factor a_mid*dt/6/pi, float and double
   double pp_kd;
+  const unsigned* pp_act;        // PP prefilter: set bits are the particles PP has kicked, the others take zero kicks
 };
 __device__ __forceinline__ float kick_amid(const KickArgs& a) { return a.sd ? __ldg(&a.sd->h.a_mid) : a.a_mid; }
 __device__ __forceinline__ float kick_dt(const KickArgs& a) { return a.sd ? __ldg(&a.sd->h.dt) : a.dt; }
@@ -326,6 +327,103 @@ __device__ __forceinline__ float kick_tau(const KickArgs& a, int d) {
 // float hi is within half an ulp).  certify_abs keeps the code only when every
 // double inside that bound encodes to it; otherwise the lane runs the exact
 // chain, so the stored code is always the reference's.
+//
+// The exact chain (and, in the coarse kick, the exact |v + vfield| of lanes
+// that may set vmax) is needed by a few components in a thousand, but a warp
+// runs it whenever one of its 32 lanes needs it, on the FP64 pipe.  So each
+// warp queues those (particle, component, code) entries in shared memory and
+// runs the chain 32 entries at a time, each lane recomputing its entry's CIC
+// corners and terms (the same arithmetic, the same bits).  An entry packs
+// the particle index (bits 18 and up), the 16-bit code and the component.
+constexpr int KICK_Q = 64;  // queue entries per warp: at most 31 pending + 32 from one component
+__device__ __forceinline__ unsigned long long kick_qkey(int64_t p, int d, int code) {
+  return ((unsigned long long)p << 18) | ((unsigned long long)(code & 0xffff) << 2) | (unsigned long long)d;
+}
+
+struct KickCorners {
+  int64_t c[8];  // c111, c211, c121, c112, c122, c212, c221, c222
+  float d1[3], d2[3];
+  int64_t cell;
+};
+
+template <bool kFine>
+__device__ __forceinline__ void kick_corners(const KickArgs& a, int64_t p, KickCorners& k) {
+  const Geo& g = a.g;
+  k.cell = a.pcell[p];
+  int gc[3];
+  cell_coords(g, k.cell, gc[0], gc[1], gc[2]);
+  int i1[3], i2[3];
+  const int n = kFine ? g.nf : g.nc;
+  for (int d = 0; d < 3; d++) {
+    int T, L;
+    tile_local(g, gc[d], T, L);
+    int code = load_code(a.xp, 3 * p + d, g.izipx);
+    float tx;
+    int base;
+    if (kFine) {
+      tx = fine_tempx(g.ncell, L, code, g.izipx);  // tile-local frame (pm.f90:138)
+      base = T * g.nt * g.ncell + (int)floorf(tx);
+    } else {
+      tx = coarse_tempx(gc[d] + 1, code, g.izipx);  // global frame (pm.f90:335)
+      base = (int)floorf(tx);
+    }
+    float fl = floorf(tx);
+    k.d1[d] = __fsub_rn(__fadd_rn(fl, 1.0f), tx);
+    k.d2[d] = __fsub_rn(1.0f, k.d1[d]);
+    i1[d] = wrap1(base, n);
+    i2[d] = wrap1(base + 1, n);
+  }
+  k.c[0] = mesh_idx(n, i1[0], i1[1], i1[2]);
+  k.c[1] = mesh_idx(n, i2[0], i1[1], i1[2]);
+  k.c[2] = mesh_idx(n, i1[0], i2[1], i1[2]);
+  k.c[3] = mesh_idx(n, i1[0], i1[1], i2[2]);
+  k.c[4] = mesh_idx(n, i1[0], i2[1], i2[2]);
+  k.c[5] = mesh_idx(n, i2[0], i1[1], i2[2]);
+  k.c[6] = mesh_idx(n, i2[0], i2[1], i1[2]);
+  k.c[7] = mesh_idx(n, i2[0], i2[1], i2[2]);
+}
+
+// the eight real(4) CIC terms of component d, in the reference's order
+template <bool kPre>
+__device__ __forceinline__ void kick_terms(const KickArgs& a, const KickCorners& k, int d, float t[8]) {
+  const float* F = a.f[d];
+  const float* d1 = k.d1;
+  const float* d2 = k.d2;
+#define KT(c, wa, wb, wc) (kPre ? kick_w(__ldg(F + (c)), wa, wb, wc) : kick_term(__ldg(F + (c)), kick_amid(a), kick_dt(a), wa, wb, wc))
+  t[0] = KT(k.c[0], d1[0], d1[1], d1[2]);
+  t[1] = KT(k.c[1], d2[0], d1[1], d1[2]);
+  t[2] = KT(k.c[2], d1[0], d2[1], d1[2]);
+  t[3] = KT(k.c[3], d1[0], d1[1], d2[2]);
+  t[4] = KT(k.c[4], d1[0], d2[1], d2[2]);
+  t[5] = KT(k.c[5], d2[0], d1[1], d2[2]);
+  t[6] = KT(k.c[6], d2[0], d2[1], d1[2]);
+  t[7] = KT(k.c[7], d2[0], d2[1], d2[2]);
+#undef KT
+}
+
+// one queued component on the reference's FP64 chain: its code, and in the
+// coarse kick vmax=max(vmax,abs(vreal+vfield)) (pm.f90:349) as real(4)
+template <bool kFine, bool kPre>
+__device__ __forceinline__ void kick_exact_entry(const KickArgs& a, unsigned long long key, float vm[3]) {
+  const int64_t p = (int64_t)(key >> 18);
+  const int d = (int)(key & 3ull);
+  const int code = (int)(int16_t)(uint16_t)((key >> 2) & 0xffffull);
+  KickCorners k;
+  kick_corners<kFine>(a, p, k);
+  float t[8];
+  kick_terms<kPre>(a, k, d, t);
+  double v = codec_decode(a.cin, code);
+  for (int i = 0; i < 8; i++) v = __dadd_rn(v, (double)t[i]);
+  if (!kFine) {
+    const double w = fabs(__dadd_rn(v, (double)a.vfield[3 * k.cell + d]));
+    const float wf = __double2float_rn(w);
+    vm[0] = d == 0 ? fmaxf(vm[0], wf) : vm[0];
+    vm[1] = d == 1 ? fmaxf(vm[1], wf) : vm[1];
+    vm[2] = d == 2 ? fmaxf(vm[2], wf) : vm[2];
+  }
+  if (!a.vmax_only) store_code(a.vp_out, 3 * p + d, a.g.izipv, codec_encode(a.cout, v));
+}
+
 // kPre: the meshes hold force*a_mid*dt/6/pi already (k_f2max<true>)
 template <bool kFine, bool kPre>
 __global__ void __launch_bounds__(256, 4) k_kick(KickArgs a) {
@@ -335,63 +433,43 @@ __global__ void __launch_bounds__(256, 4) k_kick(KickArgs a) {
       if (!(__uint_as_float(*(volatile unsigned int*)&a.vmax_bits[d]) >= kick_tau(a, d))) need = true;
     if (!need) return;
   }
+  __shared__ unsigned long long s_q[8][KICK_Q];  // 256 threads: 8 warps
   const Geo& g = a.g;
+  const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
+  int qn = 0;                      // queued entries of this warp (warp-uniform)
   float vm[3] = {0.f, 0.f, 0.f};  // coarse: exact vmax; fine: the FP32 estimate
   float vlo[3] = {0.f, 0.f, 0.f};  // coarse: lower bounds of |v + vfield|
   unsigned long long nex = 0;
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.np; p += (int64_t)gridDim.x * blockDim.x) {
-    int64_t cell = a.pcell[p];
-    int gc[3];
-    cell_coords(g, cell, gc[0], gc[1], gc[2]);
-    int i1[3], i2[3];
-    float d1[3], d2[3];
-    int n = kFine ? g.nf : g.nc;
-    for (int d = 0; d < 3; d++) {
-      int T, L;
-      tile_local(g, gc[d], T, L);
-      int code = load_code(a.xp, 3 * p + d, g.izipx);
-      float tx;
-      int base;
-      if (kFine) {
-        tx = fine_tempx(g.ncell, L, code, g.izipx);  // tile-local frame (pm.f90:138)
-        base = T * g.nt * g.ncell + (int)floorf(tx);
-      } else {
-        tx = coarse_tempx(gc[d] + 1, code, g.izipx);  // global frame (pm.f90:335)
-        base = (int)floorf(tx);
-      }
-      float fl = floorf(tx);
-      d1[d] = __fsub_rn(__fadd_rn(fl, 1.0f), tx);
-      d2[d] = __fsub_rn(1.0f, d1[d]);
-      i1[d] = wrap1(base, n);
-      i2[d] = wrap1(base + 1, n);
-    }
-    int64_t c111 = mesh_idx(n, i1[0], i1[1], i1[2]), c211 = mesh_idx(n, i2[0], i1[1], i1[2]);
-    int64_t c121 = mesh_idx(n, i1[0], i2[1], i1[2]), c112 = mesh_idx(n, i1[0], i1[1], i2[2]);
-    int64_t c122 = mesh_idx(n, i1[0], i2[1], i2[2]), c212 = mesh_idx(n, i2[0], i1[1], i2[2]);
-    int64_t c221 = mesh_idx(n, i2[0], i2[1], i1[2]), c222 = mesh_idx(n, i2[0], i2[1], i2[2]);
+  // whole warps iterate together (the queue's ballots); lanes past the end
+  // compute on the last particle and store nothing
+  for (int64_t p0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p0 - lane < a.np;
+       p0 += (int64_t)gridDim.x * blockDim.x) {
+    const bool valid = p0 < a.np;
+    const int64_t p = valid ? p0 : a.np - 1;
+    KickCorners k;
+    kick_corners<kFine>(a, p, k);
     int codes[3];
 #pragma unroll
     for (int d = 0; d < 3; d++) codes[d] = load_code(a.vp_in, 3 * p + d, g.izipv);
-    if (kFine && a.fpp) {
-      // ext_pp_force's kick (ext_pp_force.f90:116-121) before the fine kick,
-      // both in this pass: the PP code (decoded and encoded with sigma_vi) is
-      // the one the fine kick decodes
+    if (kFine && a.pp_act) {
+      // ext_pp_force's kick (ext_pp_force.f90:116-121) before the fine kick:
+      // the prefilter's active particles were kicked by PP already; the
+      // others' force is zero, their PP code the zero-kick code of theirs
+      const bool on = (__ldg(a.pp_act + (p >> 5)) >> (p & 31)) & 1u;
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        const int z = __ldg(a.cin.rt + codes[d] + a.cin.half);
+        codes[d] = on ? codes[d] : z;
+      }
+    } else if (kFine && a.fpp) {
+      // ext_pp_force's kick before the fine kick, both in this pass: the PP
+      // code (decoded and encoded with sigma_vi) is the one the fine kick decodes
       const float F[3] = {a.fpp[3 * p], a.fpp[3 * p + 1], a.fpp[3 * p + 2]};
       pp_kick3(a.cin, codes, F, a.pp_kf, a.pp_kd, a.exact_only);
     }
     for (int d = 0; d < 3; d++) {
-      const float* F = a.f[d];
       float t[8];
-#define KT(c, wa, wb, wc) (kPre ? kick_w(__ldg(F + (c)), wa, wb, wc) : kick_term(__ldg(F + (c)), kick_amid(a), kick_dt(a), wa, wb, wc))
-      t[0] = KT(c111, d1[0], d1[1], d1[2]);
-      t[1] = KT(c211, d2[0], d1[1], d1[2]);
-      t[2] = KT(c121, d1[0], d2[1], d1[2]);
-      t[3] = KT(c112, d1[0], d1[1], d2[2]);
-      t[4] = KT(c122, d1[0], d2[1], d2[2]);
-      t[5] = KT(c212, d2[0], d1[1], d2[2]);
-      t[6] = KT(c221, d2[0], d2[1], d1[2]);
-      t[7] = KT(c222, d2[0], d2[1], d2[2]);
-#undef KT
+      kick_terms<kPre>(a, k, d, t);
       const int code = codes[d];
       float dh = codec_decode_ff(a.cin, code).x;
       float S = t[0], T = fabsf(t[0]);
@@ -405,36 +483,40 @@ __global__ void __launch_bounds__(256, 4) k_kick(KickArgs a) {
       long long nc_ = 0;
       bool ok = !a.exact_only && certify_abs(ab, E, a.cout, &nc_);
       bool need_vmax = false;
-      float vfd = 0.f;
       if (!kFine) {
-        vfd = a.vfield[3 * cell + d];
+        const float vfd = a.vfield[3 * k.cell + d];
         // |v + vfield| of the reference's FP64 v lies in [lo, ub]
         float ub = (fabsf(vf) + E + fabsf(vfd)) * 1.000001f;
         float lo = __fmul_rn(__fsub_rn(fabsf(__fadd_rn(vf, vfd)), E), 0.99999f);
-        vlo[d] = fmaxf(vlo[d], lo);
+        if (valid) vlo[d] = fmaxf(vlo[d], lo);
         // the first pass: lanes that may reach tau; the rerun: lanes that may
         // reach the largest lower bound, which the maximum does
         need_vmax = ub >= (a.vmax_only ? __uint_as_float(__ldg(&a.vmax_lo[d])) : kick_tau(a, d));
-      } else if (a.vmax_est) {
-        vm[d] = fmaxf(vm[d], fabsf(__fadd_rn(vf, a.vfield[3 * cell + d])));
+      } else if (a.vmax_est && valid) {
+        vm[d] = fmaxf(vm[d], fabsf(__fadd_rn(vf, a.vfield[3 * k.cell + d])));
       }
-      long long out;
-      if (ok && !need_vmax) {
-        out = vb < 0 ? -nc_ : nc_;
-      } else {
-        // the reference's exact FP64 chain
-        double v = codec_decode(a.cin, code);
-        for (int i = 0; i < 8; i++) v = __dadd_rn(v, (double)t[i]);
-        out = codec_encode(a.cout, v);
-        nex++;
-        if (!kFine) {
-          // vmax=max(vmax,abs(vreal+vfield)) (pm.f90:349), real(4) result
-          double w = fabs(__dadd_rn(v, (double)vfd));
-          vm[d] = fmaxf(vm[d], __double2float_rn(w));
+      const bool fast = ok && !need_vmax;
+      if (fast && valid && !a.vmax_only) store_code(a.vp_out, 3 * p + d, g.izipv, vb < 0 ? -nc_ : nc_);
+      const bool defer = valid && !fast;
+      const unsigned m = __ballot_sync(0xffffffffu, defer);
+      if (m) {
+        if (defer) s_q[wq][qn + __popc(m & ((1u << lane) - 1u))] = kick_qkey(p, d, code);
+        qn += __popc(m);
+        // the chain for 32 queued entries at a time, one per lane
+        if (qn >= 32) {
+          __syncwarp();
+          kick_exact_entry<kFine, kPre>(a, s_q[wq][qn - 32 + lane], vm);
+          nex++;
+          qn -= 32;
+          __syncwarp();
         }
       }
-      if (!a.vmax_only) store_code(a.vp_out, 3 * p + d, g.izipv, out);
     }
+  }
+  __syncwarp();
+  if (lane < qn) {
+    kick_exact_entry<kFine, kPre>(a, s_q[wq][lane], vm);
+    nex++;
   }
   if (!kFine || a.vmax_est) {
     for (int d = 0; d < 3; d++) {
@@ -658,7 +740,10 @@ int cube_fine_kick_impl(cube_ctx* c, float a_mid, float dt, bool pre, bool with_
   KickArgs k{};
   if (with_pp) {  // the PP kick of cube_pp_launch(.., defer_kick), applied here
     if (c->graph_mode || !c->fpp) return cube_fail(c, CUBE_ERR_ARG, "PP kick in the fine kick: eager mode with PP only");
-    k.fpp = c->fpp;
+    if (c->pp_act_valid)
+      k.pp_act = c->pp_act;  // the active particles are kicked; the others take the zero-kick codes here
+    else
+      k.fpp = c->fpp;
     k.pp_kd = (((double)a_mid * (double)dt) / 6.0) / (double)CUBE_PI_F;
     k.pp_kf = (float)k.pp_kd;
   }

@@ -88,6 +88,9 @@ struct PPArgs {
   int64_t scr_cap;
   DevStats* st;
   const StepDev* sd;  // graph mode: the kick factors from the device
+  const int32_t* pidx;  // prefilter: staged positions -> particle index (null: the identity)
+  const unsigned* act;  // prefilter: one bit per particle, set where fpp was written (null: all)
+  const int64_t* nact;  // prefilter: the number of active particles (the entries of pidx)
 };
 __device__ __forceinline__ float pp_kick_f(const PPArgs& a) { return a.sd ? __ldg(&a.sd->h.kick_f) : a.kick_f; }
 __device__ __forceinline__ double pp_kick_d(const PPArgs& a) { return a.sd ? __ldg(&a.sd->h.kick) : a.kick; }
@@ -184,6 +187,27 @@ __global__ void __launch_bounds__(256) k_pp_kick(PPArgs a) {
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.np; p += (int64_t)gridDim.x * blockDim.x) {
     float F[3];
     int code[3];
+    // a particle the prefilter left out has a zero pair force (fpp not written)
+    const bool on = !a.act || ((__ldg(a.act + (p >> 5)) >> (p & 31)) & 1u);
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      F[d] = on ? a.fpp[3 * p + d] : 0.f;
+      code[d] = load_code(a.vp, 3 * p + d, g.izipv);
+    }
+    pp_kick3(a.cv, code, F, pp_kick_f(a), pp_kick_d(a), a.exact_only);
+#pragma unroll
+    for (int d = 0; d < 3; d++) store_code(a.vp, 3 * p + d, g.izipv, code[d]);
+  }
+}
+
+// With the prefilter: the kick of the active particles (the list pidx) ...
+__global__ void __launch_bounds__(256) k_pp_kick_active(PPArgs a) {
+  const Geo& g = a.g;
+  const int64_t n = __ldg(a.nact);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = __ldg(a.pidx + i);
+    float F[3];
+    int code[3];
 #pragma unroll
     for (int d = 0; d < 3; d++) {
       F[d] = a.fpp[3 * p + d];
@@ -192,6 +216,17 @@ __global__ void __launch_bounds__(256) k_pp_kick(PPArgs a) {
     pp_kick3(a.cv, code, F, pp_kick_f(a), pp_kick_d(a), a.exact_only);
 #pragma unroll
     for (int d = 0; d < 3; d++) store_code(a.vp, 3 * p + d, g.izipv, code[d]);
+  }
+}
+// ... and of the others: a zero force, so each code becomes the code of its
+// own decoded value (the codec's zero-kick table)
+__global__ void __launch_bounds__(256) k_pp_kick_idle(PPArgs a) {
+  const Geo& g = a.g;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.np; p += (int64_t)gridDim.x * blockDim.x) {
+    if ((__ldg(a.act + (p >> 5)) >> (p & 31)) & 1u) continue;
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+      store_code(a.vp, 3 * p + d, g.izipv, __ldg(a.cv.rt + load_code(a.vp, 3 * p + d, g.izipv) + a.cv.half));
   }
 }
 
@@ -279,60 +314,73 @@ __device__ bool pp_block(const PPArgs& a, const int C0[3], const int B[3], PPSme
   if (threadIdx.x == 0) sm.ncore = sm.nring = sm.nheavy = 0;
   __syncthreads();
   const int total = block_exclusive_scan(sm.pref, NS);
-  // Stage the particles whose fine cell lies in the block or its fine ring:
-  // one warp per row of staged coarse cells, in storage order.  A fine cell's
-  // particles all come from one coarse cell, so from one warp; its lanes of
-  // one pass take consecutive ranks (one atomic, lane order) after those of
-  // the warp's earlier passes, so every bin ends up in particle-index order
-  // whatever the block's shape, level or scheduling.
-  const int lane = threadIdx.x & 31, nrow = S1 * S2;
-  for (int row = threadIdx.x >> 5; row < nrow; row += blockDim.x >> 5) {
-    const int t0 = row * S0;
-    int rp[PS_MAX];
-#pragma unroll
-    for (int q = 0; q < PS_MAX; q++) rp[q] = q < S0 ? sm.pref[t0 + q] : 0x7fffffff;
-    const int jend = row + 1 < nrow ? sm.pref[t0 + S0] : total;
-    const int sly = row % S1 - 1, slz = row / S1 - 1;
-    for (int j0 = rp[0]; j0 < jend; j0 += 32) {  // warp-uniform trip count
-      const int j = j0 + lane;
-      unsigned key = 0xffffffffu;  // the lane's bin, or none
-      int slot = 0, pi = 0;
-      float x[3] = {0.f, 0.f, 0.f};
-      if (j < jend) {
-        int cs = rp[0], sx = 0;
-#pragma unroll
-        for (int q = 1; q < PS_MAX; q++)
-          if (rp[q] <= j) {
-            cs = rp[q];
-            sx = q;
-          }
-        const int64_t p = sm.sstart[t0 + sx] + (j - cs);
-        pi = (int)p;
-        const int sl[3] = {sx - 1, sly, slz};
-        int fi[3];
-        bool in = true, core = true;
-#pragma unroll
-        for (int d = 0; d < 3; d++) {
-          x[d] = __fadd_rn((float)(4 * sl[d]), fine_off(load_code(a.xp, 3 * p + d, g.izipx), g.izipx));
-          fi[d] = (int)floorf(x[d]) + 1;  // 0 .. 4B+1 inside the staged region
-          in = in && fi[d] >= 0 && fi[d] <= 4 * B[d] + 1;
-          core = core && fi[d] >= 1 && fi[d] <= 4 * B[d];
-        }
-        if (in) {
-          slot = core ? atomicAdd(&sm.ncore, 1) : cap - 1 - atomicAdd(&sm.nring, 1);
-          if (slot >= 0 && slot < cap) key = (unsigned)(fi[0] + F0 * (fi[1] + F1 * fi[2]));
-        }
+  if (threadIdx.x == 0) sm.pref[NS] = total;
+  __syncthreads();
+  // Stage the particles whose fine cell lies in the block or its fine ring.
+  // The staged cells' particles, in storage order, are split into one
+  // contiguous range of whole cells per warp (about equal counts), which the
+  // warp takes 32 at a time.  A fine cell's particles all come from one
+  // coarse cell, so from one warp; its lanes of one pass take consecutive
+  // ranks (one atomic, lane order) after those of the warp's earlier passes,
+  // so every bin ends up in particle-index order whatever the block's shape,
+  // level or scheduling.
+  const int lane = threadIdx.x & 31, nwarp = blockDim.x >> 5, wid = threadIdx.x >> 5;
+  // the first staged cell whose prefix reaches target (pref[NS] = total)
+  auto first_cell = [&](int target) {
+    int lo = 0, hi = NS;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (sm.pref[mid] < target) lo = mid + 1;
+      else hi = mid;
+    }
+    return lo;
+  };
+  const int ca = first_cell((int)((int64_t)total * wid / nwarp));
+  const int cb = wid + 1 < nwarp ? first_cell((int)((int64_t)total * (wid + 1) / nwarp)) : NS;
+  const int jend = sm.pref[cb];
+  const int S01 = S0 * S1;
+  for (int j0 = sm.pref[ca]; j0 < jend; j0 += 32) {  // warp-uniform trip count
+    const int j = j0 + lane;
+    unsigned key = 0xffffffffu;  // the lane's bin, or none
+    int slot = 0, pi = 0;
+    float x[3] = {0.f, 0.f, 0.f};
+    if (j < jend) {
+      // the staged cell holding j: the last one in [ca, cb) whose prefix is <= j
+      int lo = ca, hi = cb - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (sm.pref[mid] <= j) lo = mid;
+        else hi = mid - 1;
       }
-      const unsigned peers = __match_any_sync(0xffffffffu, key);
-      const int leader = __ffs(peers) - 1;
-      unsigned base = 0;
-      if (key != 0xffffffffu && lane == leader) base = bin_add(bins, key, (unsigned)__popc(peers));
-      base = __shfl_sync(0xffffffffu, base, leader);
-      if (key != 0xffffffffu) {
-        const unsigned r = base + (unsigned)__popc(peers & ((1u << lane) - 1u));
-        pts[slot] = make_float4(x[0], x[1], x[2], __int_as_float(pi));
-        kinfo[slot] = key | (r << kBinBits);
+      const int t = lo;
+      const int sz = t / S01, sy = (t - sz * S01) / S0, sx = t - sz * S01 - sy * S0;
+      const int64_t q = sm.sstart[t] + (j - sm.pref[t]);
+      const int64_t p = a.pidx ? (int64_t)__ldg(a.pidx + q) : q;
+      pi = (int)p;
+      const int sl[3] = {sx - 1, sy - 1, sz - 1};
+      int fi[3];
+      bool in = true, core = true;
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        x[d] = __fadd_rn((float)(4 * sl[d]), fine_off(load_code(a.xp, 3 * p + d, g.izipx), g.izipx));
+        fi[d] = (int)floorf(x[d]) + 1;  // 0 .. 4B+1 inside the staged region
+        in = in && fi[d] >= 0 && fi[d] <= 4 * B[d] + 1;
+        core = core && fi[d] >= 1 && fi[d] <= 4 * B[d];
       }
+      if (in) {
+        slot = core ? atomicAdd(&sm.ncore, 1) : cap - 1 - atomicAdd(&sm.nring, 1);
+        if (slot >= 0 && slot < cap) key = (unsigned)(fi[0] + F0 * (fi[1] + F1 * fi[2]));
+      }
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    const int leader = __ffs(peers) - 1;
+    unsigned base = 0;
+    if (key != 0xffffffffu && lane == leader) base = bin_add(bins, key, (unsigned)__popc(peers));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (key != 0xffffffffu) {
+      const unsigned r = base + (unsigned)__popc(peers & ((1u << lane) - 1u));
+      pts[slot] = make_float4(x[0], x[1], x[2], __int_as_float(pi));
+      kinfo[slot] = key | (r << kBinBits);
     }
   }
   __syncthreads();
@@ -672,7 +720,179 @@ __global__ void k_pp_list_all(int* list, int* word, int n, int* count, int parts
   if (blockIdx.x == 0 && threadIdx.x == 0) *count = n;
 }
 
+// ------------------------------------------------------------- prefilter
+// A particle's list holds the particles of its 27 neighbouring fine cells
+// (ext_pp_force.f90:94-96); when that is the particle itself alone, its pair
+// force is zero and its list has one entry.  The relation is symmetric, so
+// every neighbour of a particle with a longer list has one too: staging only
+// the particles with a neighbour ("active") gives each of them the same list
+// in the same order as staging every particle, hence the same bits.  Per
+// coarse cell a 64-bit mask holds the occupied fine sub-cells (bit x + 4y +
+// 16z) and a second those held by two particles or more; each particle then
+// tests the sub-cells within one fine cell of its own, in its cell and the
+// (up to 7) neighbouring cells they reach.  The active particles are
+// compacted in storage order with per-cell counts and starts, which the
+// staging kernels read in place of rhoc and cstart.
+struct PPFilter {
+  Geo g;
+  int64_t np, ncells;
+  const void* xp;
+  const int32_t* pcell;
+  const int32_t* rhoc;
+  const int64_t* cstart;
+  unsigned long long* occ;    // ncells occupied masks, then ncells multiple masks
+  unsigned* act;              // a bit per particle
+  int32_t* wcnt;              // active particles per word of act
+  const int64_t* wstart;      // exclusive scan of wcnt
+  int32_t* arhoc;
+  int64_t* acstart;
+  int32_t* aidx;
+  DevStats* st;
+};
+
+// fine sub-cell of particle p in its coarse cell: the top two bits of each
+// unsigned position code (floor(4*(code+0.5)/2^(8*izipx)), pm.f90 / ext_pp_force.f90:91)
+__device__ __forceinline__ void sub_cell(const void* xp, int64_t p, int izipx, int s[3]) {
+  const int m = (1 << (8 * izipx)) - 1, sh = 8 * izipx - 2;
+#pragma unroll
+  for (int d = 0; d < 3; d++) s[d] = (load_code(xp, 3 * p + d, izipx) & m) >> sh;
+}
+
+// a cell's occupied sub-cells and those held twice or more: one thread per
+// coarse cell over its particles (no atomics; every cell's words written)
+__global__ void __launch_bounds__(256) k_pp_occ(PPFilter f) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < f.ncells; c += (int64_t)gridDim.x * blockDim.x) {
+    const int n = __ldg(f.rhoc + c);
+    const int64_t p0 = __ldg(f.cstart + c);
+    unsigned long long m = 0ull, t = 0ull;
+    for (int j = 0; j < n; j++) {
+      int s[3];
+      sub_cell(f.xp, p0 + j, f.g.izipx, s);
+      const unsigned long long b = 1ull << (s[0] + 4 * (s[1] + 4 * s[2]));
+      t |= m & b;
+      m |= b;
+    }
+    f.occ[c] = m;
+    f.occ[f.ncells + c] = t;
+  }
+}
+
+// sub-cells whose coordinate d lies in [lo, hi] (0 <= lo <= hi <= 3)
+__device__ __forceinline__ unsigned long long sub_range(int d, int lo, int hi) {
+  if (d == 0) return (unsigned long long)((2u << hi) - (1u << lo)) * 0x1111111111111111ull;
+  if (d == 1) return (unsigned long long)((16u << (4 * hi)) - (1u << (4 * lo))) * 0x0001000100010001ull;
+  const unsigned long long top = hi == 3 ? 0ull : 1ull << (16 * (hi + 1));
+  return top - (1ull << (16 * lo));
+}
+
+// the part of cell_id that coordinate d contributes (cell_id is their sum:
+// ix + nt*iy + nt^2*iz + nt^3*(tx + nnt*ty + nnt^2*tz))
+__device__ __forceinline__ uint32_t cell_part(const Geo& g, int d, int gc) {
+  const uint32_t t = fdiv((uint32_t)gc, g.dnt), i = (uint32_t)gc - t * (uint32_t)g.nt;
+  const uint32_t nt = (uint32_t)g.nt, nt3 = nt * nt * nt, nnt = (uint32_t)g.nnt;
+  if (d == 0) return i + nt3 * t;
+  if (d == 1) return nt * i + nt3 * nnt * t;
+  return nt * nt * i + nt3 * nnt * nnt * t;
+}
+
+// the particle's own cell and, per dimension where its sub-cell touches a
+// face, the neighbouring cell: up to 8 cells, their words loaded together
+__global__ void __launch_bounds__(256) k_pp_active(PPFilter f) {
+  const Geo& g = f.g;
+  const int lane = threadIdx.x & 31, nc = g.nc;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  unsigned long long nact = 0, nidle = 0;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p - lane < f.np; p += stride) {
+    const bool v = p < f.np;
+    bool act = false;
+    if (v) {
+      const int cell = __ldg(f.pcell + p);
+      int s[3], gc[3];
+      sub_cell(f.xp, p, g.izipx, s);
+      cell_coords(g, cell, gc[0], gc[1], gc[2]);
+      const int sb = s[0] + 4 * (s[1] + 4 * s[2]);
+      uint32_t part[3][2];
+      unsigned long long rng[3][2];
+      int nopt[3];
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        part[d][0] = cell_part(g, d, gc[d]);
+        rng[d][0] = sub_range(d, max(s[d] - 1, 0), min(s[d] + 1, 3));
+        const int o = s[d] == 0 ? -1 : (s[d] == 3 ? 1 : 0);
+        nopt[d] = o ? 2 : 1;
+        part[d][1] = o ? cell_part(g, d, wrap1(gc[d] + o, nc)) : part[d][0];
+        rng[d][1] = sub_range(d, o < 0 ? 3 : 0, o < 0 ? 3 : 0);
+      }
+      unsigned long long w[8];
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        const int ix = k & 1, iy = (k >> 1) & 1, iz = k >> 2;
+        w[k] = (ix < nopt[0] && iy < nopt[1] && iz < nopt[2])
+                   ? __ldg(f.occ + (part[0][ix] + part[1][iy] + part[2][iz])) & rng[0][ix] & rng[1][iy] & rng[2][iz]
+                   : 0ull;
+      }
+      w[0] &= ~(1ull << sb);  // itself in its own cell
+      unsigned long long any = (__ldg(f.occ + f.ncells + cell) >> sb) & 1ull;  // another in its own fine cell
+#pragma unroll
+      for (int k = 0; k < 8; k++) any |= w[k];
+      act = any != 0ull;
+    }
+    const unsigned b = __ballot_sync(0xffffffffu, v && act);
+    if (lane == 0) {
+      f.act[p >> 5] = b;
+      f.wcnt[p >> 5] = __popc(b);
+    }
+    nact += (v && act) ? 1 : 0;
+    nidle += (v && !act) ? 1 : 0;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    nact += __shfl_xor_sync(0xffffffffu, nact, o);
+    nidle += __shfl_xor_sync(0xffffffffu, nidle, o);
+  }
+  if (lane == 0) {
+    // a particle left out has the one entry of itself and a zero force (itest1 counts it)
+    if (nidle) {
+      atomicAdd(&f.st->npairs, nidle);
+      atomicAdd(&f.st->itest1, nidle);
+    }
+    if (nact) atomicAdd(&f.st->pp_active, nact);
+  }
+}
+
+// active particles before storage position q
+__device__ __forceinline__ int64_t act_prefix(const PPFilter& f, int64_t q) {
+  const int64_t w = q >> 5;
+  const int r = (int)(q & 31);
+  return r == 0 ? __ldg(f.wstart + w) : __ldg(f.wstart + w) + __popc(__ldg(f.act + w) & ((1u << r) - 1u));
+}
+
+__global__ void __launch_bounds__(256) k_pp_acells(PPFilter f) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < f.ncells; c += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s0 = __ldg(f.cstart + c);
+    const int64_t a0 = act_prefix(f, s0);
+    f.acstart[c] = a0;
+    f.arhoc[c] = (int32_t)(act_prefix(f, s0 + __ldg(f.rhoc + c)) - a0);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_pp_aidx(PPFilter f) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < f.np; p += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned w = __ldg(f.act + (p >> 5));
+    const int r = (int)(p & 31);
+    if ((w >> r) & 1u) f.aidx[__ldg(f.wstart + (p >> 5)) + __popc(w & ((1u << r) - 1u))] = (int32_t)p;
+  }
+}
+
 }  // namespace
+
+// whether this PP launch runs the prefilter: automatic while under half of
+// the particles had a neighbour at the last filtered call (a uniform early
+// state has about one in ten), re-tried every 16th call otherwise
+static bool pp_filter_on(cube_ctx* c) {
+  if (!c->pp_occ || c->graph_mode || c->p.nc < 4 || c->opt_pp_filter == 1) return false;
+  if (c->opt_pp_filter == 2 || c->pp_active_frac < 0.5f) return true;
+  return ++c->pp_unfiltered % 16 == 0;
+}
 
 // every PP launch on c->stream (stats in c->dstats); the host reads nothing
 int cube_pp_launch(cube_ctx* c, float a_mid, float dt, bool defer_kick) {
@@ -716,12 +936,50 @@ int cube_pp_launch(cube_ctx* c, float a_mid, float dt, bool defer_kick) {
   a.scr_kinfo = reinterpret_cast<unsigned*>(c->pp_scr_pts + c->pp_scr_cap);
   a.scr_order = a.scr_kinfo + c->pp_scr_cap;
   CUBE_CUDA(c, cudaMemsetAsync(c->pp_nlist, 0, 11 * sizeof(int), c->stream));
+  a.pidx = nullptr;
+  a.act = nullptr;
+  a.nact = nullptr;
+  c->pp_act_valid = pp_filter_on(c) && a.cv.rt;
   auto k0 = k_pp_level<0, PP_CAP, PP_THREADS>;
   auto k1 = k_pp_level<1, PP_CAP1, PP_THREADS1>;
   auto k2 = k_pp_level<2, PP_CAP, PP_THREADS>;
   auto k3 = k_pp_level<3, PP_CAP1, PP_THREADS1>;
   const int persist = cube_grid((int64_t)1 << 40, 1, 4), one_per_sm = cube_grid((int64_t)1 << 40, 1, 1);
   cube_phase_begin(c, PH_PP);
+  if (c->pp_act_valid) {
+    PPFilter f;
+    f.g = a.g;
+    f.np = c->np;
+    f.ncells = c->ncells;
+    f.xp = a.xp;
+    f.pcell = c->pcell[c->cur];
+    f.rhoc = a.rhoc;
+    f.cstart = a.cstart;
+    f.occ = c->pp_occ;
+    f.act = c->pp_act;
+    f.wcnt = c->pp_wcnt;
+    f.wstart = c->pp_wstart;
+    f.arhoc = c->pp_arhoc;
+    f.acstart = c->pp_acstart;
+    f.aidx = c->pp_aidx;
+    f.st = c->dstats;
+    const int64_t nw = (c->np + 31) / 32;
+    k_pp_occ<<<cube_grid(c->ncells, 256), 256, 0, c->stream>>>(f);
+    if (c->np > 0) {
+      k_pp_active<<<cube_grid(c->np, 256), 256, 0, c->stream>>>(f);
+      r = cube_scan_counts(c, c->pp_wcnt, c->pp_wstart, nw);
+      if (r) return r;
+      k_pp_aidx<<<cube_grid(c->np, 256), 256, 0, c->stream>>>(f);
+    } else {
+      CUBE_CUDA(c, cudaMemsetAsync(c->pp_wstart, 0, 8, c->stream));
+    }
+    k_pp_acells<<<cube_grid(c->ncells, 256), 256, 0, c->stream>>>(f);
+    a.rhoc = c->pp_arhoc;
+    a.cstart = c->pp_acstart;
+    a.pidx = c->pp_aidx;
+    a.act = c->pp_act;
+    a.nact = c->pp_wstart + nw;
+  }
   // a forced first level lists everything for it (tests of the dense paths)
   const int start = c->opt_pp_level;
   if (start == 1 || start == 2)
@@ -740,7 +998,14 @@ int cube_pp_launch(cube_ctx* c, float a_mid, float dt, bool defer_kick) {
   const int g4 = (int)std::max<int64_t>(1, std::min<int64_t>(one_per_sm, c->pp_scr_cap / (2 * PP_CAP1)));
   if (start <= 4) k_pp_global<4><<<g4, PP_THREADS1, 0, c->stream>>>(a);
   k_pp_global<5><<<1, PP_THREADS1, 0, c->stream>>>(a);
-  if (!defer_kick) k_pp_kick<<<cube_grid(c->np, 256), 256, 0, c->stream>>>(a);
+  if (c->pp_act_valid) {
+    // the active particles' kick now (a deferred fine kick then gives the
+    // others their zero-kick codes); the others' here when not deferred
+    k_pp_kick_active<<<cube_grid(c->np, 256), 256, 0, c->stream>>>(a);
+    if (!defer_kick) k_pp_kick_idle<<<cube_grid(c->np, 256), 256, 0, c->stream>>>(a);
+  } else if (!defer_kick) {
+    k_pp_kick<<<cube_grid(c->np, 256), 256, 0, c->stream>>>(a);
+  }
   CUBE_CUDA(c, cudaGetLastError());
   cube_phase_end(c, PH_PP);
   if (c->graph_mode) {
@@ -776,6 +1041,10 @@ int cube_pp_finish(cube_ctx* c, cube_stats* st) {
                                                    std::to_string(c->pp_scr_cap) + " the PP scratch stages");
   if ((int64_t)c->hstats->itest1 != c->np)
     return cube_fail(c, CUBE_ERR_COUNT_MISMATCH, "PP updated a different number of particles than nplocal");
+  if (c->pp_act_valid && c->np > 0) {
+    c->pp_active_frac = (float)((double)c->hstats->pp_active / (double)c->np);
+    if (c->pp_active_frac < 0.5f) c->pp_unfiltered = 0;
+  }
   if (st) {
     st->f2_max_pp = bits_float(c->hstats->f2_pp_bits);
     st->npairs = (int64_t)c->hstats->npairs;

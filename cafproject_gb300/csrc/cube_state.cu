@@ -359,6 +359,17 @@ __global__ void k_encode_bounds(float sigma, const float* sigp, int nvbin, long 
   bnd[n] = hi;
 }
 
+// rt[v+half] = the code a zero kick gives code v: decode, then encode with the
+// same sigma (the reference's FP64 expressions, update_particle.f90:67,117);
+// a particle whose PP force is zero takes its code from here
+__global__ void k_reencode(CodecView k, const float* sigp, float sigma, int nvbin, int32_t* __restrict__ rt) {
+  if (sigp) sigma = *sigp;
+  k.cf = (float)vcoef(sigma);
+  k.cfp = nullptr;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nvbin) rt[i] = (int32_t)codec_encode(k, codec_decode(k, i - k.half));
+}
+
 static void view_of(const cube_ctx* c, const cube_ctx::Codec& k, CodecView* v) {
   v->dec = k.dec;
   v->dech = k.dech;
@@ -368,6 +379,7 @@ static void view_of(const cube_ctx* c, const cube_ctx::Codec& k, CodecView* v) {
   v->cf = (float)vcoef_host(k.sigma);
   v->amp = (float)((double)(c->nvbin - 1) / (double)CUBE_PI_F);
   v->cfp = nullptr;
+  v->rt = k.rt;
 }
 
 static int build_codec(cube_ctx* c, int slot, float sigma, const float* sigp = nullptr) {
@@ -375,6 +387,11 @@ static int build_codec(cube_ctx* c, int slot, float sigma, const float* sigp = n
   k_decode_table<<<(c->nvbin + 255) / 256, 256, 0, c->stream>>>(c->tan_tab, c->nvbin, sigma, sigp, k.dec, k.dech);
   int nmax = c->nvbin / 2 - 1;
   k_encode_bounds<<<(nmax + 127) / 128, 128, 0, c->stream>>>(sigma, sigp, c->nvbin, k.bnd);
+  if (k.rt) {
+    CodecView v;
+    view_of(c, k, &v);
+    k_reencode<<<(c->nvbin + 255) / 256, 256, 0, c->stream>>>(v, sigp, sigma, c->nvbin, k.rt);
+  }
   CUBE_CUDA(c, cudaGetLastError());
   k.sigma = sigma;
   return CUBE_OK;

@@ -50,6 +50,7 @@ OPT_DEPOSIT_COARSE = 5
 OPT_FAIL_ALLOC = 6
 OPT_PP_HEAVY = 7
 OPT_PP_PARTS = 8
+OPT_PP_FILTER = 9
 NPHASE = 16
 
 

@@ -335,7 +335,14 @@ void* cube_stream(cube_ctx* ctx);
    default, 8192); the two walks give bitwise the same sums, so this too only
    serves tests and timing.  CUBE_OPT_PP_PARTS=8 caps the parts a dense PP
    brick or cell is split into, each part on its own SM (0: the default cap,
-   255; 1: no split); same sums for every value. */
+   255; 1: no split); same sums for every value.  CUBE_OPT_PP_FILTER=9
+   controls PP's prefilter: a particle whose 27 neighbouring fine cells hold
+   no other particle gets a zero pair force (its list is the one entry of
+   itself, as in the reference's loop), found from per-cell occupancy masks,
+   and the staging levels then see only the other particles, whose lists are
+   unchanged.  0 (default): on while the last filtered call found fewer than
+   half the particles with a neighbour, re-tried every 16th call otherwise;
+   1: off; 2: on.  Bitwise the same forces, pair counts and codes. */
 enum cube_option {
   CUBE_OPT_EXACT_KICKS = 1,
   CUBE_OPT_PP_LEVEL = 2,
@@ -344,7 +351,8 @@ enum cube_option {
   CUBE_OPT_DEPOSIT_COARSE = 5,
   CUBE_OPT_FAIL_ALLOC = 6,
   CUBE_OPT_PP_HEAVY = 7,
-  CUBE_OPT_PP_PARTS = 8
+  CUBE_OPT_PP_PARTS = 8,
+  CUBE_OPT_PP_FILTER = 9
 };
 int cube_set_option(cube_ctx* ctx, int option, int64_t value);
 
