@@ -60,6 +60,13 @@ constexpr size_t pp_smem(int cap, int nf) {
 constexpr size_t PP_SMEM = pp_smem(PP_CAP, PNF_MAX);
 constexpr size_t PP_SMEM1 = pp_smem(PP_CAP1, PNF1);
 constexpr size_t PP_SMEM1B = pp_smem(PP_CAP1, PNF_MAX);
+// level 0 when few particles are staged (the prefilter on a sparse state):
+// 384 staged particles in 128-thread blocks, eight blocks per SM instead of
+// four, more bricks in flight to hide the staging's latency
+constexpr int PP_CAP_S = 384;
+constexpr int PP_THREADS_S = 128;
+constexpr size_t PP_SMEM_S = pp_smem(PP_CAP_S, PNF_MAX);
+constexpr float PP_SPARSE_FRAC = 0.25f;  // active share below which level 0 takes the small blocks
 static_assert(PP_CAP1 < 65536 && PP_CAP1 < (1 << 19), "slots are 16-bit, ranks fit 19 bits");
 static_assert(PNF_MAX < (1 << 13) && PNF1 < (1 << 8), "bins fit 13 bits (bricks) and 8 bits (cells)");
 
@@ -608,7 +615,7 @@ __device__ __forceinline__ void pp_list_item(const PPArgs& a, int l, int item, i
 // the cells of the bricks level 1 could not hold; levels 1 and 3: listed
 // bricks / cells in parts.  What does not fit is listed for the next level.
 template <int kLevel, int CAP, int NT>
-__global__ void __launch_bounds__(NT) k_pp_level(PPArgs a) {
+__global__ void __launch_bounds__(NT, NT <= 128 ? 8 : (NT <= 256 ? 4 : 1)) k_pp_level(PPArgs a) {
   __shared__ PPSmem sm;
   __shared__ int s3[3];
   extern __shared__ float4 dyn[];
@@ -777,13 +784,21 @@ __global__ void __launch_bounds__(256) k_pp_occ(PPFilter f) {
   }
 }
 
-// sub-cells whose coordinate d lies in [lo, hi] (0 <= lo <= hi <= 3)
-__device__ __forceinline__ unsigned long long sub_range(int d, int lo, int hi) {
-  if (d == 0) return (unsigned long long)((2u << hi) - (1u << lo)) * 0x1111111111111111ull;
-  if (d == 1) return (unsigned long long)((16u << (4 * hi)) - (1u << (4 * lo))) * 0x0001000100010001ull;
-  const unsigned long long top = hi == 3 ? 0ull : 1ull << (16 * (hi + 1));
-  return top - (1ull << (16 * lo));
+// Sub-cell masks from a 4-bit set of coordinates n (bit k: coordinate k) in
+// dimension d: x is the low bit of each nibble, y a nibble of each 16-bit
+// slab, z a 16-bit slab.
+__device__ __forceinline__ unsigned long long sub_mask(int d, unsigned n) {
+  if (d == 0) return (unsigned long long)n * 0x1111111111111111ull;
+  if (d == 1) {
+    const unsigned y = ((n & 1u) ? 0x000Fu : 0u) | ((n & 2u) ? 0x00F0u : 0u) | ((n & 4u) ? 0x0F00u : 0u) |
+                       ((n & 8u) ? 0xF000u : 0u);
+    return (unsigned long long)y * 0x0001000100010001ull;
+  }
+  return ((n & 1u) ? 0x000000000000FFFFull : 0ull) | ((n & 2u) ? 0x00000000FFFF0000ull : 0ull) |
+         ((n & 4u) ? 0x0000FFFF00000000ull : 0ull) | ((n & 8u) ? 0xFFFF000000000000ull : 0ull);
 }
+// coordinates within one of s in the same cell (s=0: 0-1, 1: 0-2, 2: 1-3, 3: 2-3)
+__device__ __forceinline__ unsigned own_range(int s) { return (0xCE73u >> (4 * s)) & 0xFu; }
 
 // the part of cell_id that coordinate d contributes (cell_id is their sum:
 // ix + nt*iy + nt^2*iz + nt^3*(tx + nnt*ty + nnt^2*tz))
@@ -797,7 +812,7 @@ __device__ __forceinline__ uint32_t cell_part(const Geo& g, int d, int gc) {
 
 // the particle's own cell and, per dimension where its sub-cell touches a
 // face, the neighbouring cell: up to 8 cells, their words loaded together
-__global__ void __launch_bounds__(256) k_pp_active(PPFilter f) {
+__global__ void __launch_bounds__(256, 5) k_pp_active(PPFilter f) {
   const Geo& g = f.g;
   const int lane = threadIdx.x & 31, nc = g.nc;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -817,24 +832,24 @@ __global__ void __launch_bounds__(256) k_pp_active(PPFilter f) {
 #pragma unroll
       for (int d = 0; d < 3; d++) {
         part[d][0] = cell_part(g, d, gc[d]);
-        rng[d][0] = sub_range(d, max(s[d] - 1, 0), min(s[d] + 1, 3));
+        rng[d][0] = sub_mask(d, own_range(s[d]));
+        // a sub-cell on a face also sees the neighbouring cell's facing layer
         const int o = s[d] == 0 ? -1 : (s[d] == 3 ? 1 : 0);
         nopt[d] = o ? 2 : 1;
         part[d][1] = o ? cell_part(g, d, wrap1(gc[d] + o, nc)) : part[d][0];
-        rng[d][1] = sub_range(d, o < 0 ? 3 : 0, o < 0 ? 3 : 0);
+        rng[d][1] = sub_mask(d, o < 0 ? 8u : 1u);
       }
-      unsigned long long w[8];
+      unsigned long long any = (__ldg(f.occ + f.ncells + cell) >> sb) & 1ull;  // another in its own fine cell
 #pragma unroll
       for (int k = 0; k < 8; k++) {
         const int ix = k & 1, iy = (k >> 1) & 1, iz = k >> 2;
-        w[k] = (ix < nopt[0] && iy < nopt[1] && iz < nopt[2])
-                   ? __ldg(f.occ + (part[0][ix] + part[1][iy] + part[2][iz])) & rng[0][ix] & rng[1][iy] & rng[2][iz]
-                   : 0ull;
+        if (ix < nopt[0] && iy < nopt[1] && iz < nopt[2]) {
+          unsigned long long w =
+              __ldg(f.occ + (part[0][ix] + part[1][iy] + part[2][iz])) & rng[0][ix] & rng[1][iy] & rng[2][iz];
+          if (k == 0) w &= ~(1ull << sb);  // itself in its own cell
+          any |= w;
+        }
       }
-      w[0] &= ~(1ull << sb);  // itself in its own cell
-      unsigned long long any = (__ldg(f.occ + f.ncells + cell) >> sb) & 1ull;  // another in its own fine cell
-#pragma unroll
-      for (int k = 0; k < 8; k++) any |= w[k];
       act = any != 0ull;
     }
     const unsigned b = __ballot_sync(0xffffffffu, v && act);
@@ -990,7 +1005,12 @@ int cube_pp_launch(cube_ctx* c, float a_mid, float dt, bool defer_kick) {
     k_pp_list_all<<<cube_grid(c->ncells, 256), 256, 0, c->stream>>>(c->pp_list[start - 1], c->pp_lpart[start - 1],
                                                                      (int)c->ncells, c->pp_nlist + start - 1,
                                                                      start == 5 ? 1 : 3);
-  if (start <= 0) k0<<<(unsigned)nbrick, PP_THREADS, PP_SMEM, c->stream>>>(a);
+  if (start <= 0) {
+    if (c->pp_act_valid && c->pp_active_frac < PP_SPARSE_FRAC)
+      k_pp_level<0, PP_CAP_S, PP_THREADS_S><<<(unsigned)nbrick, PP_THREADS_S, PP_SMEM_S, c->stream>>>(a);
+    else
+      k0<<<(unsigned)nbrick, PP_THREADS, PP_SMEM, c->stream>>>(a);
+  }
   if (start <= 1) k1<<<one_per_sm, PP_THREADS1, PP_SMEM1B, c->stream>>>(a);
   if (start <= 2) k2<<<persist, PP_THREADS, PP_SMEM, c->stream>>>(a);
   if (start <= 3) k3<<<one_per_sm, PP_THREADS1, PP_SMEM1, c->stream>>>(a);
