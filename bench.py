@@ -405,13 +405,16 @@ def run_gb300(args, ws, rank, lrank):
     barrier(ws)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    tstep = []
     for _ in range(ke):
-        e2e_step()
+        ts0 = time.perf_counter()
+        e2e_step()  # ends when the step's download has landed in host memory
+        tstep.append(1e3 * (time.perf_counter() - ts0))
     torch.cuda.synchronize()
     te = time.perf_counter() - t0
     te = allreduce_max(te, ws, dev)
     e2e = {"value": ntot * ke / te, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(h2d),
-           "steps": ke}
+           "steps": ke, "step_ms": [round(t, 2) for t in tstep]}
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
