@@ -407,9 +407,9 @@ def run_gb300(args, ws, rank, lrank):
     t0 = time.perf_counter()
     tstep = []
     for _ in range(ke):
-        ts0 = time.perf_counter()
+        t_s = time.perf_counter()
         e2e_step()  # ends when the step's download has landed in host memory
-        tstep.append(1e3 * (time.perf_counter() - ts0))
+        tstep.append(1e3 * (time.perf_counter() - t_s))
     torch.cuda.synchronize()
     te = time.perf_counter() - t0
     te = allreduce_max(te, ws, dev)
