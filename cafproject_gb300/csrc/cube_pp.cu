@@ -902,9 +902,11 @@ __global__ void __launch_bounds__(256) k_pp_aidx(PPFilter f) {
 
 // whether this PP launch runs the prefilter: automatic while under half of
 // the particles had a neighbour at the last filtered call (a uniform early
-// state has about one in ten), re-tried every 16th call otherwise
+// state has about one in ten), re-tried every 16th call otherwise; always
+// inside a captured graph, where no count comes back to the host
 static bool pp_filter_on(cube_ctx* c) {
-  if (!c->pp_occ || c->graph_mode || c->p.nc < 4 || c->opt_pp_filter == 1) return false;
+  if (!c->pp_occ || c->p.nc < 4 || c->opt_pp_filter == 1) return false;
+  if (c->graph_mode) return true;
   if (c->opt_pp_filter == 2 || c->pp_active_frac < 0.5f) return true;
   return ++c->pp_unfiltered % 16 == 0;
 }
@@ -1006,7 +1008,7 @@ int cube_pp_launch(cube_ctx* c, float a_mid, float dt, bool defer_kick) {
                                                                      (int)c->ncells, c->pp_nlist + start - 1,
                                                                      start == 5 ? 1 : 3);
   if (start <= 0) {
-    if (c->pp_act_valid && c->pp_active_frac < PP_SPARSE_FRAC)
+    if (c->pp_act_valid && !c->graph_mode && c->pp_active_frac < PP_SPARSE_FRAC)
       k_pp_level<0, PP_CAP_S, PP_THREADS_S><<<(unsigned)nbrick, PP_THREADS_S, PP_SMEM_S, c->stream>>>(a);
     else
       k0<<<(unsigned)nbrick, PP_THREADS, PP_SMEM, c->stream>>>(a);
