@@ -167,13 +167,17 @@ class ClockSampler:
 # particle counts scale together between 256^3 and 512^3, so per-particle
 # traffic carries over
 TRAFFIC_PER_PARTICLE = {
-    "pp_force": (178.5e6 + 55.0e6) / 16778347,
-    "fine_kick": (2034.4e6 + 100.0e6) / 16778347,
-    "coarse_kick": (289.6e6 + 81.0e6) / 16778347,
-    "fine_deposit": (84.1e6 + 480.1e6) / 16778347,
-    "update_dest": (244.1e6 + 78.6e6) / 16778347,
-    "update_scatter": (502.9e6 + 255.8e6) / 16778347,
-    "fine_green": (1347.6e6 + 1568.0e6) / 16778347,
+    # one ncu capture per kernel at 256^3 (profiles/step_kernels_cdm256.md),
+    # DRAM read + write per launch over the particles; pp_force: the brick
+    # kernel and the activity test (the prefilter's smaller passes uncaptured)
+    "pp_force": (93.0e6 + 33.6e6 + 153.1e6 + 5.8e6) / 16778347,
+    "fine_kick": (2192.5e6 + 115.1e6) / 16778347,
+    "coarse_kick": (324.8e6 + 90.4e6) / 16778347,
+    "fine_deposit": (83.7e6 + 476.4e6) / 16778347,
+    "update_dest": (243.8e6 + 77.9e6) / 16778347,
+    "update_scatter": (506.5e6 + 257.2e6) / 16778347,
+    "fine_green": (1347.5e6 + 1567.8e6) / 16778347,
+    "fine_f2max": (1617.1e6 + 1560.4e6) / 16778347,
 }
 
 
