@@ -784,22 +784,6 @@ __global__ void __launch_bounds__(256) k_pp_occ(PPFilter f) {
   }
 }
 
-// Sub-cell masks from a 4-bit set of coordinates n (bit k: coordinate k) in
-// dimension d: x is the low bit of each nibble, y a nibble of each 16-bit
-// slab, z a 16-bit slab.
-__device__ __forceinline__ unsigned long long sub_mask(int d, unsigned n) {
-  if (d == 0) return (unsigned long long)n * 0x1111111111111111ull;
-  if (d == 1) {
-    const unsigned y = ((n & 1u) ? 0x000Fu : 0u) | ((n & 2u) ? 0x00F0u : 0u) | ((n & 4u) ? 0x0F00u : 0u) |
-                       ((n & 8u) ? 0xF000u : 0u);
-    return (unsigned long long)y * 0x0001000100010001ull;
-  }
-  return ((n & 1u) ? 0x000000000000FFFFull : 0ull) | ((n & 2u) ? 0x00000000FFFF0000ull : 0ull) |
-         ((n & 4u) ? 0x0000FFFF00000000ull : 0ull) | ((n & 8u) ? 0xFFFF000000000000ull : 0ull);
-}
-// coordinates within one of s in the same cell (s=0: 0-1, 1: 0-2, 2: 1-3, 3: 2-3)
-__device__ __forceinline__ unsigned own_range(int s) { return (0xCE73u >> (4 * s)) & 0xFu; }
-
 // the part of cell_id that coordinate d contributes (cell_id is their sum:
 // ix + nt*iy + nt^2*iz + nt^3*(tx + nnt*ty + nnt^2*tz))
 __device__ __forceinline__ uint32_t cell_part(const Geo& g, int d, int gc) {
@@ -810,47 +794,74 @@ __device__ __forceinline__ uint32_t cell_part(const Geo& g, int d, int gc) {
   return nt * nt * i + nt3 * nnt * nnt * t;
 }
 
-// the particle's own cell and, per dimension where its sub-cell touches a
-// face, the neighbouring cell: up to 8 cells, their words loaded together
-__global__ void __launch_bounds__(256, 5) k_pp_active(PPFilter f) {
+// Sub-cell bit operations (bit x + 4y + 16z): the layer x = 0 (y = 0, z = 0)
+// of a cell, and moves of every bit by one sub-cell along a dimension
+// (bits leaving the cell drop).
+__host__ __device__ constexpr unsigned long long lay0(int d) {
+  return d == 0 ? 0x1111111111111111ull : (d == 1 ? 0x000F000F000F000Full : 0x000000000000FFFFull);
+}
+__host__ __device__ constexpr int sub_stride(int d) { return d == 0 ? 1 : (d == 1 ? 4 : 16); }
+__device__ __forceinline__ unsigned long long sub_up(unsigned long long m, int d) {   // to coordinate + 1
+  return (m << sub_stride(d)) & ~lay0(d);
+}
+__device__ __forceinline__ unsigned long long sub_down(unsigned long long m, int d) {  // to coordinate - 1
+  return (m >> sub_stride(d)) & ~(lay0(d) << (3 * sub_stride(d)));
+}
+__device__ __forceinline__ unsigned long long sub_ex(unsigned long long m, int d) { return sub_up(m, d) | sub_down(m, d); }
+__device__ __forceinline__ unsigned long long sub_dil(unsigned long long m, int d) { return m | sub_ex(m, d); }
+
+// Per coarse cell, the sub-cells whose 26 neighbouring fine cells (its own
+// and the 26 surrounding coarse cells') hold a particle, or that hold two
+// themselves: a particle there has a neighbour besides itself.  Within the
+// cell, a neighbour differs by one in z (any x, y), or in y only (any x), or
+// in x only; a surrounding cell contributes its facing layer(s), moved to
+// the adjoining layer(s) of this cell and spread by one in the other
+// dimensions.  Written over the cell's multiple mask, which no other cell
+// reads.
+__global__ void __launch_bounds__(256) k_pp_nbmask(PPFilter f) {
   const Geo& g = f.g;
-  const int lane = threadIdx.x & 31, nc = g.nc;
+  const int nc = g.nc;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < f.ncells; c += (int64_t)gridDim.x * blockDim.x) {
+    int gc[3];
+    cell_coords(g, c, gc[0], gc[1], gc[2]);
+    uint32_t part[3][3];  // coordinate - 1, itself, + 1
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+      for (int o = -1; o <= 1; o++) part[d][o + 1] = cell_part(g, d, wrap1(gc[d] + o, nc));
+    const unsigned long long own = __ldg(f.occ + c);
+    const unsigned long long dxo = sub_dil(own, 0);
+    unsigned long long e = sub_ex(sub_dil(dxo, 1), 2) | sub_ex(dxo, 1) | sub_ex(own, 0);
+#pragma unroll
+    for (int k = 0; k < 27; k++) {
+      const int o[3] = {k % 3 - 1, (k / 3) % 3 - 1, k / 9 - 1};
+      if (o[0] == 0 && o[1] == 0 && o[2] == 0) continue;
+      unsigned long long l = __ldg(f.occ + (part[0][o[0] + 1] + part[1][o[1] + 1] + part[2][o[2] + 1]));
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        if (o[d] < 0) l = (l >> (3 * sub_stride(d))) & lay0(d);                              // its layer 3 to our layer 0
+        else if (o[d] > 0) l = (l << (3 * sub_stride(d))) & (lay0(d) << (3 * sub_stride(d)));  // its layer 0 to our layer 3
+      }
+#pragma unroll
+      for (int d = 0; d < 3; d++)
+        if (o[d] == 0) l = sub_dil(l, d);
+      e |= l;
+    }
+    f.occ[f.ncells + c] = e | f.occ[f.ncells + c];
+  }
+}
+
+// a particle's activity: one bit of its cell's neighbour mask
+__global__ void __launch_bounds__(256) k_pp_active(PPFilter f) {
+  const int lane = threadIdx.x & 31;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   unsigned long long nact = 0, nidle = 0;
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p - lane < f.np; p += stride) {
     const bool v = p < f.np;
     bool act = false;
     if (v) {
-      const int cell = __ldg(f.pcell + p);
-      int s[3], gc[3];
-      sub_cell(f.xp, p, g.izipx, s);
-      cell_coords(g, cell, gc[0], gc[1], gc[2]);
-      const int sb = s[0] + 4 * (s[1] + 4 * s[2]);
-      uint32_t part[3][2];
-      unsigned long long rng[3][2];
-      int nopt[3];
-#pragma unroll
-      for (int d = 0; d < 3; d++) {
-        part[d][0] = cell_part(g, d, gc[d]);
-        rng[d][0] = sub_mask(d, own_range(s[d]));
-        // a sub-cell on a face also sees the neighbouring cell's facing layer
-        const int o = s[d] == 0 ? -1 : (s[d] == 3 ? 1 : 0);
-        nopt[d] = o ? 2 : 1;
-        part[d][1] = o ? cell_part(g, d, wrap1(gc[d] + o, nc)) : part[d][0];
-        rng[d][1] = sub_mask(d, o < 0 ? 8u : 1u);
-      }
-      unsigned long long any = (__ldg(f.occ + f.ncells + cell) >> sb) & 1ull;  // another in its own fine cell
-#pragma unroll
-      for (int k = 0; k < 8; k++) {
-        const int ix = k & 1, iy = (k >> 1) & 1, iz = k >> 2;
-        if (ix < nopt[0] && iy < nopt[1] && iz < nopt[2]) {
-          unsigned long long w =
-              __ldg(f.occ + (part[0][ix] + part[1][iy] + part[2][iz])) & rng[0][ix] & rng[1][iy] & rng[2][iz];
-          if (k == 0) w &= ~(1ull << sb);  // itself in its own cell
-          any |= w;
-        }
-      }
-      act = any != 0ull;
+      int s[3];
+      sub_cell(f.xp, p, f.g.izipx, s);
+      act = (__ldg(f.occ + f.ncells + __ldg(f.pcell + p)) >> (s[0] + 4 * (s[1] + 4 * s[2]))) & 1ull;
     }
     const unsigned b = __ballot_sync(0xffffffffu, v && act);
     if (lane == 0) {
@@ -982,6 +993,7 @@ int cube_pp_launch(cube_ctx* c, float a_mid, float dt, bool defer_kick) {
     f.st = c->dstats;
     const int64_t nw = (c->np + 31) / 32;
     k_pp_occ<<<cube_grid(c->ncells, 256), 256, 0, c->stream>>>(f);
+    k_pp_nbmask<<<cube_grid(c->ncells, 256), 256, 0, c->stream>>>(f);
     if (c->np > 0) {
       k_pp_active<<<cube_grid(c->np, 256), 256, 0, c->stream>>>(f);
       r = cube_scan_counts(c, c->pp_wcnt, c->pp_wstart, nw);
