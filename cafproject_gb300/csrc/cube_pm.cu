@@ -340,8 +340,11 @@ __device__ __forceinline__ unsigned long long kick_qkey(int64_t p, int d, int co
   return ((unsigned long long)p << 18) | ((unsigned long long)(code & 0xffff) << 2) | (unsigned long long)d;
 }
 
+// a corner's mesh index is xo[i] + yo[j] + zo[k] (i, j, k = 0 for the lower
+// corner, 1 for the upper; x and y parts in 32 bits)
 struct KickCorners {
-  int64_t c[8];  // c111, c211, c121, c112, c122, c212, c221, c222
+  int xo[2], yo[2];
+  int64_t zo[2];
   float d1[3], d2[3];
   int64_t cell;
 };
@@ -373,14 +376,13 @@ __device__ __forceinline__ void kick_corners(const KickArgs& a, int64_t p, KickC
     i1[d] = wrap1(base, n);
     i2[d] = wrap1(base + 1, n);
   }
-  k.c[0] = mesh_idx(n, i1[0], i1[1], i1[2]);
-  k.c[1] = mesh_idx(n, i2[0], i1[1], i1[2]);
-  k.c[2] = mesh_idx(n, i1[0], i2[1], i1[2]);
-  k.c[3] = mesh_idx(n, i1[0], i1[1], i2[2]);
-  k.c[4] = mesh_idx(n, i1[0], i2[1], i2[2]);
-  k.c[5] = mesh_idx(n, i2[0], i1[1], i2[2]);
-  k.c[6] = mesh_idx(n, i2[0], i2[1], i1[2]);
-  k.c[7] = mesh_idx(n, i2[0], i2[1], i2[2]);
+  // mesh_idx(n, x, y, z) = x + (n+2)*(y + n*z)
+  k.xo[0] = i1[0];
+  k.xo[1] = i2[0];
+  k.yo[0] = (n + 2) * i1[1];
+  k.yo[1] = (n + 2) * i2[1];
+  k.zo[0] = (int64_t)(n + 2) * n * i1[2];
+  k.zo[1] = (int64_t)(n + 2) * n * i2[2];
 }
 
 // the eight real(4) CIC terms of component d, in the reference's order
@@ -390,14 +392,17 @@ __device__ __forceinline__ void kick_terms(const KickArgs& a, const KickCorners&
   const float* d1 = k.d1;
   const float* d2 = k.d2;
 #define KT(c, wa, wb, wc) (kPre ? kick_w(__ldg(F + (c)), wa, wb, wc) : kick_term(__ldg(F + (c)), kick_amid(a), kick_dt(a), wa, wb, wc))
-  t[0] = KT(k.c[0], d1[0], d1[1], d1[2]);
-  t[1] = KT(k.c[1], d2[0], d1[1], d1[2]);
-  t[2] = KT(k.c[2], d1[0], d2[1], d1[2]);
-  t[3] = KT(k.c[3], d1[0], d1[1], d2[2]);
-  t[4] = KT(k.c[4], d1[0], d2[1], d2[2]);
-  t[5] = KT(k.c[5], d2[0], d1[1], d2[2]);
-  t[6] = KT(k.c[6], d2[0], d2[1], d1[2]);
-  t[7] = KT(k.c[7], d2[0], d2[1], d2[2]);
+  // corners c111, c211, c121, c112, c122, c212, c221, c222
+  const float* F0 = F + k.zo[0];
+  const float* F1 = F + k.zo[1];
+  t[0] = KT(k.xo[0] + k.yo[0] + (F0 - F), d1[0], d1[1], d1[2]);
+  t[1] = KT(k.xo[1] + k.yo[0] + (F0 - F), d2[0], d1[1], d1[2]);
+  t[2] = KT(k.xo[0] + k.yo[1] + (F0 - F), d1[0], d2[1], d1[2]);
+  t[3] = KT(k.xo[0] + k.yo[0] + (F1 - F), d1[0], d1[1], d2[2]);
+  t[4] = KT(k.xo[0] + k.yo[1] + (F1 - F), d1[0], d2[1], d2[2]);
+  t[5] = KT(k.xo[1] + k.yo[0] + (F1 - F), d2[0], d1[1], d2[2]);
+  t[6] = KT(k.xo[1] + k.yo[1] + (F0 - F), d2[0], d2[1], d1[2]);
+  t[7] = KT(k.xo[1] + k.yo[1] + (F1 - F), d2[0], d2[1], d2[2]);
 #undef KT
 }
 
