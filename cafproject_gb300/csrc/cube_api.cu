@@ -235,7 +235,12 @@ static int create_impl(const cube_params* p, const float* fine_table, const floa
     ALLOC(c->pp_aidx, 4 * (size_t)np);
     ALLOC(c->dstats_pp, sizeof(DevStats));
     CUBE_CUDA(c, cudaMallocHost((void**)&c->hstats_pp, sizeof(DevStats)));
-    CUBE_CUDA(c, cudaStreamCreateWithFlags(&c->stream_pp, cudaStreamNonBlocking));
+    // PP beside the PM force chain at the higher priority: its blocks take
+    // free SM slots first while the transforms stream (74.4 against 75.2 ms
+    // a 512^3 step; the other way round, 77.2)
+    int prio_lo = 0, prio_hi = 0;
+    CUBE_CUDA(c, cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
+    CUBE_CUDA(c, cudaStreamCreateWithPriority(&c->stream_pp, cudaStreamNonBlocking, prio_hi));
     CUBE_CUDA(c, cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
     CUBE_CUDA(c, cudaEventCreateWithFlags(&c->ev_pp, cudaEventDisableTiming));
     int r = cube_pp_init(c);
