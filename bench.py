@@ -169,10 +169,11 @@ class ClockSampler:
 TRAFFIC_PER_PARTICLE = {
     # one ncu capture per kernel at 256^3 (profiles/step_kernels_cdm256.md),
     # DRAM read + write per launch over the particles; pp_force: the brick
-    # kernel and the activity test (the prefilter's smaller passes uncaptured)
-    "pp_force": (93.0e6 + 33.6e6 + 153.1e6 + 5.8e6) / 16778347,
-    "fine_kick": (2192.5e6 + 115.1e6) / 16778347,
-    "coarse_kick": (324.8e6 + 90.4e6) / 16778347,
+    # kernel and the activity test's two passes (the prefilter's smaller
+    # passes uncaptured)
+    "pp_force": (93.1e6 + 34.2e6 + 134.2e6 + 4.9e6 + 33.6e6) / 16778347,
+    "fine_kick": (2194.1e6 + 114.8e6) / 16778347,
+    "coarse_kick": (325.2e6 + 89.9e6) / 16778347,
     "fine_deposit": (83.7e6 + 476.4e6) / 16778347,
     "update_dest": (243.8e6 + 77.9e6) / 16778347,
     "update_scatter": (506.5e6 + 257.2e6) / 16778347,
