@@ -634,11 +634,14 @@ def workload_config(p, n, z_init):
 
 def gpu_launches(p, steps):
     """Launches of this library's kernels per step (cuFFT kernels not counted)."""
-    upd = 1 + 2 + 3 + 3 + 1 + 1  # dest, counting ranks (2), scan (3), place + two vfield passes, scatter, sigma
-    pp = 6 if p.pp_on else 0     # five pair levels (bricks, large bricks, cells, large cells, global), kick
-    fine = 4                     # deposit, green, maxima + kick factors, kick
+    upd = 1 + 3 + 3 + 3 + 1 + 1  # dest, counting ranks (3: local, dense cells, base), scan (3),
+    #                               place + two vfield passes, scatter, sigma
+    # PP: the prefilter (occupancy, neighbour masks, activity, a scan of 3,
+    # compaction, cell starts), six staging levels, the active particles' kick
+    pp = 8 + 6 + 1 if p.pp_on else 0
+    fine = 4                     # deposit, green, maxima + kick factors, kick (PP's zero kicks inside)
     coarse = 4
-    codec = 2                    # decode table and encode boundaries for the new sigma
+    codec = 3                    # decode table, encode boundaries and zero-kick table for the new sigma
     return steps * (upd + pp + fine + coarse + codec)
 
 
