@@ -821,6 +821,7 @@ __device__ __forceinline__ unsigned long long sub_dil(unsigned long long m, int 
 __global__ void __launch_bounds__(256) k_pp_nbmask(PPFilter f) {
   const Geo& g = f.g;
   const int nc = g.nc;
+  unsigned long long nact = 0, nidle = 0;
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < f.ncells; c += (int64_t)gridDim.x * blockDim.x) {
     int gc[3];
     cell_coords(g, c, gc[0], gc[1], gc[2]);
@@ -846,36 +847,29 @@ __global__ void __launch_bounds__(256) k_pp_nbmask(PPFilter f) {
         if (o[d] == 0) l = sub_dil(l, d);
       e |= l;
     }
-    f.occ[f.ncells + c] = e | f.occ[f.ncells + c];
-  }
-}
-
-// a particle's activity: one bit of its cell's neighbour mask
-__global__ void __launch_bounds__(256) k_pp_active(PPFilter f) {
-  const int lane = threadIdx.x & 31;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  unsigned long long nact = 0, nidle = 0;
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p - lane < f.np; p += stride) {
-    const bool v = p < f.np;
-    bool act = false;
-    if (v) {
+    // then the cell's own particles: active where their sub-cell's bit is
+    // set (act and wcnt zeroed before the launch)
+    const unsigned long long a = e | __ldg(f.occ + f.ncells + c);
+    const int n = __ldg(f.rhoc + c);
+    const int64_t p0 = __ldg(f.cstart + c);
+    for (int j = 0; j < n; j++) {
+      const int64_t p = p0 + j;
       int s[3];
-      sub_cell(f.xp, p, f.g.izipx, s);
-      act = (__ldg(f.occ + f.ncells + __ldg(f.pcell + p)) >> (s[0] + 4 * (s[1] + 4 * s[2]))) & 1ull;
+      sub_cell(f.xp, p, g.izipx, s);
+      if ((a >> (s[0] + 4 * (s[1] + 4 * s[2]))) & 1ull) {
+        atomicOr(&f.act[p >> 5], 1u << (p & 31));
+        atomicAdd(&f.wcnt[p >> 5], 1);
+        nact++;
+      } else {
+        nidle++;
+      }
     }
-    const unsigned b = __ballot_sync(0xffffffffu, v && act);
-    if (lane == 0) {
-      f.act[p >> 5] = b;
-      f.wcnt[p >> 5] = __popc(b);
-    }
-    nact += (v && act) ? 1 : 0;
-    nidle += (v && !act) ? 1 : 0;
   }
   for (int o = 16; o > 0; o >>= 1) {
     nact += __shfl_xor_sync(0xffffffffu, nact, o);
     nidle += __shfl_xor_sync(0xffffffffu, nidle, o);
   }
-  if (lane == 0) {
+  if ((threadIdx.x & 31) == 0) {
     // a particle left out has the one entry of itself and a zero force (itest1 counts it)
     if (nidle) {
       atomicAdd(&f.st->npairs, nidle);
@@ -993,9 +987,10 @@ int cube_pp_launch(cube_ctx* c, float a_mid, float dt, bool defer_kick) {
     f.st = c->dstats;
     const int64_t nw = (c->np + 31) / 32;
     k_pp_occ<<<cube_grid(c->ncells, 256), 256, 0, c->stream>>>(f);
+    CUBE_CUDA(c, cudaMemsetAsync(c->pp_act, 0, 4 * (size_t)nw, c->stream));
+    CUBE_CUDA(c, cudaMemsetAsync(c->pp_wcnt, 0, 4 * (size_t)nw, c->stream));
     k_pp_nbmask<<<cube_grid(c->ncells, 256), 256, 0, c->stream>>>(f);
     if (c->np > 0) {
-      k_pp_active<<<cube_grid(c->np, 256), 256, 0, c->stream>>>(f);
       r = cube_scan_counts(c, c->pp_wcnt, c->pp_wstart, nw);
       if (r) return r;
       k_pp_aidx<<<cube_grid(c->np, 256), 256, 0, c->stream>>>(f);
