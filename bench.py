@@ -636,9 +636,10 @@ def gpu_launches(p, steps):
     """Launches of this library's kernels per step (cuFFT kernels not counted)."""
     upd = 1 + 3 + 3 + 3 + 1 + 1  # dest, counting ranks (3: local, dense cells, base), scan (3),
     #                               place + two vfield passes, scatter, sigma
-    # PP: the prefilter (occupancy, neighbour masks, activity, a scan of 3,
-    # compaction, cell starts), six staging levels, the active particles' kick
-    pp = 8 + 6 + 1 if p.pp_on else 0
+    # PP: the prefilter (occupancy, neighbour masks with the activity bits, a
+    # scan of 3, compaction, cell starts), six staging levels, the active
+    # particles' kick
+    pp = 7 + 6 + 1 if p.pp_on else 0
     fine = 4                     # deposit, green, maxima + kick factors, kick (PP's zero kicks inside)
     coarse = 4
     codec = 3                    # decode table, encode boundaries and zero-kick table for the new sigma

@@ -53,7 +53,7 @@ def test_library_arm_line(monkeypatch):
     assert {"value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step"} <= set(d["e2e"])
     assert {"bound", "achieved", "peak", "unit", "frac", "traffic"} <= set(d["roofline"])
     assert {"value", "unit", "cores", "kind", "sample"} <= set(d["cpu_baseline"])
-    assert d["gpu_launches"] == 38 * 5  # this library's launches per step, as the launch list shows
+    assert d["gpu_launches"] == 37 * 5  # this library's launches per step, as the launch list shows
     assert "workload" in d["config"] and "model" not in d["config"]
     assert set(d["redshifts"]) == {"49", "5", "1"}
     for k in ("adjoint", "batched", "two_species"):
