@@ -341,8 +341,9 @@ void* cube_stream(cube_ctx* ctx);
    itself, as in the reference's loop), found from per-cell occupancy masks,
    and the staging levels then see only the other particles, whose lists are
    unchanged.  0 (default): on while the last filtered call found fewer than
-   half the particles with a neighbour, re-tried every 16th call otherwise;
-   1: off; 2: on.  Bitwise the same forces, pair counts and codes. */
+   half the particles with a neighbour, re-tried every 16th call otherwise,
+   and always inside the batched ensemble's captured graphs; 1: off; 2: on.
+   Bitwise the same forces, pair counts and codes. */
 enum cube_option {
   CUBE_OPT_EXACT_KICKS = 1,
   CUBE_OPT_PP_LEVEL = 2,
