@@ -169,9 +169,9 @@ class ClockSampler:
 TRAFFIC_PER_PARTICLE = {
     # one ncu capture per kernel at 256^3 (profiles/step_kernels_cdm256.md),
     # DRAM read + write per launch over the particles; pp_force: the brick
-    # kernel and the activity test's two passes (the prefilter's smaller
-    # passes uncaptured)
-    "pp_force": (93.1e6 + 34.2e6 + 134.2e6 + 4.9e6 + 33.6e6) / 16778347,
+    # kernel and the neighbour-mask pass that marks the active particles
+    # (the prefilter's smaller passes uncaptured)
+    "pp_force": (93.1e6 + 34.2e6 + 113.5e6 + 4.5e6) / 16778347,
     "fine_kick": (2194.1e6 + 114.8e6) / 16778347,
     "coarse_kick": (325.2e6 + 89.9e6) / 16778347,
     "fine_deposit": (83.7e6 + 476.4e6) / 16778347,
