@@ -135,6 +135,8 @@ static int create_impl(const cube_params* p, const float* fine_table, const floa
   // LRCKCORR rescales the coarse modes with |k|<=8 by 1/Im FFT(raw kernel)
   // (kernel_c.f90:111-113); below nc = 16 that sphere wraps past Nyquist
   if (p->nc < 16) return bad("nc must be at least 16 (coarse kernel correction needs |k|<=8 up to Nyquist)");
+  // the deposits keep a cell's coordinates in 16-bit fields; far beyond any mesh HBM holds
+  if (p->nc > 16384) return bad("nc must be at most 16384");
   if (p->ncell != 4) return bad("ncell must be 4");
   if (p->izipx < 1 || p->izipx > 2 || p->izipv < 1 || p->izipv > 2) return bad("izipx/izipv must be 1 or 2");
   c->nt = p->nc / p->nnt;

@@ -111,6 +111,15 @@ __global__ void __launch_bounds__(256) k_deposit_det(DepArgs a) {
   unsigned* carry = acc + MX * MY * MZ;
   __shared__ int pref[NSRC];
   __shared__ long long sstart[NSRC];
+  // kAxis: the fine deposit tests the stencil per axis (a 2-bit mask each,
+  // the whole stencil skipped when one is empty) and shares the x*y weight
+  // products between z's two corners; the coarse deposit, whose stencils more
+  // often straddle the brick's edge, measured faster with the plain per-corner
+  // test (0.21 ms of 2.70 at 512^3), the fine one slower (0.37 ms of 5.54)
+  constexpr bool kAxis = MPC > 1;
+  // per source cell, 16 bits a dimension: the 1-based tile-local coordinate
+  // (kPk: the global coarse coordinate) that the particle's frame needs
+  __shared__ unsigned long long sframe[NSRC];
   __shared__ unsigned long long btot;
   const Geo& g = a.g;
   const int nc = g.nc, n = kPk ? a.ng : (MPC == 1 ? g.nc : g.nf);
@@ -120,56 +129,79 @@ __global__ void __launch_bounds__(256) k_deposit_det(DepArgs a) {
   int B[3] = {min(BX, nc - C0[0]), min(BY, nc - C0[1]), min(BZ, nc - C0[2])};
   for (int i = threadIdx.x; i < 2 * MX * MY * MZ; i += blockDim.x) acc[i] = 0u;
   if (threadIdx.x == 0) btot = 0ull;
-  // source cells and their particle counts
+  // source cells, their particle counts and frames
   for (int t = threadIdx.x; t < NSRC; t += blockDim.x) {
-    int sx = t % SX - LO, sy = (t / SX) % SY - LO, sz = t / (SX * SY) - LO;
+    const int sl[3] = {t % SX - LO, (t / SX) % SY - LO, t / (SX * SY) - LO};
     int cnt = 0;
     long long st = 0;
-    if (sx < B[0] + HI && sy < B[1] + HI && sz < B[2] + HI) {
-      int64_t c = cell_id(g, wrap1(C0[0] + sx, nc), wrap1(C0[1] + sy, nc), wrap1(C0[2] + sz, nc));
+    unsigned long long fr = 0;
+    if (sl[0] < B[0] + HI && sl[1] < B[1] + HI && sl[2] < B[2] + HI) {
+      int gc[3];
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        gc[d] = wrap1(C0[d] + sl[d], nc);
+        int Tq, L;
+        tile_local(g, gc[d], Tq, L);
+        fr |= (unsigned long long)(unsigned)(kPk ? gc[d] : L) << (16 * d);
+      }
+      int64_t c = cell_id(g, gc[0], gc[1], gc[2]);
       cnt = a.rhoc[c];
       st = a.cstart[c];
     }
     pref[t] = cnt;
     sstart[t] = st;
+    sframe[t] = fr;
   }
   __syncthreads();
   const int total = block_exclusive_scan(pref, NSRC);
   const int lim[3] = {MPC * B[0], MPC * B[1], MPC * B[2]};
   for_box_particles<SX>(pref, sstart, SX, SY * SZ, total, [&](int64_t p, int sxi, int row) {
     const int sl[3] = {sxi - LO, row % SY - LO, row / SY - LO};
+    const unsigned long long fr = sframe[sxi + SX * row];
     int rel[3];
+    unsigned ok[3];  // bit o: mesh index rel + o lies in the brick
     float d1[3], d2[3];
 #pragma unroll
     for (int d = 0; d < 3; d++) {
-      int gcd = wrap1(C0[d] + sl[d], nc), Tq, L;
-      tile_local(g, gcd, Tq, L);
+      const int v = (int)((fr >> (16 * d)) & 0xffffu);  // L, or kPk the global coordinate
       int code = load_code(a.xp, 3 * p + d, g.izipx);
       float tx;
       if (kPk) {
         float frac = __fmul_rn(pos_off_f(code, g.izipx), g.izipx == 1 ? 1.0f / 256.0f : 1.0f / 65536.0f);
         // the particle's own global frame, as the reference rounds it
-        float pos = __fadd_rn((float)gcd, frac);
+        float pos = __fadd_rn((float)v, frac);
         tx = __fsub_rn(__fdiv_rn(__fmul_rn(pos, (float)a.ng), (float)nc), 0.5f);
       } else {
-        tx = MPC == 1 ? coarse_tempx(L, code, g.izipx) : fine_tempx(MPC, L, code, g.izipx);
+        tx = MPC == 1 ? coarse_tempx(v, code, g.izipx) : fine_tempx(MPC, v, code, g.izipx);
       }
       float fl = floorf(tx);
       d1[d] = __fsub_rn(__fadd_rn(fl, 1.0f), tx);
       d2[d] = __fsub_rn(1.0f, d1[d]);
       // mesh index relative to the brick
       // (kPk: unwrap the ring cell's periodic image, then relative to the brick)
-      rel[d] = kPk ? (int)fl + MPC * (sl[d] - gcd) : MPC * sl[d] + (int)fl - MPC * (L - 1);
+      rel[d] = kPk ? (int)fl + MPC * (sl[d] - v) : MPC * sl[d] + (int)fl - MPC * (v - 1);
+      ok[d] = (unsigned)(rel[d] >= 0 && rel[d] < lim[d]) | ((unsigned)(rel[d] >= -1 && rel[d] + 1 < lim[d]) << 1);
     }
+    if (kAxis && !(ok[0] && ok[1] && ok[2])) return;  // the whole stencil lies outside the brick
+    // the reference's product order ((d_x * d_y) * d_z) * mass
+    float wxy[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) wxy[k] = kAxis ? __fmul_rn(k & 1 ? d2[0] : d1[0], k & 2 ? d2[1] : d1[1]) : 0.f;
+    const int e0 = rel[0] + MX * (rel[1] + MY * rel[2]);
 #pragma unroll
     for (int k = 0; k < 8; k++) {
-      int ox = k & 1, oy = (k >> 1) & 1, oz = k >> 2;
-      int x = rel[0] + ox, y = rel[1] + oy, z = rel[2] + oz;
-      if (x < 0 || y < 0 || z < 0 || x >= lim[0] || y >= lim[1] || z >= lim[2]) continue;
-      float w = __fmul_rn(__fmul_rn(__fmul_rn(ox ? d2[0] : d1[0], oy ? d2[1] : d1[1]), oz ? d2[2] : d1[2]), a.mass);
+      const int ox = k & 1, oy = (k >> 1) & 1, oz = k >> 2;
+      if (kAxis) {
+        if (!((ok[0] >> ox) & (ok[1] >> oy) & (ok[2] >> oz) & 1u)) continue;
+      } else {
+        const int x = rel[0] + ox, y = rel[1] + oy, z = rel[2] + oz;
+        if (x < 0 || y < 0 || z < 0 || x >= lim[0] || y >= lim[1] || z >= lim[2]) continue;
+      }
+      const float wxyk = kAxis ? wxy[k & 3] : __fmul_rn(ox ? d2[0] : d1[0], oy ? d2[1] : d1[1]);
+      float w = __fmul_rn(__fmul_rn(wxyk, oz ? d2[2] : d1[2]), a.mass);
       // w * 2^s (exact scaling, truncated) < 2^31; carry out of the low word
       const unsigned q = __float2uint_rz(__fmul_rn(w, a.qscale));
-      const int e = x + MX * (y + MY * z);
+      const int e = kAxis ? e0 + ox + MX * (oy + MY * oz) : (rel[0] + ox) + MX * ((rel[1] + oy) + MY * (rel[2] + oz));
       const unsigned old = atomicAdd(&acc[e], q);
       if (old + q < old) atomicAdd(&carry[e], 1u);
     }
