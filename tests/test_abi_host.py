@@ -39,16 +39,17 @@ def test_stats_struct_layout():
     assert CubeStats.npairs.offset % 8 == 0 and CubeStats.testrhof.offset % 8 == 0
 
 
-def test_cube_create_rejects_bad_sizes(built_lib):
+@pytest.mark.parametrize("nc,msg", [(14, b"at least 16"), (32768, b"at most 16384")])
+def test_cube_create_rejects_bad_sizes(built_lib, nc, msg):
     from cafproject_gb300 import cube
     L = cube.load_library()
-    bad = P.CubeParams(nc=14, nnt=1).to_c()
+    bad = P.CubeParams(nc=nc, nnt=1).to_c()
     fine, coarse = cube.force_tables()
     h = ctypes.c_void_p()
     rc = L.cube_create(ctypes.byref(bad), fine.ctypes.data_as(ctypes.c_void_p),
                        coarse.ctypes.data_as(ctypes.c_void_p), 0, ctypes.byref(h))
     assert rc == 1  # CUBE_ERR_ARG before any device call
-    assert b"at least 16" in L.cube_last_error(h)
+    assert msg in L.cube_last_error(h)
     L.cube_destroy(h)
 
 
