@@ -138,7 +138,12 @@ enum cube_field {
    tables (replaces initialize + kernel_f + kernel_c, initialize.f90:21-38,
    kernel_f.f90:14-37, kernel_c.f90:16-117).
    fine_table: fk_table(i,j,k,d), 16x16x16x3 float, Fortran order.
-   coarse_table: ck_table(d,i,j,k), 3x4x4x4 float, Fortran order. */
+   coarse_table: ck_table(d,i,j,k), 3x4x4x4 float, Fortran order.
+   Sizes rejected with CUBE_ERR_ARG before any device call (the message in
+   cube_last_error): nc outside 16..16384 or not a multiple of nnt, ncell
+   other than 4, izipx/izipv outside 1..2, nc/nnt below 2*ncb, ncb outside
+   1..8, nf_cutoff not below ncb*ncell, pp_range other than 1 with PP on,
+   np_max not positive. */
 int cube_create(const cube_params* p, const float* fine_table, const float* coarse_table, int device,
                 cube_ctx** out);
 int cube_destroy(cube_ctx* ctx);
