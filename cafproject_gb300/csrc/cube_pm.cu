@@ -107,7 +107,7 @@ __global__ void __launch_bounds__(256) k_deposit_det(DepArgs a) {
   constexpr int SX = BX + LO + HI, SY = BY + LO + HI, SZ = BZ + LO + HI;
   constexpr int NSRC = SX * SY * SZ;
   constexpr int MX = MPC * BX, MY = MPC * BY, MZ = MPC * BZ;
-  extern __shared__ unsigned acc[];  // low words [0, MX*MY*MZ), carry words after them
+  extern __shared__ __align__(16) unsigned acc[];  // low words [0, MX*MY*MZ), carry words after them
   unsigned* carry = acc + MX * MY * MZ;
   __shared__ int pref[NSRC];
   __shared__ long long sstart[NSRC];
@@ -127,7 +127,9 @@ __global__ void __launch_bounds__(256) k_deposit_det(DepArgs a) {
   int b = blockIdx.x;
   int C0[3] = {(b % nbx) * BX, ((b / nbx) % nby) * BY, (b / (nbx * nby)) * BZ};
   int B[3] = {min(BX, nc - C0[0]), min(BY, nc - C0[1]), min(BZ, nc - C0[2])};
-  for (int i = threadIdx.x; i < 2 * MX * MY * MZ; i += blockDim.x) acc[i] = 0u;
+  // 2*MX*MY*MZ is a multiple of 4: 16-byte stores
+  for (int i = 4 * threadIdx.x; i < 2 * MX * MY * MZ; i += 4 * blockDim.x)
+    *reinterpret_cast<uint4*>(acc + i) = make_uint4(0u, 0u, 0u, 0u);
   if (threadIdx.x == 0) btot = 0ull;
   // source cells, their particle counts and frames
   for (int t = threadIdx.x; t < NSRC; t += blockDim.x) {
@@ -208,15 +210,37 @@ __global__ void __launch_bounds__(256) k_deposit_det(DepArgs a) {
   });
   __syncthreads();
   unsigned long long mysum = 0;
-  for (int i = threadIdx.x; i < MX * MY * MZ; i += blockDim.x) {
-    int x = i % MX, y = (i / MX) % MY, z = i / (MX * MY);
-    if (x >= MPC * B[0] || y >= MPC * B[1] || z >= MPC * B[2]) continue;
-    const unsigned lo = acc[i], hi = carry[i];
-    mysum += ((unsigned long long)hi << 32) | lo;
-    // (hi*2^32 + lo) * 2^-s as float
-    float r = __fmaf_rn((float)lo, a.qinv, __fmul_rn((float)hi, __fmul_rn(a.qinv, 4294967296.0f)));
-    float* cell = a.rho + mesh_idx(n, MPC * C0[0] + x, MPC * C0[1] + y, MPC * C0[2] + z);
-    *cell = a.accumulate ? __fadd_rn(*cell, r) : r;
+  // (hi*2^32 + lo) * 2^-s as float
+  const float qhi = __fmul_rn(a.qinv, 4294967296.0f);
+  if (kAxis) {
+    // two neighbouring x cells a thread: MX and the brick's extent MPC*B[0]
+    // are multiples of 4, and n is even, so an even x starts an 8-byte
+    // aligned pair of the padded mesh (row stride n+2)
+    for (int i = 2 * threadIdx.x; i < MX * MY * MZ; i += 2 * blockDim.x) {
+      const int x = i % MX, y = (i / MX) % MY, z = i / (MX * MY);
+      if (x >= MPC * B[0] || y >= MPC * B[1] || z >= MPC * B[2]) continue;
+      const uint2 lo = *reinterpret_cast<const uint2*>(acc + i);
+      const uint2 hi = *reinterpret_cast<const uint2*>(carry + i);
+      mysum += (((unsigned long long)hi.x << 32) | lo.x) + (((unsigned long long)hi.y << 32) | lo.y);
+      float2 r = make_float2(__fmaf_rn((float)lo.x, a.qinv, __fmul_rn((float)hi.x, qhi)),
+                             __fmaf_rn((float)lo.y, a.qinv, __fmul_rn((float)hi.y, qhi)));
+      float2* cell = reinterpret_cast<float2*>(a.rho + mesh_idx(n, MPC * C0[0] + x, MPC * C0[1] + y, MPC * C0[2] + z));
+      if (a.accumulate) {
+        const float2 o = *cell;
+        r = make_float2(__fadd_rn(o.x, r.x), __fadd_rn(o.y, r.y));
+      }
+      *cell = r;
+    }
+  } else {
+    for (int i = threadIdx.x; i < MX * MY * MZ; i += blockDim.x) {
+      const int x = i % MX, y = (i / MX) % MY, z = i / (MX * MY);
+      if (x >= MPC * B[0] || y >= MPC * B[1] || z >= MPC * B[2]) continue;
+      const unsigned lo = acc[i], hi = carry[i];
+      mysum += ((unsigned long long)hi << 32) | lo;
+      float r = __fmaf_rn((float)lo, a.qinv, __fmul_rn((float)hi, qhi));
+      float* cell = a.rho + mesh_idx(n, MPC * C0[0] + x, MPC * C0[1] + y, MPC * C0[2] + z);
+      *cell = a.accumulate ? __fadd_rn(*cell, r) : r;
+    }
   }
   for (int o = 16; o > 0; o >>= 1) mysum += __shfl_xor_sync(0xffffffffu, mysum, o);
   if ((threadIdx.x & 31) == 0) atomicAdd(&btot, mysum);
