@@ -213,23 +213,37 @@ __global__ void __launch_bounds__(256) k_deposit_det(DepArgs a) {
   // (hi*2^32 + lo) * 2^-s as float
   const float qhi = __fmul_rn(a.qinv, 4294967296.0f);
   if (kAxis) {
-    // two neighbouring x cells a thread: MX and the brick's extent MPC*B[0]
-    // are multiples of 4, and n is even, so an even x starts an 8-byte
-    // aligned pair of the padded mesh (row stride n+2)
-    for (int i = 2 * threadIdx.x; i < MX * MY * MZ; i += 2 * blockDim.x) {
+    // KX neighbouring x cells a thread, written as KX/2 pairs: KX divides
+    // MPC, so MX and the brick's extent MPC*B[0] are multiples of KX, and n
+    // is even, so x starts an 8-byte aligned stretch of the padded mesh
+    // (row stride n+2)
+    constexpr int KX = MPC >= 4 ? 4 : 2;
+    for (int i = KX * threadIdx.x; i < MX * MY * MZ; i += KX * blockDim.x) {
       const int x = i % MX, y = (i / MX) % MY, z = i / (MX * MY);
       if (x >= MPC * B[0] || y >= MPC * B[1] || z >= MPC * B[2]) continue;
-      const uint2 lo = *reinterpret_cast<const uint2*>(acc + i);
-      const uint2 hi = *reinterpret_cast<const uint2*>(carry + i);
-      mysum += (((unsigned long long)hi.x << 32) | lo.x) + (((unsigned long long)hi.y << 32) | lo.y);
-      float2 r = make_float2(__fmaf_rn((float)lo.x, a.qinv, __fmul_rn((float)hi.x, qhi)),
-                             __fmaf_rn((float)lo.y, a.qinv, __fmul_rn((float)hi.y, qhi)));
-      float2* cell = reinterpret_cast<float2*>(a.rho + mesh_idx(n, MPC * C0[0] + x, MPC * C0[1] + y, MPC * C0[2] + z));
-      if (a.accumulate) {
-        const float2 o = *cell;
-        r = make_float2(__fadd_rn(o.x, r.x), __fadd_rn(o.y, r.y));
+      unsigned lo[KX], hi[KX];
+      if constexpr (KX == 4) {
+        const uint4 l = *reinterpret_cast<const uint4*>(acc + i), h = *reinterpret_cast<const uint4*>(carry + i);
+        lo[0] = l.x, lo[1] = l.y, lo[2] = l.z, lo[3] = l.w;
+        hi[0] = h.x, hi[1] = h.y, hi[2] = h.z, hi[3] = h.w;
+      } else {
+        const uint2 l = *reinterpret_cast<const uint2*>(acc + i), h = *reinterpret_cast<const uint2*>(carry + i);
+        lo[0] = l.x, lo[1] = l.y;
+        hi[0] = h.x, hi[1] = h.y;
       }
-      *cell = r;
+      float2* cell = reinterpret_cast<float2*>(a.rho + mesh_idx(n, MPC * C0[0] + x, MPC * C0[1] + y, MPC * C0[2] + z));
+#pragma unroll
+      for (int q = 0; q < KX / 2; q++) {
+        mysum += (((unsigned long long)hi[2 * q] << 32) | lo[2 * q]) +
+                 (((unsigned long long)hi[2 * q + 1] << 32) | lo[2 * q + 1]);
+        float2 r = make_float2(__fmaf_rn((float)lo[2 * q], a.qinv, __fmul_rn((float)hi[2 * q], qhi)),
+                               __fmaf_rn((float)lo[2 * q + 1], a.qinv, __fmul_rn((float)hi[2 * q + 1], qhi)));
+        if (a.accumulate) {
+          const float2 o = cell[q];
+          r = make_float2(__fadd_rn(o.x, r.x), __fadd_rn(o.y, r.y));
+        }
+        cell[q] = r;
+      }
     }
   } else {
     for (int i = threadIdx.x; i < MX * MY * MZ; i += blockDim.x) {
