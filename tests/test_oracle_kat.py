@@ -3,7 +3,6 @@
 The reference ships no golden vectors for this path, so each test checks one
 documented behaviour of the Fortran loops with an answer derived by hand.
 """
-import ctypes
 
 import numpy as np
 import pytest
